@@ -1,0 +1,305 @@
+"""Benchmark of the fv3d hydro step on GB300.
+
+Workload (one JSON line): the plain FP64 Rayleigh-Taylor configuration,
+512 x 1536 cells in the x-z plane, HLL, PLM, RK2, CFL 0.8, gravity -0.1,
+periodic x / reflecting z (seeded synthetic initial state).  One step = one
+RK2 step of the whole grid: the control kernel (CFL dt from the reduction
+fused into the previous step), stage 1 and stage 2.
+
+  value     Mcell-updates/s with the state resident in HBM, CUDA events on
+            the library's stream around each step, L2 flushed (256 MiB
+            write) between timed steps because the state fits in L2.
+  e2e       the same metric through the C ABI with host buffers: per step
+            set_prim from pinned host arrays, the step, get_prim back.
+  roofline  the stage kernels (dominant) against measured HBM bandwidth:
+            algorithmic bytes 5 state passes x 4 fields x 8 B = 160 B per
+            cell-update, over their CUDA-event durations.
+  cpu_baseline  the CPU oracle port of the reference algorithm on all host
+            cores, a bounded sample of the same workload.
+
+--impl reference times the reference's CPU implementation of the path
+(oracle/_ref when it is loadable here, else the C port of it) on the same
+workload and prints the same line with "impl": "reference".
+
+Multi-GPU (torchrun, one rank per GPU): independent replicas, no collective
+on the data path; value = total cell-updates of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-updates/s: FP64 plain vs mixed/batched at stated L1 err; HBM % of peak"
+UNIT = "Mcell-updates/s"
+WORKLOAD = "rayleigh_taylor_512x1536_fp64"
+ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2-D)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def problem():
+    from fv3d_gb300 import problems
+    return problems.rayleigh_taylor(512, 1536)
+
+
+def config_dict(pr, l2):
+    return {"workload": WORKLOAD, "cells": pr.cells, "grid": [pr.params.Nx, pr.params.Nz],
+            "riemann": "hll", "reconstruction": "plm", "time_stepping": "rk2", "precision": "fp64",
+            "l2": l2, "parallelism": "replicas"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self, gpu_index=0):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(gpu_index)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(pr, seconds=15.0, max_steps=20, use_ref=False):
+    """Time the CPU reference path on the same workload (all host cores)."""
+    from oracle import pyoracle
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    kind = "port"
+    if use_ref:
+        try:
+            path = os.path.join(tempfile.mkdtemp(), "bench.ini")
+            with open(path, "w") as f:
+                f.write(pr.ini)
+            o = pyoracle.RefOracle(path)
+            kind = "reference"
+        except Exception:
+            o = pyoracle.Oracle(pr.params)
+    else:
+        o = pyoracle.Oracle(pr.params)
+    o.set_prim(*pr.prim)
+    o.step(o.compute_dt())  # warm-up (first touch)
+    n, t0 = 0, time.perf_counter()
+    while n < max_steps and (n == 0 or time.perf_counter() - t0 < seconds):
+        o.step(o.compute_dt())
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": pr.cells * n / el / 1e6, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d RK2 steps (dt each step) of %s on %d threads, %.2f s" % (n, WORKLOAD, threads, el)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    pr = problem()
+    from oracle import pyoracle
+    use_ref = pyoracle.reference_available()
+    per_step = []
+    base = None
+    for _ in range(args.warmup):
+        cpu_sample(pr, seconds=0.0, max_steps=1, use_ref=use_ref)
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r = cpu_sample(pr, seconds=0.0, max_steps=1, use_ref=use_ref)
+        per_step.append(pr.cells / (r["value"] * 1e6) * 1e3)
+        base = r
+    value = pr.cells * args.steps / (sum(per_step) / 1e3) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(per_step)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": config_dict(pr, "n/a (CPU)"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
+                             "sample": "%d timed RK2 steps of %s on %d threads" % (args.steps, WORKLOAD,
+                                                                                   base["cores"])},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_all}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import fv3d_gb300 as fv
+
+    world, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pr = problem()
+    sim = fv.Simulation(pr.params)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.set_prim(*pr.prim)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+
+    for _ in range(args.warmup):
+        sim.enqueue_steps(1)
+    sim.synchronize()
+    launches0 = sim.launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else tempfile.mkdtemp(),
+                              "bench_clocks.csv"))
+    with clk:
+        for k in range(args.steps):
+            flush_l2()
+            evs[k][0].record(stream)
+            sim.enqueue_steps(1)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    launches = sim.launch_count() - launches0
+    ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = pr.cells * args.steps * world / (total_ms / 1e3) / 1e6
+    sim.get_prim()  # surfaces any error of the timed steps
+
+    # Dominant kernel: per-launch CUDA events (profile mode), L2 flushed per step.
+    sim.profile(True)
+    nprof = max(4, min(args.steps, 20))
+    for _ in range(nprof):
+        flush_l2()
+        sim.enqueue_steps(1)
+    kt = sim.kernel_times()
+    sim.profile(False)
+    stage_n, stage_ms = kt["stage"]
+    ms_per_step_stages = stage_ms / (stage_n / 2.0)
+    hbm_peak, peak_kind = peaks()
+    achieved = ALGO_BYTES_PER_CELL_UPDATE * pr.cells / (ms_per_step_stages / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "stage2d_fp64 (RK2 stages 1+2)", "achieved": achieved,
+                "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "algo_bytes_per_cell_update": ALGO_BYTES_PER_CELL_UPDATE,
+                "stage_ms_per_launch": stage_ms / stage_n, "dt_kernel_ms_per_launch": kt["dt"][1] / max(kt["dt"][0], 1)}
+
+    # e2e through the C ABI with pinned host buffers
+    host_in = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in pr.prim]
+    host_in[2] = None  # v is identically zero in the x-z plane
+    host_out = [torch.empty(pr.shape, dtype=torch.float64).pin_memory() for _ in range(5)]
+    np_in = [None if a is None else a.numpy() for a in host_in]
+    np_out = [a.numpy() for a in host_out]
+    for _ in range(2):
+        sim.set_prim(*np_in)
+        sim.enqueue_steps(1)
+        sim.get_prim(out=np_out)
+    e2e_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        sim.set_prim(*np_in)
+        sim.enqueue_steps(1)
+        sim.get_prim(out=np_out)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    h2d = sum(a.numel() * 8 for a in host_in if a is not None)
+    d2h = sum(a.numel() * 8 for a in host_out)
+    e2e = {"value": pr.cells * world / (float(np.mean(e2e_ms)) / 1e3) / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": float(np.mean(e2e_ms))}
+
+    # one-step parity against the oracle on the same state (stated L1 error)
+    from oracle import pyoracle
+    from fv3d_gb300 import problems
+    chk = problems.rayleigh_taylor(512, 1536)
+    o = pyoracle.Oracle(chk.params)
+    o.set_prim(*chk.prim)
+    g = fv.Simulation(chk.params)
+    g.set_prim(*chk.prim)
+    dt = o.compute_dt()
+    o.step(dt)
+    g.step(dt)
+    l1 = []
+    for a, b in zip(g.get_prim(), o.get_prim()):
+        den = float(np.abs(b).sum())
+        l1.append(float(np.abs(a - b).sum()) / den if den else 0.0)
+    g.close()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config_dict(pr, "flushed (256 MiB write between timed steps)"),
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(local),
+            "rel_l1_vs_oracle_one_step": dict(zip(["rho", "u", "v", "w", "p"], l1))}
+    if rank == 0:
+        line["cpu_baseline"] = cpu_sample(pr)
+        print(json.dumps(line))
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

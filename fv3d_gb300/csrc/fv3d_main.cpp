@@ -1,0 +1,193 @@
+// fv3d_main.cpp -- command-line driver, the counterpart of the reference's
+// main.cpp (main.cpp:12-89) on the GB300 path.
+//
+//   fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]
+//
+// Reads the same .ini file (readInifile semantics), sets the initial state,
+// and runs the reference's time loop: while (t + epsilon < tend) { dt =
+// computeDt; log every log_frequency steps; save when due; update; t += dt }.
+// The problem generators of Init.h that need no random numbers are provided
+// (sod_x, sod_y, sod_z, blast, diffusion, rayleigh-taylor); any other initial
+// state is read with --ic from a raw file of 5 float64 arrays (rho, u, v, w,
+// p), each Nz*Ny*Nx in C order.  Snapshots are written as the same raw
+// format (<prefix>_<ite>.bin) instead of HDF5.
+//
+// --device-loop runs the steps between two saves with fvgpu_advance (dt stays
+// on the GPU) instead of one compute_dt/step round trip per step.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fv3d_gb300.h"
+
+namespace {
+
+struct Fields {
+  std::vector<double> f[5];
+};
+
+double PosX(const fv_params& p, int i) { return p.xmin + (i + 0.5) * p.dx; }
+double PosY(const fv_params& p, int j) { return p.ymin + (j + 0.5) * p.dy; }
+double PosZ(const fv_params& p, int k) { return p.zmin + (k + 0.5) * p.dz; }
+
+// Init.h:18-99, 150-209 on the interior cells.
+bool Generate(const fv_params& p, Fields& q) {
+  const std::string prob = p.problem;
+  const size_t n = (size_t)p.Nx * p.Ny * p.Nz;
+  for (auto& a : q.f) a.assign(n, 0.0);
+  for (int k = 0; k < p.Nz; ++k)
+    for (int j = 0; j < p.Ny; ++j)
+      for (int i = 0; i < p.Nx; ++i) {
+        const size_t c = ((size_t)k * p.Ny + j) * p.Nx + i;
+        const double x = PosX(p, i), y = PosY(p, j), z = PosZ(p, k);
+        double r = 0, u = 0, v = 0, w = 0, pr = 0;
+        if (prob == "sod_x" || prob == "sod_y" || prob == "sod_z") {
+          const double s = prob == "sod_x" ? x : prob == "sod_y" ? y : z;
+          r = s <= 0.5 ? 1.0 : 0.125;
+          pr = s <= 0.5 ? 1.0 : 0.1;
+        } else if (prob == "blast") {
+          const double xr = 0.5 * (p.xmin + p.xmax) - x, yr = 0.5 * (p.ymin + p.ymax) - y,
+                       zr = 0.5 * (p.zmin + p.zmax) - z;
+          const double rr = std::sqrt(xr * xr + yr * yr + zr * zr);
+          r = rr < 0.2 ? 1.0 : 1.2;
+          pr = rr < 0.2 ? 10.0 : 0.1;
+        } else if (prob == "diffusion") {
+          const double x0 = x - 0.5 * (p.xmin + p.xmax), y0 = y - 0.5 * (p.ymin + p.ymax),
+                       z0 = z - 0.5 * (p.zmin + p.zmax);
+          const double rr = std::sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+          r = rr < 0.2 ? 1.0 : 0.1;
+          pr = 1.0;
+          u = v = w = 1.0;
+        } else if (prob == "rayleigh-taylor") {
+          const double zmid = 0.5 * (p.zmin + p.zmax);
+          r = z < zmid ? 1.0 : 2.0;
+          pr = 2.5 + 0.1 * p.g * z;
+          if (z > -1.0 / 3.0 && z < 1.0 / 3.0)
+            w = 0.01 * (1.0 + std::cos(4 * M_PI * x)) * (1.0 + std::cos(4.0 * M_PI * y)) *
+                (1 + std::cos(3.0 * M_PI * z)) / 4.0;
+        } else {
+          return false;
+        }
+        q.f[0][c] = r;
+        q.f[1][c] = u;
+        q.f[2][c] = v;
+        q.f[3][c] = w;
+        q.f[4][c] = pr;
+      }
+  return true;
+}
+
+bool ReadRaw(const std::string& path, size_t n, Fields& q) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  bool ok = true;
+  for (auto& a : q.f) {
+    a.resize(n);
+    ok = ok && std::fread(a.data(), sizeof(double), n, f) == n;
+  }
+  std::fclose(f);
+  return ok;
+}
+
+bool WriteRaw(const std::string& path, const Fields& q) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return false;
+  bool ok = true;
+  for (const auto& a : q.f) ok = ok && std::fwrite(a.data(), sizeof(double), a.size(), f) == a.size();
+  std::fclose(f);
+  return ok;
+}
+
+int Check(fv_sim* s, int rc, const char* what) {
+  if (rc != FV_OK) std::fprintf(stderr, "%s: %s (%s)\n", what, fv_status_string(rc), fvgpu_last_error(s));
+  return rc;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    std::fprintf(stderr, "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]\n");
+    return 2;
+  }
+  std::string ini = argv[1], ic, out;
+  bool device_loop = false;
+  for (int a = 2; a < argc; ++a) {
+    if (!std::strcmp(argv[a], "--ic") && a + 1 < argc) ic = argv[++a];
+    else if (!std::strcmp(argv[a], "--out") && a + 1 < argc) out = argv[++a];
+    else if (!std::strcmp(argv[a], "--device-loop")) device_loop = true;
+    else {
+      std::fprintf(stderr, "unknown argument %s\n", argv[a]);
+      return 2;
+    }
+  }
+  fv_params p;
+  fv_read_ini(ini.c_str(), &p);
+  if (out.empty()) out = p.filename_out;
+  const size_t n = (size_t)p.Nx * p.Ny * p.Nz;
+  Fields q;
+  if (!ic.empty()) {
+    if (!ReadRaw(ic, n, q)) {
+      std::fprintf(stderr, "cannot read %zu cells from %s\n", n, ic.c_str());
+      return 1;
+    }
+  } else if (!Generate(p, q)) {
+    std::fprintf(stderr, "Error unknown problem %s (give --ic)\n", p.problem);
+    return 1;
+  }
+  fv_sim* s = nullptr;
+  if (Check(s, fvgpu_create(&p, &s), "fvgpu_create")) return 1;
+  if (Check(s, fvgpu_set_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data()),
+            "set_prim"))
+    return 1;
+
+  double t = 0.0, dt = 0.0, next_save = 0.0;
+  int ite = 0, next_log = 0;
+  long steps = 0;
+  auto save = [&](double tt) {
+    fvgpu_get_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data());
+    char name[512];
+    std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite++);
+    std::printf(" - Saving at time %g\n", tt);
+    WriteRaw(name, q);
+  };
+  while (t + p.epsilon < p.tend) {
+    const bool save_needed = (t + p.epsilon > next_save);
+    double inv[3];
+    if (Check(s, fvgpu_compute_dt(s, &dt, inv), "compute_dt")) return 1;
+    if (next_log == 0) {
+      std::printf("Computing dts at (t=%g) : dt_hyp=%g; dt_TC=%g; dt_visc=%g\n", t, 1.0 / inv[0], 1.0 / inv[1],
+                  1.0 / inv[2]);
+      next_log = p.log_frequency;
+    } else {
+      next_log--;
+    }
+    if (save_needed) {
+      save(t);
+      next_save += p.save_freq;
+    }
+    if (device_loop) {
+      // run on the device up to the next save time (or tend)
+      long k = 0;
+      const double bound = std::fmin(p.tend, next_save);
+      if (Check(s, fvgpu_advance(s, bound, 0, &t, &k), "advance")) return 1;
+      steps += k;
+      if (k == 0) {  // next_save within epsilon: take one ordinary step
+        if (Check(s, fvgpu_step(s, dt), "step")) return 1;
+        t += dt;
+        ++steps;
+      }
+    } else {
+      if (Check(s, fvgpu_step(s, dt), "step")) return 1;
+      t += dt;
+      ++steps;
+    }
+  }
+  save(t);
+  std::printf("done: %ld steps, t = %.17g\n", steps, t);
+  fvgpu_destroy(s);
+  return 0;
+}

@@ -1,0 +1,638 @@
+// fv_api.cpp -- extern "C" entry points for one problem (fvgpu_*).
+//
+// Host-side runtime of the drop-in: owns the device state of one problem,
+// orders all work on one CUDA stream, and drives the fused stage kernels.
+// The reference's time loop (main.cpp:51-74) runs on the device: a control
+// kernel turns the max reduced by the previous step into dt, decides whether
+// the step is active (t + epsilon < tend), and the stage kernels follow;
+// fvgpu_advance replays a captured CUDA graph of several such steps and only
+// reads the control block back between replays.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fv3d_gb300.h"
+#include "fv_kernels.h"
+
+using fv::Fields;
+using fv::Grid2D;
+using fv::StepCtrl;
+
+namespace {
+
+constexpr int kGraphSteps = 8;     // steps per captured graph replay
+constexpr int kMaxTotalsBlocks = 1024;
+
+enum KernelClass { KC_STAGE = 0, KC_DT = 1, KC_CONV = 2 };
+
+}  // namespace
+
+struct fv_sim {
+  fv_params p{};
+  Grid2D G{};
+  bool wact = false;          // third momentum component carried
+  int deg_bc = FV_BC_PERIODIC;
+  double* buf = nullptr;      // 3 states x 5 fields x fstride doubles
+  Fields A{}, B{}, S{};       // A: state, B: U* / ping-pong, S: scratch
+  int cur = 0;                // Euler ping-pong: state in A (0) or B (1)
+  StepCtrl* d_ctrl = nullptr;
+  StepCtrl* h_ctrl = nullptr; // pinned mirror (read after synchronisation only)
+  double* d_partial = nullptr;
+  double* h_partial = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  long long step = 0;         // mirror of ctrl->step
+  bool slot_valid = false;    // ctrl->slot[step & 1] reduces the current state
+  bool state_set = false;
+  double inv_tc = 0.0, inv_visc = 0.0;
+  std::string err;
+  long launches = 0;
+  bool profile = false;
+  long prof_count[3] = {0, 0, 0};
+  double prof_ms[3] = {0, 0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  const void* graph_key = nullptr;
+  cudaStream_t graph_stream = nullptr;
+};
+
+namespace {
+
+int Fail(fv_sim* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  return code;
+}
+
+#define CUDA_TRY(s, call)                                                                  \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return Fail((s), FV_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+  } while (0)
+
+// Cell sizes and loop constants of ComputeDt.h:36-47 (constant kappa / mu).
+void DtConstants(const fv_params& p, double* inv_tc, double* inv_visc) {
+  *inv_tc = p.epsilon;
+  if (p.thermal_conductivity_active)
+    *inv_tc = std::fmax(std::fmax(2.0 * p.kappa / (p.dx * p.dx), 2.0 * p.kappa / (p.dy * p.dy)),
+                        2.0 * p.kappa / (p.dz * p.dz));
+  *inv_visc = p.epsilon;
+  if (p.viscosity_active)
+    *inv_visc = std::fmax(std::fmax(2.0 * p.mu / (p.dx * p.dx), 2.0 * p.mu / (p.dy * p.dy)),
+                          2.0 * p.mu / (p.dz * p.dz));
+}
+
+int DevBC(int bc) { return bc == FV_BC_ABSORBING ? fv::DBC_ABSORBING : bc == FV_BC_REFLECTING ? fv::DBC_REFLECTING : fv::DBC_PERIODIC; }
+
+// Checks that the parameter set is one this build runs and fills the grid.
+int Configure(fv_sim* s) {
+  const fv_params& p = s->p;
+  if (p.Nx < 1 || p.Ny < 1 || p.Nz < 1) return Fail(s, FV_ERR_PARAM, "Nx, Ny, Nz must be >= 1");
+  if (p.Ng < 2) return Fail(s, FV_ERR_PARAM, "Nghosts must be >= 2 (slopes read two cells out)");
+  if (!(p.dx > 0 && p.dy > 0 && p.dz > 0)) return Fail(s, FV_ERR_PARAM, "cell sizes must be positive");
+  if (!(p.gamma0 > 1.0)) return Fail(s, FV_ERR_PARAM, "gamma0 must be > 1");
+  if (p.precision != FV_PREC_FP64)
+    return Fail(s, FV_ERR_UNSUPPORTED, "fvgpu_create runs the FP64 form; the FP32-mixed form is batch-only");
+  Grid2D& G = s->G;
+  int plane;
+  if (p.Nz == 1 && p.Ny >= 2 && p.Nx >= 2) {
+    plane = fv::PLANE_XY;
+    s->deg_bc = p.boundary_z;
+  } else if (p.Ny == 1 && p.Nz >= 2 && p.Nx >= 2) {
+    plane = fv::PLANE_XZ;
+    s->deg_bc = p.boundary_y;
+  } else {
+    return Fail(s, FV_ERR_UNSUPPORTED, "only 2-D runs (Nz == 1 or Ny == 1, other axes >= 2) are built");
+  }
+  if (plane == fv::PLANE_XY && p.gravity)
+    return Fail(s, FV_ERR_UNSUPPORTED, "gravity acts along z only (Update.h:148); use the x-z plane (Ny = 1)");
+  if (p.well_balanced_flux_at_z_bc) return Fail(s, FV_ERR_UNSUPPORTED, "well_balanced_flux_at_z_bc is not built");
+  if (p.boundary_z == FV_BC_C91) return Fail(s, FV_ERR_UNSUPPORTED, "the C91 z boundary is not built");
+  if (p.thermal_conductivity_active && p.thermal_conductivity_mode != FV_TCM_CONSTANT)
+    return Fail(s, FV_ERR_UNSUPPORTED, "only constant thermal conductivity is built");
+  if (p.thermal_conductivity_active && (p.bctc_zmin != FV_BCTC_NONE || p.bctc_zmax != FV_BCTC_NONE))
+    return Fail(s, FV_ERR_UNSUPPORTED, "fixed-temperature/gradient z boundaries of conduction are not built");
+  if (p.viscosity_active && s->deg_bc == FV_BC_REFLECTING)
+    return Fail(s, FV_ERR_UNSUPPORTED, "viscosity with a reflecting degenerate axis is not built");
+
+  G.plane = plane;
+  G.na = p.Nx;
+  G.nb = plane == fv::PLANE_XY ? p.Ny : p.Nz;
+  G.pitch = (G.na + 15) / 16 * 16;  // 128-byte rows
+  G.fstride = ((long long)G.pitch * G.nb + 31) / 32 * 32;
+  G.bc_a = DevBC(p.boundary_x);
+  G.bc_b = DevBC(plane == fv::PLANE_XY ? p.boundary_y : p.boundary_z);
+  G.recon = p.reconstruction;
+  G.gravity = p.gravity ? 1 : 0;
+  G.tc = p.thermal_conductivity_active ? 1 : 0;
+  G.visc = p.viscosity_active ? 1 : 0;
+  G.dx = p.dx;
+  G.dy = p.dy;
+  G.dz = p.dz;
+  G.da = p.dx;
+  G.db = plane == fv::PLANE_XY ? p.dy : p.dz;
+  G.dc = plane == fv::PLANE_XY ? p.dz : p.dy;
+  G.gamma = p.gamma0;
+  G.g = p.g;
+  G.kappa = p.kappa;
+  G.mu = p.mu;
+  DtConstants(p, &s->inv_tc, &s->inv_visc);
+  return FV_OK;
+}
+
+Fields StateAt(double* base, long long fstride) {
+  Fields f;
+  for (int v = 0; v < 5; ++v) f.f[v] = base + v * fstride;
+  return f;
+}
+
+// Storage slot of each reference field (rho, u|mx, v|my, w|mz, p|E).
+void StorageOrder(int plane, int slot_of[5]) {
+  slot_of[0] = 0;
+  slot_of[1] = 1;
+  slot_of[2] = plane == fv::PLANE_XY ? 2 : 3;
+  slot_of[3] = plane == fv::PLANE_XY ? 3 : 2;
+  slot_of[4] = 4;
+}
+
+const Fields& Current(const fv_sim* s) { return s->cur == 0 ? s->A : s->B; }
+
+struct Timed {
+  fv_sim* s;
+  int cls;
+  Timed(fv_sim* s_, int cls_) : s(s_), cls(cls_) {
+    if (s->profile) cudaEventRecord(s->ev0, s->stream);
+  }
+  void done() {
+    s->launches += 1;
+    if (s->profile) {
+      cudaEventRecord(s->ev1, s->stream);
+      cudaEventSynchronize(s->ev1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+      s->prof_ms[cls] += ms;
+      s->prof_count[cls] += 1;
+    }
+  }
+};
+
+enum StepMode { STEP_LOOP = -1, STEP_GIVEN_DT = 0, STEP_FIXED = 2 };
+
+// Launches the kernels of one time step (control + stages) on the stream.
+// STEP_GIVEN_DT uses the host-supplied dt; STEP_LOOP derives dt from the CFL
+// reduction and stops at the loop bound; STEP_FIXED derives dt with no bound.
+int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
+  {
+    Timed t(s, KC_DT);
+    cudaError_t e = fv::launch_control(s->d_ctrl, 1, mode, dt, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "control launch: %s", cudaGetErrorString(e));
+    if (counting) t.done();
+  }
+  const int rs = s->p.riemann_solver == FV_HLL ? 0 : 1;
+  if (s->p.time_stepping == FV_TS_RK2) {
+    {
+      Timed t(s, KC_STAGE);
+      cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream);
+      if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 1 launch: %s", cudaGetErrorString(e));
+      if (counting) t.done();
+    }
+    {
+      Timed t(s, KC_STAGE);
+      cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream);
+      if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 2 launch: %s", cudaGetErrorString(e));
+      if (counting) t.done();
+    }
+  } else {
+    Timed t(s, KC_STAGE);
+    const Fields& in = Current(s);
+    const Fields& out = s->cur == 0 ? s->B : s->A;
+    cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "euler stage launch: %s", cudaGetErrorString(e));
+    if (counting) t.done();
+    s->cur ^= 1;
+  }
+  return FV_OK;
+}
+
+int KernelsPerStep(const fv_sim* s) { return s->p.time_stepping == FV_TS_RK2 ? 3 : 2; }
+
+// Writes fields of the control block from the host (stream-ordered).
+int SetCtrl(fv_sim* s, const StepCtrl& c) {
+  CUDA_TRY(s, cudaMemcpyAsync(s->d_ctrl, &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return FV_OK;
+}
+
+int ReadCtrl(fv_sim* s) {
+  CUDA_TRY(s, cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(StepCtrl), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return FV_OK;
+}
+
+// Makes ctrl->slot[step & 1] hold max inv_dt_hyp of the current state.
+int EnsureSlot(fv_sim* s) {
+  if (s->slot_valid) return FV_OK;
+  const int slot = (int)(s->step & 1);
+  CUDA_TRY(s, cudaMemsetAsync(&s->d_ctrl->slot[slot], 0, sizeof(unsigned long long), s->stream));
+  Timed t(s, KC_DT);
+  cudaError_t e = fv::launch_reduce2d(s->G, s->wact, Current(s), s->d_ctrl, slot, s->stream);
+  if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "dt reduction launch: %s", cudaGetErrorString(e));
+  t.done();
+  s->slot_valid = true;
+  return FV_OK;
+}
+
+void ResetGraph(fv_sim* s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  s->graph_key = nullptr;
+}
+
+int CopyIn(fv_sim* s, const Fields& dst, const double* const src[5], bool zero_missing) {
+  const size_t rowb = (size_t)s->G.na * sizeof(double);
+  for (int v = 0; v < 5; ++v) {
+    if (src[v]) {
+      CUDA_TRY(s, cudaMemcpy2DAsync(dst.f[v], (size_t)s->G.pitch * sizeof(double), src[v], rowb, rowb, s->G.nb,
+                                    cudaMemcpyHostToDevice, s->stream));
+    } else if (zero_missing) {
+      CUDA_TRY(s, cudaMemsetAsync(dst.f[v], 0, (size_t)s->G.fstride * sizeof(double), s->stream));
+    }
+  }
+  return FV_OK;
+}
+
+int CopyOut(fv_sim* s, const Fields& src, double* const dst[5]) {
+  const size_t rowb = (size_t)s->G.na * sizeof(double);
+  for (int v = 0; v < 5; ++v) {
+    if (!dst[v]) continue;
+    CUDA_TRY(s, cudaMemcpy2DAsync(dst[v], rowb, src.f[v], (size_t)s->G.pitch * sizeof(double), rowb, s->G.nb,
+                                  cudaMemcpyDeviceToHost, s->stream));
+  }
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return FV_OK;
+}
+
+bool AnyNonzero(const double* a, long long n) {
+  if (!a) return false;
+  for (long long i = 0; i < n; ++i)
+    if (a[i] != 0.0) return true;
+  return false;
+}
+
+int SetState(fv_sim* s, const double* const ref_fields[5], bool prim) {
+  if (!s) return FV_ERR_PARAM;
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  const double* src[5];
+  for (int v = 0; v < 5; ++v) src[slot_of[v]] = ref_fields[v];
+  if (!src[0] || !src[4]) return Fail(s, FV_ERR_PARAM, "density and pressure/energy arrays are required");
+  const long long ncell = (long long)s->G.na * s->G.nb;
+  s->wact = s->p.viscosity_active || AnyNonzero(src[3], ncell);
+  if (s->wact && s->deg_bc == FV_BC_REFLECTING)
+    return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  ResetGraph(s);
+  s->cur = 0;
+  int rc = CopyIn(s, s->A, src, true);
+  if (rc) return rc;
+  if (prim) {
+    Timed t(s, KC_CONV);
+    cudaError_t e = fv::launch_prim_to_cons2d(s->G, s->A, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "primToCons launch: %s", cudaGetErrorString(e));
+    t.done();
+  }
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  s->slot_valid = false;
+  s->state_set = true;
+  return FV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fvgpu_create(const fv_params* params, fv_sim** out) {
+  if (!params || !out) return FV_ERR_PARAM;
+  *out = nullptr;
+  fv_sim* s = new fv_sim();
+  s->p = *params;
+  int rc = Configure(s);
+  if (rc != FV_OK) {
+    // keep the handle so the caller can read the message, but mark it unusable
+    *out = s;
+    s->state_set = false;
+    s->buf = nullptr;
+    return rc;
+  }
+  const size_t bytes = (size_t)3 * 5 * s->G.fstride * sizeof(double);
+  if (cudaMalloc(&s->buf, bytes) != cudaSuccess) {
+    *out = s;
+    return Fail(s, FV_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
+  }
+  cudaMemset(s->buf, 0, bytes);
+  s->A = StateAt(s->buf, s->G.fstride);
+  s->B = StateAt(s->buf + 5 * s->G.fstride, s->G.fstride);
+  s->S = StateAt(s->buf + 10 * s->G.fstride, s->G.fstride);
+  if (cudaMalloc(&s->d_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
+      cudaMallocHost(&s->h_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
+      cudaMalloc(&s->d_partial, kMaxTotalsBlocks * 10 * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&s->h_partial, kMaxTotalsBlocks * 10 * sizeof(double)) != cudaSuccess) {
+    *out = s;
+    return Fail(s, FV_ERR_NOMEM, "control block allocation failed");
+  }
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
+    *out = s;
+    return Fail(s, FV_ERR_CUDA, "stream/event creation failed");
+  }
+  s->stream = s->own_stream;
+  StepCtrl c{};
+  c.cfl = s->p.CFL;
+  c.inv_tc = s->inv_tc;
+  c.inv_visc = s->inv_visc;
+  c.epsilon = s->p.epsilon;
+  c.mode = 1;
+  rc = SetCtrl(s, c);
+  *out = s;
+  return rc;
+}
+
+int fvgpu_destroy(fv_sim* s) {
+  if (!s) return FV_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  ResetGraph(s);
+  if (s->buf) cudaFree(s->buf);
+  if (s->d_ctrl) cudaFree(s->d_ctrl);
+  if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+  if (s->d_partial) cudaFree(s->d_partial);
+  if (s->h_partial) cudaFreeHost(s->h_partial);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return FV_OK;
+}
+
+const char* fvgpu_last_error(const fv_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+int fvgpu_set_prim(fv_sim* s, const double* rho, const double* u, const double* v, const double* w,
+                   const double* p) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  const double* f[5] = {rho, u, v, w, p};
+  return SetState(s, f, true);
+}
+
+int fvgpu_set_cons(fv_sim* s, const double* rho, const double* mx, const double* my, const double* mz,
+                   const double* E) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  const double* f[5] = {rho, mx, my, mz, E};
+  return SetState(s, f, false);
+}
+
+int fvgpu_get_prim(fv_sim* s, double* rho, double* u, double* v, double* w, double* p) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  double* ref[5] = {rho, u, v, w, p};
+  double* dst[5];
+  for (int k = 0; k < 5; ++k) dst[slot_of[k]] = ref[k];
+  {
+    Timed t(s, KC_CONV);
+    cudaError_t e = fv::launch_cons_to_prim2d(s->G, Current(s), s->S, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "consToPrim launch: %s", cudaGetErrorString(e));
+    t.done();
+  }
+  if (!s->wact) {
+    CUDA_TRY(s, cudaMemsetAsync(s->S.f[3], 0, (size_t)s->G.fstride * sizeof(double), s->stream));
+  }
+  return CopyOut(s, s->S, dst);
+}
+
+int fvgpu_get_cons(fv_sim* s, double* rho, double* mx, double* my, double* mz, double* E) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  double* ref[5] = {rho, mx, my, mz, E};
+  double* dst[5];
+  for (int k = 0; k < 5; ++k) dst[slot_of[k]] = ref[k];
+  if (!s->wact) {
+    // the third momentum is identically zero and not stored by the stages
+    if (dst[3]) std::memset(dst[3], 0, sizeof(double) * (size_t)s->G.na * s->G.nb);
+    dst[3] = nullptr;
+  }
+  return CopyOut(s, Current(s), dst);
+}
+
+int fvgpu_compute_dt(fv_sim* s, double* dt, double inv[3]) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  int rc = EnsureSlot(s);
+  if (rc) return rc;
+  rc = ReadCtrl(s);
+  if (rc) return rc;
+  const double inv_hyp = [&] {
+    double d;
+    unsigned long long b = s->h_ctrl->slot[s->step & 1];
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+  }();
+  double m = inv_hyp;
+  if (s->inv_tc > m) m = s->inv_tc;
+  if (s->inv_visc > m) m = s->inv_visc;
+  const double d = s->p.CFL / m;
+  if (inv) {
+    inv[0] = inv_hyp;
+    inv[1] = s->inv_tc;
+    inv[2] = s->inv_visc;
+  }
+  if (dt) *dt = d;
+  if (s->h_ctrl->err || !std::isfinite(d))
+    return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
+  return FV_OK;
+}
+
+int fvgpu_step(fv_sim* s, double dt) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  // stream-ordered and asynchronous: the control kernel takes dt as an argument
+  int rc = EnqueueStep(s, STEP_GIVEN_DT, dt);
+  if (rc) return rc;
+  s->step += 1;
+  s->slot_valid = true;
+  return FV_OK;
+}
+
+int fvgpu_enqueue_steps(fv_sim* s, long nsteps) {
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  if (nsteps < 0) return Fail(s, FV_ERR_PARAM, "nsteps must be >= 0");
+  int rc = EnsureSlot(s);
+  if (rc) return rc;
+  for (long k = 0; k < nsteps; ++k) {
+    rc = EnqueueStep(s, STEP_FIXED, 0.0);
+    if (rc) return rc;
+  }
+  s->step += nsteps;
+  s->slot_valid = true;
+  return FV_OK;
+}
+
+int fvgpu_advance(fv_sim* s, double tend, long max_steps, double* t, long* nsteps) {
+  if (!s || !s->buf || !t) return s ? Fail(s, FV_ERR_PARAM, "null argument") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  int rc = EnsureSlot(s);
+  if (rc) return rc;
+  rc = ReadCtrl(s);
+  if (rc) return rc;
+  StepCtrl c = *s->h_ctrl;
+  const long long step0 = c.step;
+  c.mode = 1;
+  c.t = *t;
+  c.tend = tend;
+  c.max_steps = max_steps > 0 ? step0 + max_steps : 0;
+  c.cfl = s->p.CFL;
+  c.inv_tc = s->inv_tc;
+  c.inv_visc = s->inv_visc;
+  c.epsilon = s->p.epsilon;
+  rc = SetCtrl(s, c);
+  if (rc) return rc;
+
+  // Short fixed-step runs are launched directly; longer ones replay a graph.
+  const bool use_graph = !s->profile && !(max_steps > 0 && max_steps < kGraphSteps);
+  for (;;) {
+    if (use_graph) {
+      const void* key = (const void*)Current(s).f[0];
+      if (!s->graph || s->graph_key != key || s->graph_stream != s->stream) {
+        ResetGraph(s);
+        const int cur0 = s->cur;
+        cudaGraph_t g;
+        CUDA_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kGraphSteps; ++k) {
+          rc = EnqueueStep(s, STEP_LOOP, 0.0, false);
+          if (rc) {
+            cudaStreamEndCapture(s->stream, &g);
+            return rc;
+          }
+        }
+        CUDA_TRY(s, cudaStreamEndCapture(s->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        s->cur = cur0;  // capture only recorded the launches
+        s->graph_key = key;
+        s->graph_stream = s->stream;
+      }
+      CUDA_TRY(s, cudaGraphLaunch(s->graph, s->stream));
+      s->launches += (long)kGraphSteps * KernelsPerStep(s);
+      if (s->p.time_stepping != FV_TS_RK2 && (kGraphSteps & 1)) s->cur ^= 1;
+    } else {
+      const bool short_run = max_steps > 0 && max_steps < kGraphSteps;
+      const int n = short_run ? (int)max_steps : kGraphSteps;
+      for (int k = 0; k < n; ++k) {
+        rc = EnqueueStep(s, STEP_LOOP, 0.0);
+        if (rc) return rc;
+      }
+      if (short_run) {
+        rc = ReadCtrl(s);
+        if (rc) return rc;
+        break;
+      }
+    }
+    rc = ReadCtrl(s);
+    if (rc) return rc;
+    if (s->h_ctrl->err) break;
+    if (!s->h_ctrl->active) break;
+  }
+  // Euler ping-pong: inactive steps copy the state through, so the buffer
+  // holding it alternates exactly with the launched step count.
+  s->step = s->h_ctrl->step;
+  s->slot_valid = true;
+  *t = s->h_ctrl->t;
+  if (nsteps) *nsteps = (long)(s->h_ctrl->step - step0);
+  if (s->h_ctrl->err) return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt during advance");
+  return FV_OK;
+}
+
+int fvgpu_conserved_totals(fv_sim* s, double out[5]) {
+  if (!s || !s->buf || !out) return s ? Fail(s, FV_ERR_PARAM, "null argument") : FV_ERR_PARAM;
+  if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
+  int nb = 0;
+  {
+    Timed t(s, KC_CONV);
+    cudaError_t e = fv::launch_totals2d(s->G, Current(s), s->d_partial, kMaxTotalsBlocks, &nb, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "totals launch: %s", cudaGetErrorString(e));
+    t.done();
+  }
+  CUDA_TRY(s, cudaMemcpyAsync(s->h_partial, s->d_partial, (size_t)nb * 10 * sizeof(double), cudaMemcpyDeviceToHost,
+                              s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  for (int k = 0; k < 5; ++k) {
+    const int v = slot_of[k];
+    double S = 0.0, C = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const double x = s->h_partial[(b * 5 + v) * 2];
+      const double tt = S + x;
+      if (std::fabs(S) >= std::fabs(x)) C += (S - tt) + x;
+      else C += (x - tt) + S;
+      S = tt;
+      C += s->h_partial[(b * 5 + v) * 2 + 1];
+    }
+    out[k] = (v == 3 && !s->wact) ? 0.0 : S + C;
+  }
+  return FV_OK;
+}
+
+int fvgpu_set_stream(fv_sim* s, void* stream) {
+  if (!s) return FV_ERR_PARAM;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  ResetGraph(s);
+  return FV_OK;
+}
+
+int fvgpu_synchronize(fv_sim* s) {
+  if (!s) return FV_ERR_PARAM;
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return FV_OK;
+}
+
+int fvgpu_launch_count(const fv_sim* s, long* count) {
+  if (!s || !count) return FV_ERR_PARAM;
+  *count = s->launches;
+  return FV_OK;
+}
+
+int fvgpu_profile_enable(fv_sim* s, int enable) {
+  if (!s) return FV_ERR_PARAM;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  s->profile = enable != 0;
+  for (int k = 0; k < 3; ++k) {
+    s->prof_count[k] = 0;
+    s->prof_ms[k] = 0.0;
+  }
+  return FV_OK;
+}
+
+int fvgpu_kernel_times(fv_sim* s, long counts[3], double ms[3]) {
+  if (!s) return FV_ERR_PARAM;
+  for (int k = 0; k < 3; ++k) {
+    if (counts) counts[k] = s->prof_count[k];
+    if (ms) ms[k] = s->prof_ms[k];
+  }
+  return FV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,185 @@
+/*
+ * fv3d_gb300.h -- C ABI of the GB300 (sm_103a) finite-volume hydro step.
+ *
+ * The entry points replace the reference fv3d's hot path, which sits behind
+ * C++ classes taking `const Params&` and `Kokkos::View` handles:
+ *
+ *   fv_read_ini / fv_parse_ini   <- fv3d::readInifile            (SimInfo.h:169-306)
+ *   fvgpu_set_prim / get_prim    <- fv3d::primToCons/consToPrim  (SimInfo.h:313-331)
+ *   fvgpu_compute_dt             <- ComputeDtFunctor::computeDt  (ComputeDt.h:17-63)
+ *   fvgpu_step                   <- UpdateFunctor::update        (Update.h:180-206),
+ *                                   which runs BoundaryManager::fillBoundaries
+ *                                   (BoundaryConditions.h:146-215) inside euler_step
+ *                                   (Update.h:164-178)
+ *   fvgpu_advance                <- the time loop of main.cpp:51-74 (without I/O)
+ *   fvgpu_batch_*                <- no counterpart: many independent problems
+ *                                   advanced together, each with its own dt.
+ *
+ * Conventions
+ *   - Every function returns an int status (FV_OK == 0).  No C++ exception
+ *     crosses this boundary.
+ *   - Field arrays passed in or out are HOST arrays of the interior cells only,
+ *     in C order [Nz][Ny][Nx] (x fastest), i.e. element (i,j,k) of the
+ *     reference's View Q(k+Ng, j+Ng, i+Ng, var).  A NULL pointer means "all
+ *     zeros" on input and "do not copy" on output.
+ *   - A handle is not thread-safe and owns all of its device memory.  Work is
+ *     ordered on one CUDA stream per handle; fvgpu_step returns before the GPU
+ *     has finished, every call that returns data synchronises.
+ */
+#ifndef FV3D_GB300_H
+#define FV3D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Enumerations.  Numeric values equal the reference's enums (SimInfo.h:32-69). */
+enum fv_boundary   { FV_BC_ABSORBING = 0, FV_BC_REFLECTING = 1, FV_BC_PERIODIC = 2, FV_BC_C91 = 3 };
+enum fv_riemann    { FV_HLL = 0, FV_HLLC = 1 };
+enum fv_stepping   { FV_TS_EULER = 0, FV_TS_RK2 = 1 };
+enum fv_recon      { FV_PCM = 0, FV_PCM_WB = 1, FV_PLM = 2 };
+enum fv_tc_mode    { FV_TCM_CONSTANT = 0, FV_TCM_B02 = 1 };
+enum fv_bctc_mode  { FV_BCTC_NONE = 0, FV_BCTC_FIXED_TEMPERATURE = 1, FV_BCTC_FIXED_GRADIENT = 2 };
+enum fv_visc_mode  { FV_VSC_CONSTANT = 0 };
+/* Storage/arithmetic of the GPU path (driver-only setting, no reference counterpart). */
+enum fv_precision  { FV_PREC_FP64 = 0, FV_PREC_FP32_MIXED = 1 };
+
+/* Status codes. */
+enum fv_status {
+  FV_OK = 0,
+  FV_ERR_PARAM = 1,        /* invalid argument or parameter set                  */
+  FV_ERR_UNSUPPORTED = 2,  /* valid reference setting this build does not run    */
+  FV_ERR_CUDA = 3,         /* a CUDA runtime call or kernel launch failed        */
+  FV_ERR_NONFINITE = 4,    /* the dt reduction met NaN/Inf or rho<=0 / p<=0      */
+  FV_ERR_NOMEM = 5,        /* device or pinned host allocation failed            */
+  FV_ERR_IO = 6,           /* file could not be read                             */
+  FV_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up                 */
+  FV_ERR_STATE = 8         /* call order violated (e.g. step before set_prim)    */
+};
+
+/*
+ * Run parameters.  Mirrors fv3d::Params (SimInfo.h:72-159) minus the Kokkos
+ * ranges, plus two driver-only fields (precision, problem/filename strings).
+ * Fill it with fv_read_ini / fv_parse_ini (reference readInifile semantics,
+ * including single-precision parsing of every GetFloat key) or by hand; dx,
+ * dy, dz must then equal (max-min)/N as readInifile computes them.
+ */
+typedef struct fv_params {
+  /* mesh */
+  int Nx, Ny, Nz, Ng;
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double dx, dy, dz;
+  /* run */
+  double save_freq, tend;
+  int boundary_x, boundary_y, boundary_z;
+  int reconstruction, riemann_solver, time_stepping;
+  double CFL;
+  /* physics */
+  double epsilon, gamma0;
+  int gravity, well_balanced_flux_at_z_bc;
+  double g;
+  int well_balanced, thermal_conductivity_active;
+  /* thermal conduction */
+  int thermal_conductivity_mode, bctc_zmin;
+  double kappa;
+  int bctc_zmax, viscosity_active;
+  double bctc_zmin_value, bctc_zmax_value;
+  /* viscosity */
+  int viscosity_mode, seed;
+  double mu;
+  /* polytrope / H84 / C91 / B02 */
+  double m1, theta1, m2, theta2, h84_pert, c91_pert;
+  double b02_zmid, b02_kappa1, b02_kappa2, b02_thickness;
+  /* misc */
+  int log_frequency, precision;
+  char problem[64];
+  char filename_out[256];
+} fv_params;
+
+/* Human-readable name of a status code (static storage). */
+const char* fv_status_string(int status);
+
+/* readInifile (SimInfo.h:169-306) on a file / on INI text held in memory.
+ * Like the reference, a missing file or malformed line is not an error: the
+ * affected keys take their defaults.  FV_ERR_PARAM only for NULL arguments. */
+int fv_read_ini(const char* path, fv_params* out);
+int fv_parse_ini(const char* text, fv_params* out);
+
+/* ---- single problem --------------------------------------------------- */
+typedef struct fv_sim fv_sim;
+
+/* Allocate device state for one problem on the current CUDA device.
+ * FV_ERR_UNSUPPORTED names settings this build does not run (see
+ * fvgpu_last_error). */
+int fvgpu_create(const fv_params* params, fv_sim** out);
+int fvgpu_destroy(fv_sim* sim);
+/* Message for the last failing call on this handle ("" if none). */
+const char* fvgpu_last_error(const fv_sim* sim);
+
+/* Set the state from primitive (rho,u,v,w,p) or conserved (rho,rhou,rhov,rhow,E)
+ * host arrays; primToCons/consToPrim arithmetic as States.h:20-45. */
+int fvgpu_set_prim(fv_sim* sim, const double* rho, const double* u, const double* v,
+                   const double* w, const double* p);
+int fvgpu_get_prim(fv_sim* sim, double* rho, double* u, double* v, double* w, double* p);
+int fvgpu_set_cons(fv_sim* sim, const double* rho, const double* mx, const double* my,
+                   const double* mz, const double* E);
+int fvgpu_get_cons(fv_sim* sim, double* rho, double* mx, double* my, double* mz, double* E);
+
+/* ComputeDtFunctor::computeDt on the current state: *dt = CFL/max(inv[0..2]);
+ * inv (may be NULL) receives {inv_dt_hyp, inv_dt_tc, inv_dt_visc}. */
+int fvgpu_compute_dt(fv_sim* sim, double* dt, double inv[3]);
+/* One UpdateFunctor::update with the given dt (Euler or RK2 per params). */
+int fvgpu_step(fv_sim* sim, double dt);
+/* The main.cpp:51-74 loop: while (t + epsilon < tend && steps < max_steps)
+ * { dt = computeDt(); update(dt); t += dt; }.  *t is read and written; *nsteps
+ * (may be NULL) receives the number of steps taken.  max_steps <= 0 means no
+ * limit.  dt never leaves the GPU between steps. */
+int fvgpu_advance(fv_sim* sim, double tend, long max_steps, double* t, long* nsteps);
+/* Enqueue nsteps steps of the same loop without a time bound (each dt from
+ * the CFL reduction of the previous step, computed on the GPU) and return
+ * without waiting.  A non-finite dt stops the remaining steps and is reported
+ * by the next synchronising call (fvgpu_compute_dt / fvgpu_advance). */
+int fvgpu_enqueue_steps(fv_sim* sim, long nsteps);
+/* Sum over the interior of each conserved field (compensated summation). */
+int fvgpu_conserved_totals(fv_sim* sim, double out[5]);
+
+/* Launch on a caller-owned CUDA stream (cudaStream_t); NULL restores the
+ * handle's own stream. */
+int fvgpu_set_stream(fv_sim* sim, void* cuda_stream);
+int fvgpu_synchronize(fv_sim* sim);
+/* Number of kernels this handle has launched since creation. */
+int fvgpu_launch_count(const fv_sim* sim, long* count);
+/* Per-kernel CUDA-event timing.  While enabled every kernel launch is
+ * bracketed by events on the launching stream.  fvgpu_kernel_times reports,
+ * for kernel classes {0: stage kernels, 1: dt reduction, 2: conversions},
+ * the launch count and the summed milliseconds since the last reset. */
+int fvgpu_profile_enable(fv_sim* sim, int enable);
+int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
+
+/* ---- many independent problems (no reference counterpart) --------------- */
+typedef struct fv_batch fv_batch;
+
+/* n problems, each with its own parameters (grid size, gamma, BCs ...), all
+ * advanced together: one persistent kernel launch per RK stage walks a tile
+ * work-queue across every problem, each problem with its own dt. */
+int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out);
+int fvgpu_batch_destroy(fv_batch* b);
+const char* fvgpu_batch_last_error(const fv_batch* b);
+int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double* u,
+                         const double* v, const double* w, const double* p);
+int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* v,
+                         double* w, double* p);
+/* Advance every problem by nsteps steps, each with its own CFL dt (the
+ * fixed-step form of the main.cpp loop).  Steps are replayed from a captured
+ * CUDA graph. */
+int fvgpu_batch_run(fv_batch* b, long nsteps);
+/* Current time of each problem (host array of n). */
+int fvgpu_batch_times(fv_batch* b, double* t);
+int fvgpu_batch_set_stream(fv_batch* b, void* cuda_stream);
+int fvgpu_batch_synchronize(fv_batch* b);
+int fvgpu_batch_launch_count(const fv_batch* b, long* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FV3D_GB300_H */

@@ -1,0 +1,55 @@
+"""Shared helpers of the test suite."""
+import json
+import os
+
+import numpy as np
+
+from fv3d_gb300._abi import FvParams
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# Per-step parity bound of the plain FP64 path against the reference's FP64
+# CPU arithmetic: relative L1 per field.
+REL_L1_STEP = 1e-12
+
+
+def golden_cases():
+    with open(os.path.join(GOLDEN, "index.json")) as f:
+        return json.load(f)
+
+
+def load_case(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    params = json.loads(str(d["params"]))
+    return {
+        "ini": str(d["ini"]),
+        "params": params,
+        "qin": d["qin"],
+        "q0": d["q0"],
+        "q1": d["q1"],
+        "qN": d["qN"],
+        "dts": d["dts"],
+    }
+
+
+def params_from_dict(dct):
+    p = FvParams()
+    for name, _ in FvParams._fields_:
+        v = dct[name]
+        setattr(p, name, v.encode() if isinstance(v, str) else v)
+    return p
+
+
+def rel_l1(a, b):
+    """sum|a-b| / sum|b|; 0 when both vanish identically."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    num = float(np.abs(a - b).sum())
+    den = float(np.abs(b).sum())
+    if den == 0.0:
+        return 0.0 if num == 0.0 else float("inf")
+    return num / den
+
+
+def rel_l1_fields(A, B):
+    return [rel_l1(a, b) for a, b in zip(A, B)]

@@ -1,0 +1,164 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+Runs the reference's own FP64 hot-path headers (compiled unmodified against
+the Kokkos/INIReader shims into oracle/_ref/ by oracle/build.py) on small
+seeded problems and records, per case:
+  ini       the .ini text (parsed by the reference's readInifile)
+  params    every Params field readInifile produced (JSON)
+  qin       the primitive input state, shape (5, Nz, Ny, Nx)
+  q0        consToPrim(primToCons(qin)) as the reference stores it
+  dts       the dt of each step (ComputeDtFunctor::computeDt)
+  q1        primitive state after one step
+  qN        primitive state after all steps
+and Riemann-solver known answers (hll / hllc) on seeded state pairs that
+cover every wave-speed branch.
+
+Needs the reference sources (only present where the fixtures are made):
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fv3d_gb300 import problems  # noqa: E402
+from oracle import pyoracle  # noqa: E402
+
+
+def random_state(shape, seed, wmag=0.0, vmag=1.5):
+    n = int(np.prod(shape))
+    u = lambda s: problems.uniform(seed, s, n).reshape(shape)  # noqa: E731
+    rho = 0.5 + 1.5 * u(1)
+    prs = 0.5 + 1.5 * u(2)
+    vx = vmag * (2 * u(3) - 1)
+    vy = vmag * (2 * u(4) - 1)
+    vz = wmag * (2 * u(5) - 1)
+    return [rho, vx, vy, vz, prs]
+
+
+def random_problem(name, mesh, run, solvers, physics, seed, extra=None, wmag=0.0):
+    sec = {"mesh": mesh, "run": run, "solvers": solvers, "physics": physics}
+    sec.update(extra or {})
+    ini = problems.ini_text(sec)
+    p = problems._parse(ini)
+    return problems.Problem(name, ini, random_state((p.Nz, p.Ny, p.Nx), seed, wmag=wmag), params=p)
+
+
+def cases():
+    out = []
+    s = problems.sedov(64)
+    s.name = "sedov_64"
+    out.append((s, 4))
+    r = problems.rayleigh_taylor(32, 96)
+    r.name = "rt_32x96"
+    out.append((r, 4))
+    r = problems.rayleigh_taylor(24, 40, riemann="hllc", kappa=1e-3, mu=1e-3)
+    r.name = "rt_hllc_tc_visc"
+    out.append((r, 3))
+    t = problems.thermal_pulse(40)
+    t.name = "thermal_40"
+    out.append((t, 3))
+    sh = problems.shear_layer(36)
+    sh.name = "shear_36"
+    out.append((sh, 3))
+    out.append((problems.sod(48, "x", nx_other=8), 4))
+    out.append((problems.sod(48, "y", nx_other=8), 4))
+    mesh = problems._mesh(37, 23, 1)
+    out.append((random_problem("random_hll_absorbing", mesh,
+                               {"tend": 1.0, "boundaries_x": "absorbing", "boundaries_y": "reflecting",
+                                "boundaries_z": "periodic"},
+                               {"riemann_solver": "hll", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4}, seed=101, wmag=0.7), 3))
+    out.append((random_problem("random_hllc_periodic_w", mesh,
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                                "boundaries_z": "absorbing"},
+                               {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.6}, {"gamma0": 1.6666667}, seed=102, wmag=0.9), 3))
+    out.append((random_problem("random_euler_pcm", problems._mesh(33, 17, 1),
+                               {"tend": 1.0, "boundaries_x": "reflecting", "boundaries_y": "absorbing",
+                                "boundaries_z": "periodic"},
+                               {"riemann_solver": "hllc", "reconstruction": "pcm", "time_stepping": "euler",
+                                "CFL": 0.4}, {"gamma0": 1.4}, seed=103), 3))
+    out.append((random_problem("random_xz_pcm_wb_gravity", problems._mesh(20, 1, 28),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                                "boundaries_z": "reflecting"},
+                               {"riemann_solver": "hllc", "reconstruction": "pcm_wb", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4, "gravity": True, "g": -0.7}, seed=104), 3))
+    out.append((random_problem("random_xy_tc_visc", problems._mesh(26, 30, 1),
+                               {"tend": 1.0, "boundaries_x": "absorbing", "boundaries_y": "periodic",
+                                "boundaries_z": "periodic"},
+                               {"riemann_solver": "hll", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4}, seed=105,
+                               extra={"thermal_conduction": {"active": True, "kappa": 0.02},
+                                      "viscosity": {"active": True, "mu": 0.01}}), 3))
+    out.append((random_problem("random_xz_visc_hll", problems._mesh(22, 1, 18),
+                               {"tend": 1.0, "boundaries_x": "reflecting", "boundaries_y": "periodic",
+                                "boundaries_z": "absorbing"},
+                               {"riemann_solver": "hll", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4, "gravity": True, "g": -0.3}, seed=106,
+                               extra={"thermal_conduction": {"active": True, "kappa": 0.01},
+                                      "viscosity": {"active": True, "mu": 0.02}}), 3))
+    out.append((random_problem("random_3d_oracle_only", problems._mesh(9, 7, 6),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "reflecting",
+                                "boundaries_z": "absorbing"},
+                               {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4}, seed=107, wmag=1.0,
+                               extra={"thermal_conduction": {"active": True, "kappa": 0.01},
+                                      "viscosity": {"active": True, "mu": 0.01}}), 2))
+    return out
+
+
+def riemann_kats(seed=2024, n=600):
+    """State pairs over every branch: subsonic, supersonic left/right moving,
+    strong contrasts, and exact ties."""
+    u = lambda s: problems.uniform(seed, s, n)  # noqa: E731
+    qL = np.stack([0.1 + 3 * u(1), 6 * (2 * u(2) - 1), 2 * (2 * u(3) - 1), 2 * (2 * u(4) - 1), 0.05 + 5 * u(5)], 1)
+    qR = np.stack([0.1 + 3 * u(6), 6 * (2 * u(7) - 1), 2 * (2 * u(8) - 1), 2 * (2 * u(9) - 1), 0.05 + 5 * u(10)], 1)
+    qR[: n // 10] = qL[: n // 10]  # identical states
+    out = {"qL": qL, "qR": qR}
+    for solver, name in ((0, "hll"), (1, "hllc")):
+        for g in (1.4, 5.0 / 3.0):
+            f, po = pyoracle.riemann(solver, g, qL, qR, use_ref=True)
+            out["%s_%g_flux" % (name, g)] = f
+            out["%s_%g_pout" % (name, g)] = po
+    return out
+
+
+def main():
+    pyoracle.load_ref()
+    tmp = tempfile.mkdtemp()
+    index = []
+    for pr, nsteps in cases():
+        path = os.path.join(tmp, pr.name + ".ini")
+        with open(path, "w") as f:
+            f.write(pr.ini)
+        ref = pyoracle.RefOracle(path)
+        ref.set_prim(*pr.prim)
+        q0 = np.stack(ref.get_prim())
+        dts, q1 = [], None
+        for k in range(nsteps):
+            dt = ref.compute_dt()
+            ref.step(dt)
+            dts.append(dt)
+            if k == 0:
+                q1 = np.stack(ref.get_prim())
+        qN = np.stack(ref.get_prim())
+        params = ref.params.as_dict()
+        np.savez_compressed(os.path.join(HERE, pr.name + ".npz"), qin=np.stack(pr.prim), q0=q0, q1=q1, qN=qN,
+                            dts=np.array(dts),
+                            ini=np.array(pr.ini), params=np.array(json.dumps(params)))
+        index.append({"name": pr.name, "steps": nsteps, "shape": list(q0.shape[1:])})
+        print(pr.name, q0.shape, dts[:2])
+    np.savez_compressed(os.path.join(HERE, "riemann_kats.npz"), **riemann_kats())
+    with open(os.path.join(HERE, "index.json"), "w") as f:
+        json.dump(index, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
