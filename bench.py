@@ -60,7 +60,7 @@ def problem():
 def config_dict(pr, l2):
     return {"workload": WORKLOAD, "cells": pr.cells, "grid": [pr.params.Nx, pr.params.Nz],
             "riemann": "hll", "reconstruction": "plm", "time_stepping": "rk2", "precision": "fp64",
-            "l2": l2, "parallelism": "replicas"}
+            "l2": l2, "parallelism": "replicas", "build": os.environ.get("FV3D_LIB_VARIANT", "default")}
 
 
 class Clocks:
@@ -287,13 +287,31 @@ def run_gpu(args):
     return 0
 
 
+def run_profile_case(args):
+    """Only the workload's steps (warm-up + steps), for launch lists and ncu
+    captures: no timing, no CPU baseline, no e2e."""
+    import fv3d_gb300 as fv
+    pr = problem()
+    sim = fv.Simulation(pr.params)
+    sim.set_prim(*pr.prim)
+    sim.enqueue_steps(args.warmup + args.steps)
+    sim.synchronize()
+    sim.get_prim()
+    print("profile case done: %d steps of %s" % (args.warmup + args.steps, WORKLOAD))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run only the workload's steps (for ncu); prints no JSON")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

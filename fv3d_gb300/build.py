@@ -6,9 +6,13 @@ parallel with ``nvcc -gencode arch=compute_103a,code=sm_103a`` and links
 ``fv3d_gb300/_lib/fv3d`` driver executable.  Objects go to
 ``fv3d_gb300/_build``.  Rebuilds only what changed.
 
-``variant="strict"`` builds the same sources with ``-fmad=false`` into
-``fv3d_gb300/_lib_strict/``: no fused multiply-adds, so the kernels round
-exactly like the reference's FP64 CPU build (a bit-exactness check mode).
+The FP64 translation units (FP64_EXACT_SOURCES) are compiled with
+``-fmad=false``: the compiler may not contract a*b+c into one fused
+operation, so every FP64 operation rounds exactly as in the reference's FP64
+CPU build and the plain path reproduces it bit for bit.  Fused operations in
+those files are written out explicitly (fma()) only where they are exact by
+construction.  ``variant="fmad"`` lets the compiler contract them too (faster,
+no longer bit-exact), for comparison.
 """
 import concurrent.futures as cf
 import os
@@ -23,6 +27,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["fv_stage2d.cu", "fv_api.cpp", "fv_ini.cpp", "fv_batch.cpp"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
+FP64_EXACT_SOURCES = {"fv_stage2d.cu"}
 
 
 def _nvcc():
@@ -67,7 +72,6 @@ def _compile(src, obj, fmad):
 
 def build(variant="default", jobs=None, verbose=False):
     """Compile and link; returns the path of the shared library."""
-    fmad = variant != "strict"
     objdir = os.path.join(PKG, "_build", variant)
     os.makedirs(objdir, exist_ok=True)
     os.makedirs(lib_dir(variant), exist_ok=True)
@@ -80,10 +84,11 @@ def build(variant="default", jobs=None, verbose=False):
         o = os.path.join(objdir, os.path.splitext(src)[0] + ".o")
         objs[src] = o
         if _stale(o, [s, __file__] + headers):
-            todo.append((s, o))
+            fmad = variant == "fmad" or src not in FP64_EXACT_SOURCES
+            todo.append((s, o, fmad))
     if todo:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
-            list(ex.map(lambda a: _compile(a[0], a[1], fmad), todo))
+            list(ex.map(lambda a: _compile(*a), todo))
     lib = lib_path(variant)
     lib_objs = [objs[s] for s in LIB_SOURCES if s in objs]
     if _stale(lib, lib_objs):
