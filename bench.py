@@ -41,6 +41,10 @@ METRIC = "Mcell-updates/s: FP64 plain vs mixed/batched at stated L1 err; HBM % o
 UNIT = "Mcell-updates/s"
 WORKLOAD = "rayleigh_taylor_512x1536_fp64"
 ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2-D)
+# dram__bytes_read.sum + dram__bytes_write.sum of the two stage launches of one
+# RK2 step of this workload, from one ncu --set full capture
+# (profiles/stage2d_fp64_rt512x1536.md: 25.29+0.09 MB and 50.40+0.12 MB).
+NCU_TRAFFIC_BYTES_PER_STEP = 75.90e6
 
 
 def peaks():
@@ -228,9 +232,11 @@ def run_gpu(args):
     ms_per_step_stages = stage_ms / (stage_n / 2.0)
     hbm_peak, peak_kind = peaks()
     achieved = ALGO_BYTES_PER_CELL_UPDATE * pr.cells / (ms_per_step_stages / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "stage2d_fp64 (RK2 stages 1+2)", "achieved": achieved,
+    roofline = {"bound": "hbm", "kernel": "stage2d_fp64, both launches of one RK2 step", "achieved": achieved,
                 "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "algo_bytes_per_cell_update": ALGO_BYTES_PER_CELL_UPDATE,
+                "traffic": NCU_TRAFFIC_BYTES_PER_STEP, "traffic_unit": "bytes per RK2 step (ncu)",
+                "algo_bytes": ALGO_BYTES_PER_CELL_UPDATE * pr.cells,
+                "algo_bytes_per_cell_update": ALGO_BYTES_PER_CELL_UPDATE,
                 "stage_ms_per_launch": stage_ms / stage_n, "dt_kernel_ms_per_launch": kt["dt"][1] / max(kt["dt"][0], 1)}
 
     # e2e through the C ABI with pinned host buffers

@@ -94,6 +94,25 @@ void DtConstants(const fv_params& p, double* inv_tc, double* inv_visc) {
 
 int DevBC(int bc) { return bc == FV_BC_ABSORBING ? fv::DBC_ABSORBING : bc == FV_BC_REFLECTING ? fv::DBC_REFLECTING : fv::DBC_PERIODIC; }
 
+// True when d > 0 is an exact power of two, so 1/d is exact too.
+bool PowerOfTwo(double d) {
+  int e;
+  return d > 0.0 && std::isfinite(d) && std::frexp(d, &e) == 0.5 && e > -1021 && e < 1022;
+}
+
+// Reciprocals and flags the kernels use to replace divisions by the cell
+// sizes and by gamma - 1 with operations that round identically.
+void SetExactConstants(Grid2D& G) {
+  G.inv_dx = 1.0 / G.dx;
+  G.inv_dy = 1.0 / G.dy;
+  G.inv_dz = 1.0 / G.dz;
+  G.pow2_x = PowerOfTwo(G.dx);
+  G.pow2_y = PowerOfTwo(G.dy);
+  G.pow2_z = PowerOfTwo(G.dz);
+  G.gm1 = G.gamma - 1.0;
+  G.inv_gm1 = 1.0 / G.gm1;
+}
+
 // Checks that the parameter set is one this build runs and fills the grid.
 int Configure(fv_sim* s) {
   const fv_params& p = s->p;
@@ -146,6 +165,7 @@ int Configure(fv_sim* s) {
   G.g = p.g;
   G.kappa = p.kappa;
   G.mu = p.mu;
+  SetExactConstants(G);
   DtConstants(p, &s->inv_tc, &s->inv_visc);
   return FV_OK;
 }

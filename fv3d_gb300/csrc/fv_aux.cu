@@ -1,0 +1,193 @@
+// fv_aux.cu -- the small kernels around the stage kernel: the standalone CFL
+// reduction, the per-step control kernel, primitive <-> conserved
+// conversions and the conservation sums.  Built without FMA contraction, like
+// the stage kernel, so every value rounds as in the reference.
+#include "fv_kernels.h"
+#include "fv_plane2d.cuh"
+
+namespace fv {
+
+namespace {
+
+int grid_for(long long n, int block) {
+  long long b = (n + block - 1) / block;
+  if (b > 152 * 16) b = 152 * 16;
+  return b < 1 ? 1 : (int)b;
+}
+
+// ComputeDt.h:28-54 over the interior: max inv_dt_hyp into ctrl->slot[slot].
+template <int PLANE, bool WACT>
+__global__ void __launch_bounds__(256) reduce2d_fp64(const Grid2D G, const Fields u, StepCtrl* ctrl, int slot) {
+  __shared__ unsigned long long s_red[8];
+  unsigned long long red = 0ull;
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+    double w[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = (WACT || v != 3) ? u.f[v][o] : 0.0;
+    const double inv = inv_dt_hyp64<PLANE, WACT>(w, G);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
+    red = b > red ? b : red;
+    if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+  }
+  block_max_atomic(red, &ctrl->slot[slot], s_red);
+}
+
+__global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  StepCtrl& c = ctrl[i];
+  const int p = (int)(c.step & 1);
+  const int mode = mode_override >= 0 ? mode_override : c.mode;
+  double dt;
+  int active;
+  if (mode == 0) {
+    dt = mode_override == 0 ? dt_given : c.dt_given;
+    active = 1;
+  } else {
+    // ComputeDt.h:62: CFL / max(inv_hyp, inv_tc, inv_visc); main.cpp:51 loop bound.
+    const double inv_hyp = __longlong_as_double((long long)c.slot[p]);
+    double m = inv_hyp;
+    if (c.inv_tc > m) m = c.inv_tc;
+    if (c.inv_visc > m) m = c.inv_visc;
+    dt = c.cfl / m;
+    // mode 2: fixed step count, no time bound; a previous error stops it
+    active = mode == 2 ? !c.err
+                       : (c.t + c.epsilon < c.tend) && (c.max_steps <= 0 || c.step < c.max_steps);
+    if (active && !(dt > 0.0 && dt <= 1.0e300)) {
+      c.err |= 1;
+      active = 0;
+    }
+  }
+  c.slot[p ^ 1] = 0ull;
+  c.parity = p;
+  c.active = active;
+  c.dt_cur = active ? dt : 0.0;
+  if (active) {
+    c.t = c.t + dt;
+    c.step = c.step + 1;
+  }
+}
+
+// primToCons in place (States.h:20-31).  Storage order in and out.
+template <int PLANE>
+__global__ void prim_to_cons2d(const Grid2D G, const Fields u) {
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+    const double r = u.f[0][o];
+    const double ma = __dmul_rn(r, u.f[1][o]), mb = __dmul_rn(r, u.f[2][o]), mc = __dmul_rn(r, u.f[3][o]);
+    const double mx = ma, my = PLANE == PLANE_XY ? mb : mc, mz = PLANE == PLANE_XY ? mc : mb;
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
+    const double Ek = __ddiv_rn(__dmul_rn(0.5, s), r);
+    const double E = __dadd_rn(Ek, __ddiv_rn(u.f[4][o], G.gm1));
+    u.f[1][o] = ma;
+    u.f[2][o] = mb;
+    u.f[3][o] = mc;
+    u.f[4][o] = E;
+  }
+}
+
+// consToPrim (States.h:34-45); src and dst may alias.
+template <int PLANE>
+__global__ void cons_to_prim2d(const Grid2D G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+    const double r = src.f[0][o];
+    const double va = __ddiv_rn(src.f[1][o], r), vb = __ddiv_rn(src.f[2][o], r), vc = __ddiv_rn(src.f[3][o], r);
+    const double vx = va, vy = PLANE == PLANE_XY ? vb : vc, vz = PLANE == PLANE_XY ? vc : vb;
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+    const double Ek = __dmul_rn(__dmul_rn(0.5, r), s);
+    const double p = __dmul_rn(__dsub_rn(src.f[4][o], Ek), G.gm1);
+    dst.f[0][o] = r;
+    dst.f[1][o] = va;
+    dst.f[2][o] = vb;
+    dst.f[3][o] = vc;
+    dst.f[4][o] = p;
+  }
+}
+
+// Neumaier-compensated accumulation.
+__device__ __forceinline__ void kadd(double& s, double& c, double x) {
+  const double t = s + x;
+  if (fabs(s) >= fabs(x)) c += (s - t) + x;
+  else c += (x - t) + s;
+  s = t;
+}
+
+__global__ void __launch_bounds__(256) totals2d(const Grid2D G, const Fields u, double* partial) {
+  __shared__ double s_sum[5][256], s_cmp[5][256];
+  double s[5] = {0, 0, 0, 0, 0}, cc[5] = {0, 0, 0, 0, 0};
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) kadd(s[v], cc[v], u.f[v][o]);
+  }
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    s_sum[v][t] = s[v];
+    s_cmp[v][t] = cc[v];
+  }
+  __syncthreads();
+  if (t < 5) {
+    double S = 0.0, Cm = 0.0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      kadd(S, Cm, s_sum[t][i]);
+      Cm += s_cmp[t][i];
+    }
+    partial[((long long)blockIdx.x * 5 + t) * 2 + 0] = S;
+    partial[((long long)blockIdx.x * 5 + t) * 2 + 1] = Cm;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_reduce2d(const Grid2D& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.nb, 256);
+  if (G.plane == PLANE_XY) {
+    if (wact) reduce2d_fp64<PLANE_XY, true><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
+    else reduce2d_fp64<PLANE_XY, false><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
+  } else {
+    if (wact) reduce2d_fp64<PLANE_XZ, true><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
+    else reduce2d_fp64<PLANE_XZ, false><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_control(StepCtrl* ctrl, int n, int mode_override, double dt_given, cudaStream_t st) {
+  control_kernel<<<(n + 127) / 128, 128, 0, st>>>(ctrl, n, mode_override, dt_given);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prim_to_cons2d(const Grid2D& G, Fields u, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.nb, 256);
+  if (G.plane == PLANE_XY) prim_to_cons2d<PLANE_XY><<<grid, 256, 0, st>>>(G, u);
+  else prim_to_cons2d<PLANE_XZ><<<grid, 256, 0, st>>>(G, u);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cons_to_prim2d(const Grid2D& G, Fields src, Fields dst, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.nb, 256);
+  if (G.plane == PLANE_XY) cons_to_prim2d<PLANE_XY><<<grid, 256, 0, st>>>(G, src, dst);
+  else cons_to_prim2d<PLANE_XZ><<<grid, 256, 0, st>>>(G, src, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_totals2d(const Grid2D& G, Fields u, double* partial, int max_blocks, int* nblocks,
+                            cudaStream_t st) {
+  int grid = grid_for((long long)G.na * G.nb, 256);
+  if (grid > max_blocks) grid = max_blocks;
+  *nblocks = grid;
+  totals2d<<<grid, 256, 0, st>>>(G, u, partial);
+  return cudaGetLastError();
+}
+
+}  // namespace fv

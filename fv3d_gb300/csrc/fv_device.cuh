@@ -48,6 +48,10 @@ struct Grid2D {
   double da, db, dc;   // cell size along a, b and the degenerate axis
   double dx, dy, dz;   // the same in reference (x,y,z) naming
   double gamma, g, kappa, mu;
+  // Exact-arithmetic helpers (host-computed with IEEE double):
+  double inv_dx, inv_dy, inv_dz;   // RN(1/d)
+  int pow2_x, pow2_y, pow2_z;      // d is a power of two (1/d exact)
+  double gm1, inv_gm1;             // gamma - 1, RN(1/(gamma - 1))
 };
 
 // Maps a cell index g (may be a ghost, -2 <= g < n+2) along an axis with n

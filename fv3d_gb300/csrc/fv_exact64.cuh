@@ -1,0 +1,71 @@
+// fv_exact64.cuh -- FP64 building blocks that round exactly like the plain
+// IEEE operations they replace, with fewer FP64-pipe instructions.
+//
+// On GB300 the FP64 pipe executes about 1/73 of the FP32 rate, so the plain
+// FP64 path is bound by its count of FP64 instructions.  Every helper here
+// returns bit-for-bit the value of the reference expression it stands for
+// (for finite operands away from the subnormal range), so the FP64 stage
+// kernel stays bit-identical to the reference's CPU arithmetic.
+//
+// Division by a value whose correctly rounded reciprocal is known uses
+// Markstein's correction (P. Markstein, "Computation of elementary functions
+// on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990; see
+// also Muller et al., Handbook of Floating-Point Arithmetic, the theorem on
+// correcting a quotient with a fused multiply-add): with y = RN(1/b) and
+// q0 = RN(a*y), which lies within one ulp of a/b, the residual
+// r = a - b*q0 is exactly representable (one fma) and RN(q0 + r*y) = RN(a/b).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fv {
+
+// RN(a / b) given y = RN(1 / b): one multiply and two fused operations
+// instead of a full IEEE division.
+__device__ __forceinline__ double div_by_rcp(double a, double b, double y) {
+  const double q0 = __dmul_rn(a, y);
+  const double r = fma(-b, q0, a);
+  return fma(r, y, q0);
+}
+
+// (x) / d for a cell size d: an exact multiplication by 1/d when d is a power
+// of two (then 1/d is exact and scaling by it rounds nowhere), else the
+// corrected quotient above.
+__device__ __forceinline__ double div_cell(double x, double d, double inv_d, bool pow2) {
+  return pow2 ? __dmul_rn(x, inv_d) : div_by_rcp(x, d, inv_d);
+}
+
+// minmod of Update.h:73-80 -- 0 if dL*dR < 0, else the argument of smaller
+// magnitude, ties to dR -- decided on the bit patterns without FP64
+// instructions.  The sign test equals `dL*dR < 0` whenever the product cannot
+// underflow to zero (exponent sum check) and neither operand is NaN; the
+// magnitude test equals `fabs(dL) < fabs(dR)` because IEEE magnitudes order
+// like their bit patterns.  The remaining cases take the reference formula.
+__device__ __forceinline__ double minmod_exact(double dL, double dR) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(dL);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(dR);
+  const unsigned long long ma = a & 0x7fffffffffffffffull, mb = b & 0x7fffffffffffffffull;
+  const unsigned long long kInf = 0x7ff0000000000000ull;
+  if (ma <= kInf && mb <= kInf) {
+    if (ma == 0ull || mb == 0ull || ((a ^ b) >> 63) == 0ull) return ma < mb ? dL : dR;
+    const unsigned ea = (unsigned)(ma >> 52), eb = (unsigned)(mb >> 52);
+    if (ea != 0u && eb != 0u && ea + eb >= 972u) return 0.0;  // |dL*dR| >= 2^-1074
+  }
+  if (dL * dR < 0.0) return 0.0;
+  return fabs(dL) < fabs(dR) ? dL : dR;
+}
+
+// Face-state reconstruction q + (slope*sign)*0.5 (Update.h:21): the product
+// with +-0.5 is exact, so a single fused operation rounds identically.
+__device__ __forceinline__ double recon_plus(double q, double slope) { return fma(slope, 0.5, q); }
+__device__ __forceinline__ double recon_minus(double q, double slope) { return fma(slope, -0.5, q); }
+
+// Constants every FP64 kernel needs, computed on the host with IEEE double
+// arithmetic exactly as the reference evaluates them.
+struct Consts64 {
+  double gamma;     // gamma0
+  double gm1;       // gamma0 - 1 (exact for 1 < gamma0 < 3)
+  double inv_gm1;   // RN(1 / (gamma0 - 1)), also HLLC's `entho`
+};
+
+}  // namespace fv

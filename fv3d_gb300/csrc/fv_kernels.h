@@ -16,7 +16,7 @@ struct Fields {
 
 // Tile of the 2-D FP64 stage kernel.
 constexpr int kTileX = 32;
-constexpr int kTileY = 8;
+constexpr int kTileY = 16;
 
 // One fused stage (Euler step, RK2 stage 1 or RK2 stage 2) over a 2-D plane.
 //   uin  : the stage's input state (read with a 2-cell ghost halo)

@@ -64,6 +64,25 @@ def test_golden_trajectory(name):
     assert max(rel_l1_fields(sim.get_prim(), case["qN"])) <= n * REL_L1_STEP
 
 
+@pytest.mark.parametrize("name", GPU_CASES)
+def test_golden_bitwise(name):
+    """The plain FP64 path rounds like the reference: its free-running
+    trajectory reproduces the reference's dt sequence and fields bit for bit
+    (tolerance 0, stronger than the 1e-12 bound)."""
+    case = load_case(name)
+    p = params_from_dict(case["params"])
+    sim = fv.Simulation(p)
+    sim.set_prim(*case["qin"])
+    np.testing.assert_array_equal(np.stack(sim.get_prim()), case["q0"])
+    for k, dt_ref in enumerate(case["dts"]):
+        dt = sim.compute_dt()
+        assert dt == dt_ref, (k, dt, dt_ref)
+        sim.step(dt)
+        if k == 0:
+            np.testing.assert_array_equal(np.stack(sim.get_prim()), case["q1"])
+    np.testing.assert_array_equal(np.stack(sim.get_prim()), case["qN"])
+
+
 @pytest.mark.parametrize("builder,kw", [
     ("sedov", dict(n=256)),                       # config 0, full size
     ("rayleigh_taylor", dict(nx=512, nz=1536)),   # config 1 (RT), full size
