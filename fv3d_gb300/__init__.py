@@ -80,6 +80,8 @@ def _declare(lib):
         "fvgpu_step": (C.c_int, [vp, C.c_double]),
         "fvgpu_advance": (C.c_int, [vp, C.c_double, C.c_long, _dp, C.POINTER(C.c_long)]),
         "fvgpu_enqueue_steps": (C.c_int, [vp, C.c_long]),
+        "fvgpu_step_noalloc": (C.c_int, [P, C.POINTER(C.c_void_p), C.c_long, C.c_double, _dp, vp,
+                                         C.c_char_p, C.c_size_t]),
         "fvgpu_conserved_totals": (C.c_int, [vp, _dp]),
         "fvgpu_set_stream": (C.c_int, [vp, vp]),
         "fvgpu_synchronize": (C.c_int, [vp]),

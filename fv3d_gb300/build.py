@@ -25,7 +25,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["fv_stage2d.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp", "fv_batch.cpp"]
+LIB_SOURCES = ["fv_stage2d.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp", "fv_batch.cpp", "fv_noalloc.cu"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
 FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_aux.cu"}
 

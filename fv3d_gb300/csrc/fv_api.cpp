@@ -338,6 +338,26 @@ int SetState(fv_sim* s, const double* const ref_fields[5], bool prim) {
 
 }  // namespace
 
+namespace fv {
+
+// The parameter checks and grid set-up of fvgpu_create, without allocating:
+// fills G and the constant CFL terms, or returns a status with a message.
+int configure_grid(const fv_params& p, Grid2D* G, double* inv_tc, double* inv_visc, int* deg_bc,
+                   std::string* err) {
+  fv_sim s;
+  s.p = p;
+  const int rc = Configure(&s);
+  if (err) *err = s.err;
+  if (rc != FV_OK) return rc;
+  *G = s.G;
+  *inv_tc = s.inv_tc;
+  *inv_visc = s.inv_visc;
+  *deg_bc = s.deg_bc;
+  return FV_OK;
+}
+
+}  // namespace fv
+
 extern "C" {
 
 int fvgpu_create(const fv_params* params, fv_sim** out) {

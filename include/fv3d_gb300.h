@@ -29,6 +29,8 @@
 #ifndef FV3D_GB300_H
 #define FV3D_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -155,6 +157,34 @@ int fvgpu_launch_count(const fv_sim* sim, long* count);
  * the launch count and the summed milliseconds since the last reset. */
 int fvgpu_profile_enable(fv_sim* sim, int enable);
 int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
+
+/* One update (Euler or RK2 per params, with the given dt) of a 2-D problem
+ * whose conserved state lives in device arrays the caller owns, allocating
+ * no memory at all.  No counterpart in the reference: it exists for host
+ * codes that cannot call cudaMalloc in their time loop -- applications whose
+ * device memory belongs to another allocator (a pool or arena that already
+ * reserved the GPU) and latency-critical loops that cannot take the device
+ * synchronisation of cudaMalloc/cudaFree.  The stage scratch (U* and the
+ * dt/reduction control block) is one fixed 32 MiB array per device, held
+ * until the process exits once the call has been used on that device.
+ *   fields  device pointers to rho, rho*u, rho*v, rho*w, E of the interior
+ *           cells, rows of Nx cells along x with a stride of `pitch`
+ *           doubles, rows following y (Nz == 1) or z (Ny == 1); the
+ *           momentum along the one-cell axis may be NULL when it is zero and
+ *           viscosity is off.  Updated in place.
+ *   pitch   row stride in doubles (>= Nx).  5 x pitch x rows x 8 bytes
+ *           + 256 must fit in 32 MiB (e.g. 512 x 1536 at pitch 512); larger
+ *           problems get FV_ERR_PARAM and a message -- use fvgpu_create.
+ *   next_dt if non-NULL, receives the CFL dt of the updated state (this
+ *           synchronises the stream); otherwise the call returns after
+ *           enqueueing its work on `stream` (NULL: the legacy default stream).
+ *   errbuf  optional buffer for a message when the status is not FV_OK.
+ * All calls share the scratch and leave its last contents there: calls whose
+ * work overlaps on the GPU race.  The first call on each device looks up the
+ * scratch address once (with that device current); make it before any
+ * stream capture. */
+int fvgpu_step_noalloc(const fv_params* params, double* const fields[5], long pitch, double dt,
+                       double* next_dt, void* stream, char* errbuf, size_t errlen);
 
 /* ---- many independent problems (no reference counterpart) --------------- */
 typedef struct fv_batch fv_batch;

@@ -1,0 +1,99 @@
+"""fvgpu_step_noalloc: the time step for callers that cannot allocate.
+
+Host codes whose device memory belongs to another allocator (a pool or arena
+that already reserved the GPU), or whose time loop cannot take the device
+synchronisation of cudaMalloc/cudaFree, keep their conserved state in their
+own device arrays and call fvgpu_step_noalloc, which allocates nothing: its
+stage scratch is a fixed 32 MiB array in device memory.  These tests drive it
+through the C ABI on device arrays with a padded row pitch and check, over
+two calls in a row, that it produces the same state as the regular handle
+(fvgpu_create / fvgpu_step) within the per-step tolerance of the parity
+tests -- in fact bit for bit -- and that the next dt it reports equals
+fvgpu_compute_dt's.  Kept in a file pytest collects last.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import fv3d_gb300 as fv
+from fv3d_gb300 import problems
+from _helpers import REL_L1_STEP, rel_l1_fields
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_state(torch, cons, pitch, skip):
+    """Copies (rho, mx, my, mz, E) into padded device rows; field `skip`
+    (the momentum along the one-cell axis) is passed as NULL."""
+    nz, ny, nx = cons[0].shape
+    rows = nz * ny
+    arrs, ptrs = [], (C.c_void_p * 5)()
+    for k, a in enumerate(cons):
+        if k == skip:
+            arrs.append(None)
+            ptrs[k] = None
+            continue
+        t = torch.full((rows, pitch), float("nan"), dtype=torch.float64, device="cuda")
+        t[:, :nx] = torch.from_numpy(np.ascontiguousarray(a).reshape(rows, nx)).cuda()
+        arrs.append(t)
+        ptrs[k] = t.data_ptr()
+    return arrs, ptrs
+
+
+def _to_host(arrs, shape):
+    nz, ny, nx = shape
+    return [np.zeros(shape) if t is None else t[:, :nx].cpu().numpy().reshape(shape) for t in arrs]
+
+
+@pytest.mark.parametrize("case", ["rt_xz_null_v", "thermal_xy_visc"])
+def test_noalloc_matches_handle_two_calls(case):
+    torch = pytest.importorskip("torch")
+    if case == "rt_xz_null_v":
+        pr = problems.rayleigh_taylor(64, 192)
+        skip = 2          # rho*v: zero in the x-z plane without viscosity
+    else:
+        pr = problems.thermal_pulse(96)
+        skip = -1         # viscosity drives rho*w: pass it
+    lib = fv.load_library()
+    sim = fv.Simulation(pr.params)
+    sim.set_prim(*pr.prim)
+    shape = sim.shape
+    pitch = shape[2] + 24  # padded rows
+    arrs, ptrs = _device_state(torch, sim.get_cons(), pitch, skip)
+    params = pr.params.copy()
+    err = C.create_string_buffer(512)
+    next_dt = C.c_double()
+    dt = sim.compute_dt()
+    for call in range(2):
+        sim.step(dt)
+        torch.cuda.synchronize()
+        rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs, pitch, dt, C.byref(next_dt), None, err, 512)
+        assert rc == 0, (rc, err.value)
+        got = _to_host(arrs, shape)
+        want = sim.get_cons()
+        errs = rel_l1_fields(got, [w if k != skip else np.zeros(shape) for k, w in enumerate(want)])
+        assert max(errs) <= REL_L1_STEP, (call, errs)
+        for k in range(5):
+            if k != skip:
+                np.testing.assert_array_equal(got[k], want[k])
+        dt_handle = sim.compute_dt()
+        assert next_dt.value == dt_handle, (call, next_dt.value, dt_handle)
+        dt = dt_handle
+    # the padding columns were never written
+    for t in arrs:
+        if t is not None:
+            assert torch.isnan(t[:, shape[2]:]).all()
+
+
+def test_noalloc_rejects_problems_beyond_its_scratch():
+    """A 2048^2 run needs 160 MiB of stage scratch, more than the fixed 32 MiB:
+    the call refuses with a message before touching the GPU."""
+    lib = fv.load_library()
+    params = fv.parse_ini("[mesh]\nNx=2048\nNy=2048\nNz=1\n[run]\nboundaries_z=periodic\n"
+                          "[solvers]\ntime_stepping=RK2\nreconstruction=plm\n")
+    ptrs = (C.c_void_p * 5)(1, 1, 1, None, 1)  # never dereferenced: rejected first
+    err = C.create_string_buffer(512)
+    rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs, 2048, 1e-3, None, None, err, 512)
+    assert rc == 1
+    assert b"scratch" in err.value and b"fvgpu_create" in err.value
