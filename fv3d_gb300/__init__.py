@@ -98,6 +98,7 @@ def _declare(lib):
         "fvgpu_batch_set_stream": (C.c_int, [vp, vp]),
         "fvgpu_batch_synchronize": (C.c_int, [vp]),
         "fvgpu_batch_launch_count": (C.c_int, [vp, C.POINTER(C.c_long)]),
+        "fvgpu_batch_tiling": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -242,3 +243,86 @@ class Simulation:
         self._check(self.lib.fvgpu_kernel_times(self._h, counts, C.cast(ms, _dp)), "kernel_times")
         names = ("stage", "dt", "conversion")
         return {n: (counts[i], ms[i]) for i, n in enumerate(names)}
+
+
+class Batch:
+    """Many independent problems advanced together (fvgpu_batch_* handle).
+
+    Every problem keeps its own grid, parameters and dt; problems sharing the
+    plane and layout are advanced by one persistent kernel launch per stage.
+    All problems must share the precision (FV_PREC_FP64 or
+    FV_PREC_FP32_MIXED) and the time-stepping scheme.
+    """
+
+    def __init__(self, params_list):
+        self.lib = load_library()
+        self.params = [p.copy() for p in params_list]
+        arr = (FvParams * len(self.params))(*self.params)
+        h = C.c_void_p()
+        rc = self.lib.fvgpu_batch_create(arr, len(self.params), C.byref(h))
+        self._h = h
+        if rc:
+            msg = self.last_error()
+            self.close()
+            raise FvError(rc, msg)
+
+    def __len__(self):
+        return len(self.params)
+
+    def shape(self, i):
+        p = self.params[i]
+        return (p.Nz, p.Ny, p.Nx)
+
+    def last_error(self):
+        return (self.lib.fvgpu_batch_last_error(self._h) or b"").decode()
+
+    def _check(self, rc, what):
+        if rc:
+            raise FvError(rc, "%s: %s" % (what, self.last_error()))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.fvgpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_prim(self, i, rho, u=None, v=None, w=None, p=None):
+        arrs = [_as_field(a, self.shape(i)) for a in (rho, u, v, w, p)]
+        self._check(self.lib.fvgpu_batch_set_prim(self._h, int(i), *[_ptr(a) for a in arrs]), "batch_set_prim")
+
+    def get_prim(self, i):
+        arrs = [np.empty(self.shape(i), np.float64) for _ in range(5)]
+        self._check(self.lib.fvgpu_batch_get_prim(self._h, int(i), *[_ptr(a) for a in arrs]), "batch_get_prim")
+        return arrs
+
+    def run(self, nsteps):
+        self._check(self.lib.fvgpu_batch_run(self._h, int(nsteps)), "batch_run")
+
+    def times(self):
+        t = np.empty(len(self), np.float64)
+        self._check(self.lib.fvgpu_batch_times(self._h, _ptr(t)), "batch_times")
+        return t
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.fvgpu_batch_set_stream(self._h, C.c_void_p(stream_ptr)), "batch_set_stream")
+
+    def synchronize(self):
+        self._check(self.lib.fvgpu_batch_synchronize(self._h), "batch_synchronize")
+
+    def launch_count(self):
+        c = C.c_long()
+        self._check(self.lib.fvgpu_batch_launch_count(self._h, C.byref(c)), "batch_launch_count")
+        return c.value
+
+    def tiling(self):
+        """[(tx, ty)] tile shape chosen per group."""
+        ng = C.c_int()
+        tx = (C.c_int * 8)()
+        ty = (C.c_int * 8)()
+        self._check(self.lib.fvgpu_batch_tiling(self._h, C.byref(ng), tx, ty, 8), "batch_tiling")
+        return [(tx[g], ty[g]) for g in range(ng.value)]

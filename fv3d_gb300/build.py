@@ -25,9 +25,12 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["fv_stage2d.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp", "fv_batch.cpp", "fv_noalloc.cu"]
+LIB_SOURCES = ["fv_stage2d.cu", "fv_batch64.cu", "fv_batch32.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp",
+               "fv_batch.cpp", "fv_noalloc.cu"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
-FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_aux.cu"}
+FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_batch64.cu", "fv_aux.cu"}
+# the FP32-mixed kernels: approximate FP32 division/sqrt, FMA contraction
+FAST_MATH_SOURCES = {"fv_batch32.cu"}
 
 
 def _nvcc():
@@ -63,6 +66,8 @@ def _compile(src, obj, fmad):
            "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj + ".tmp"]
     if not fmad:
         cmd.insert(1, "-fmad=false")
+    if os.path.basename(src) in FAST_MATH_SOURCES:
+        cmd.insert(1, "-use_fast_math")
     if src.endswith(".cpp"):
         cmd[cmd.index("-c"):cmd.index("-c")] = ["-x", "cu"]
     subprocess.check_call(cmd)

@@ -35,10 +35,9 @@ __global__ void __launch_bounds__(256) reduce2d_fp64(const Grid2D G, const Field
   block_max_atomic(red, &ctrl->slot[slot], s_red);
 }
 
-__global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  StepCtrl& c = ctrl[i];
+// The control step of one problem: dt, active flag, parity, time and step
+// counter, next reduction slot cleared.
+__device__ __forceinline__ void step_control(StepCtrl& c, int mode_override, double dt_given) {
   const int p = (int)(c.step & 1);
   const int mode = mode_override >= 0 ? mode_override : c.mode;
   double dt;
@@ -69,6 +68,18 @@ __global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double 
     c.t = c.t + dt;
     c.step = c.step + 1;
   }
+}
+
+__global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) step_control(ctrl[i], mode_override, dt_given);
+}
+
+__global__ void batch_control_kernel(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override,
+                                     double dt_given) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) step_control(ctrl[i], mode_override, dt_given);
+  if (i < nq) queue[i] = 0u;
 }
 
 // primToCons in place (States.h:20-31).  Storage order in and out.
@@ -164,6 +175,13 @@ cudaError_t launch_reduce2d(const Grid2D& G, bool wact, Fields u, StepCtrl* ctrl
 
 cudaError_t launch_control(StepCtrl* ctrl, int n, int mode_override, double dt_given, cudaStream_t st) {
   control_kernel<<<(n + 127) / 128, 128, 0, st>>>(ctrl, n, mode_override, dt_given);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override, double dt_given,
+                                 cudaStream_t st) {
+  const int m = n > nq ? n : nq;
+  batch_control_kernel<<<(m + 127) / 128, 128, 0, st>>>(ctrl, n, queue, nq, mode_override, dt_given);
   return cudaGetLastError();
 }
 

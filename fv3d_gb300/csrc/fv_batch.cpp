@@ -1,48 +1,665 @@
-// fv_batch.cpp -- extern "C" entry points for batches of independent problems.
+// fv_batch.cpp -- extern "C" entry points for batches of independent problems
+// (fvgpu_batch_*).  No counterpart in the reference, which runs one problem
+// per process (main.cpp:25-30).
 //
-// Placeholder until the persistent batched kernel lands: every call reports
-// FV_ERR_UNSUPPORTED with a message.
+// A batch owns one device allocation holding every problem's two state
+// buffers, one control block per problem (each problem has its own dt, time
+// and CFL reduction) and a few work-queue counters.  Problems that share the
+// plane and the third-momentum layout form a group; one persistent kernel
+// launch per RK stage advances a whole group (fv_batch64.cu /
+// fv_batch32.cu).  Steps are replayed from a captured CUDA graph of
+// kGraphSteps steps.  The tile shape of each group is chosen by timing the
+// candidate shapes on the group's own data (autotuner), and remembered per
+// (precision, plane, layout, problem sizes) in memory and in a small cache
+// file (FV3D_TILE_CACHE, default $XDG_CACHE_HOME/fv3d_gb300/tiles.txt).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
 #include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include <cuda_runtime.h>
 
 #include "fv3d_gb300.h"
+#include "fv_kernels.h"
+
+namespace fv {
+int configure_grid(const fv_params& p, Grid2D* G, double* inv_tc, double* inv_visc, int* deg_bc,
+                   std::string* err);
+}
+
+using fv::BatchInst;
+using fv::Fields;
+using fv::Grid2D;
+using fv::StepCtrl;
+
+namespace {
+
+constexpr int kGraphSteps = 8;
+
+struct Group {
+  int plane = 0;
+  bool wact = false;
+  bool tc = false;
+  std::vector<int> members;
+  int shape = 0;
+  int ntiles = 0;
+  int grid = 0;
+  BatchInst* d_inst = nullptr;
+};
+
+}  // namespace
 
 struct fv_batch {
+  int n = 0;
+  int precision = FV_PREC_FP64;
+  int ts = FV_TS_RK2;
+  std::vector<fv_params> p;
+  std::vector<Grid2D> G;
+  std::vector<int> deg_bc;
+  std::vector<double> inv_tc, inv_visc;
+  std::vector<char> wact, state_set, slot_valid;
+  std::vector<Fields> A, B;
+  double* buf = nullptr;
+  double* scratch = nullptr;
+  long long max_fstride = 0;
+  StepCtrl* d_ctrl = nullptr;
+  StepCtrl* h_ctrl = nullptr;
+  unsigned* d_queue = nullptr;
+  std::vector<Group> groups;
+  bool prepared = false;
+  int flip = 0;  // Euler: current states are in B
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  long launches = 0;
   std::string err;
 };
 
 namespace {
-int Unsupported(fv_batch* b) {
-  if (b) b->err = "batched problems are not built yet";
-  return FV_ERR_UNSUPPORTED;
+
+int Fail(fv_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return code;
 }
+
+#define BCUDA(b, call)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return Fail((b), FV_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+void StorageOrder(int plane, int slot_of[5]) {
+  slot_of[0] = 0;
+  slot_of[1] = 1;
+  slot_of[2] = plane == fv::PLANE_XY ? 2 : 3;
+  slot_of[3] = plane == fv::PLANE_XY ? 3 : 2;
+  slot_of[4] = 4;
+}
+
+const Fields& Current(const fv_batch* b, int i) { return b->flip ? b->B[i] : b->A[i]; }
+
+// ---- tile-shape cache --------------------------------------------------
+
+std::mutex g_cache_mutex;
+std::map<std::string, std::pair<int, int>> g_cache;
+bool g_cache_loaded = false;
+
+std::string CachePath() {
+  if (const char* f = std::getenv("FV3D_TILE_CACHE")) return f;
+  std::string dir;
+  if (const char* x = std::getenv("XDG_CACHE_HOME")) dir = x;
+  else if (const char* h = std::getenv("HOME")) dir = std::string(h) + "/.cache";
+  else return "";
+  return dir + "/fv3d_gb300/tiles.txt";
+}
+
+void LoadCache() {
+  if (g_cache_loaded) return;
+  g_cache_loaded = true;
+  std::ifstream in(CachePath());
+  std::string key;
+  int tx, ty;
+  while (in >> key >> tx >> ty) g_cache[key] = {tx, ty};
+}
+
+void SaveCacheEntry(const std::string& key, int tx, int ty) {
+  const std::string path = CachePath();
+  if (path.empty()) return;
+  const std::string dir = path.substr(0, path.find_last_of('/'));
+  const std::string parent = dir.substr(0, dir.find_last_of('/'));
+  mkdir(parent.c_str(), 0755);
+  mkdir(dir.c_str(), 0755);
+  std::ofstream out(path, std::ios::app);
+  if (out) out << key << " " << tx << " " << ty << "\n";
+}
+
+// Key of a group: precision, plane, layout, conduction, solver mix and the
+// multiset of problem sizes (hashed).
+std::string GroupKey(const fv_batch* b, const Group& g) {
+  std::vector<std::pair<int, int>> sizes;
+  int rs_mask = 0;
+  bool visc = false;
+  for (int i : g.members) {
+    sizes.push_back({b->G[i].na, b->G[i].nb});
+    rs_mask |= 1 << (b->p[i].riemann_solver == FV_HLL ? 0 : 1);
+    visc = visc || b->G[i].visc;
+  }
+  std::sort(sizes.begin(), sizes.end());
+  unsigned long long h = 1469598103934665603ull;
+  long long cells = 0;
+  for (auto& s : sizes) {
+    h = (h ^ (unsigned long long)s.first) * 1099511628211ull;
+    h = (h ^ (unsigned long long)s.second) * 1099511628211ull;
+    cells += (long long)s.first * s.second;
+  }
+  std::ostringstream k;
+  k << "p" << b->precision << "_pl" << g.plane << "_w" << g.wact << "_tc" << g.tc << "_v" << visc << "_rs"
+    << rs_mask << "_ts" << b->ts << "_n" << g.members.size() << "_c" << cells << "_h" << std::hex << h;
+  return k.str();
+}
+
+int NumShapes(int precision, const fv::TileShape** shapes) {
+  return precision == FV_PREC_FP64 ? fv::batch_tile_shapes64(shapes) : fv::batch_tile_shapes32(shapes);
+}
+
+int Occupancy(const fv_batch* b, const Group& g, int shape) {
+  return b->precision == FV_PREC_FP64 ? fv::batch_stage_occupancy64(g.plane, g.wact, shape, g.tc)
+                                      : fv::batch_stage_occupancy32(g.plane, g.wact, shape, g.tc);
+}
+
+cudaError_t LaunchStage(const fv_batch* b, const Group& g, const BatchInst* insts, int ntiles, int grid,
+                        unsigned* queue, int kind, int flip) {
+  return b->precision == FV_PREC_FP64
+             ? fv::launch_batch_stage64(g.plane, g.wact, g.shape, insts, (int)g.members.size(), ntiles, queue, kind,
+                                        flip, grid, g.tc, b->stream)
+             : fv::launch_batch_stage32(g.plane, g.wact, g.shape, insts, (int)g.members.size(), ntiles, queue, kind,
+                                        flip, grid, g.tc, b->stream);
+}
+
+// Descriptors of group g for tile shape `shape` (tile numbering per group).
+std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, StepCtrl* ctrl_base, int* ntiles) {
+  const fv::TileShape* shapes;
+  NumShapes(b->precision, &shapes);
+  const int tx = shapes[shape].tx, ty = shapes[shape].ty;
+  std::vector<BatchInst> out;
+  int t0 = 0;
+  for (int i : g.members) {
+    BatchInst I;
+    std::memset(&I, 0, sizeof(I));
+    I.G = b->G[i];
+    I.A = b->A[i];
+    I.B = b->B[i];
+    I.ctrl = ctrl_base + i;
+    I.tiles_x = (I.G.na + tx - 1) / tx;
+    const int tiles_y = (I.G.nb + ty - 1) / ty;
+    I.tile0 = t0;
+    I.rs = b->p[i].riemann_solver == FV_HLL ? 0 : 1;
+    t0 += I.tiles_x * tiles_y;
+    out.push_back(I);
+  }
+  *ntiles = t0;
+  return out;
+}
+
+int SmCount() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+// Times the candidate shapes of a group on its own data.  Only the first
+// stage is run (RK2 stage 1 writes U* alone; Euler writes the idle buffer),
+// against a scratch copy of the control blocks, so the problems' state and
+// clocks are untouched.
+int Autotune(fv_batch* b, Group& g) {
+  const fv::TileShape* shapes;
+  const int ns = NumShapes(b->precision, &shapes);
+  if (const char* force = std::getenv("FV3D_TILE")) {
+    int tx = 0, ty = 0;
+    if (std::sscanf(force, "%dx%d", &tx, &ty) == 2)
+      for (int s = 0; s < ns; ++s)
+        if (shapes[s].tx == tx && shapes[s].ty == ty && Occupancy(b, g, s) > 0) {
+          g.shape = s;
+          return FV_OK;
+        }
+  }
+  const std::string key = GroupKey(b, g);
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    LoadCache();
+    auto it = g_cache.find(key);
+    if (it != g_cache.end())
+      for (int s = 0; s < ns; ++s)
+        if (shapes[s].tx == it->second.first && shapes[s].ty == it->second.second && Occupancy(b, g, s) > 0) {
+          g.shape = s;
+          return FV_OK;
+        }
+  }
+  StepCtrl* tune_ctrl = nullptr;
+  BatchInst* tune_inst = nullptr;
+  unsigned* tune_queue = nullptr;
+  BCUDA(b, cudaMalloc(&tune_ctrl, sizeof(StepCtrl) * b->n));
+  BCUDA(b, cudaMalloc(&tune_inst, sizeof(BatchInst) * g.members.size()));
+  BCUDA(b, cudaMalloc(&tune_queue, sizeof(unsigned)));
+  std::vector<StepCtrl> hc(b->n);
+  for (int i = 0; i < b->n; ++i) {
+    std::memset(&hc[i], 0, sizeof(StepCtrl));
+    hc[i].active = 1;
+    hc[i].dt_cur = 1.0e-9;
+  }
+  cudaMemcpyAsync(tune_ctrl, hc.data(), sizeof(StepCtrl) * b->n, cudaMemcpyHostToDevice, b->stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int kind = b->ts == FV_TS_RK2 ? fv::STAGE_RK_1 : fv::STAGE_EULER;
+  float best = 1e30f;
+  int best_s = -1;
+  const int saved = g.shape;
+  for (int s = 0; s < ns; ++s) {
+    const int occ = Occupancy(b, g, s);
+    if (occ <= 0) continue;
+    int ntiles = 0;
+    std::vector<BatchInst> d = Describe(b, g, s, tune_ctrl, &ntiles);
+    cudaMemcpyAsync(tune_inst, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice, b->stream);
+    g.shape = s;
+    const int grid = std::min(occ * SmCount(), ntiles);
+    float tot = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+      cudaMemsetAsync(tune_queue, 0, sizeof(unsigned), b->stream);
+      cudaEventRecord(e0, b->stream);
+      cudaError_t e = LaunchStage(b, g, tune_inst, ntiles, grid, tune_queue, kind, b->flip);
+      cudaEventRecord(e1, b->stream);
+      if (e != cudaSuccess) {
+        tot = 1e30f;
+        break;
+      }
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;  // first launch is a warm-up
+    }
+    if (tot < best) {
+      best = tot;
+      best_s = s;
+    }
+  }
+  g.shape = best_s < 0 ? saved : best_s;
+  cudaStreamSynchronize(b->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(tune_ctrl);
+  cudaFree(tune_inst);
+  cudaFree(tune_queue);
+  if (best_s < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
+  std::lock_guard<std::mutex> lock(g_cache_mutex);
+  g_cache[key] = {shapes[best_s].tx, shapes[best_s].ty};
+  SaveCacheEntry(key, shapes[best_s].tx, shapes[best_s].ty);
+  return FV_OK;
+}
+
+void ReleaseGroups(fv_batch* b) {
+  for (auto& g : b->groups)
+    if (g.d_inst) cudaFree(g.d_inst);
+  b->groups.clear();
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->prepared = false;
+}
+
+// Groups problems by (plane, third-momentum layout), picks tile shapes and
+// uploads the descriptors.
+int Prepare(fv_batch* b) {
+  if (b->prepared) return FV_OK;
+  ReleaseGroups(b);
+  for (int i = 0; i < b->n; ++i) {
+    Group* g = nullptr;
+    for (auto& h : b->groups)
+      if (h.plane == b->G[i].plane && h.wact == (bool)b->wact[i]) g = &h;
+    if (!g) {
+      b->groups.push_back(Group());
+      g = &b->groups.back();
+      g->plane = b->G[i].plane;
+      g->wact = b->wact[i];
+    }
+    g->members.push_back(i);
+    g->tc = g->tc || b->G[i].tc;
+  }
+  if (b->groups.size() > 4) return Fail(b, FV_ERR_UNSUPPORTED, "more than 4 batch groups");
+  for (auto& g : b->groups) {
+    int rc = Autotune(b, g);
+    if (rc) return rc;
+    std::vector<BatchInst> d = Describe(b, g, g.shape, b->d_ctrl, &g.ntiles);
+    BCUDA(b, cudaMalloc(&g.d_inst, sizeof(BatchInst) * d.size()));
+    BCUDA(b, cudaMemcpyAsync(g.d_inst, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice, b->stream));
+    g.grid = std::max(1, std::min(Occupancy(b, g, g.shape) * SmCount(), g.ntiles));
+  }
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  b->prepared = true;
+  return FV_OK;
+}
+
+int ReadCtrl(fv_batch* b) {
+  BCUDA(b, cudaMemcpyAsync(b->h_ctrl, b->d_ctrl, sizeof(StepCtrl) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return FV_OK;
+}
+
+// Makes every problem's reduction slot for its next step hold the CFL max
+// of its current state.
+int EnsureSlots(fv_batch* b) {
+  bool any = false;
+  for (int i = 0; i < b->n; ++i) any = any || !b->slot_valid[i];
+  if (!any) return FV_OK;
+  int rc = ReadCtrl(b);
+  if (rc) return rc;
+  for (int i = 0; i < b->n; ++i) {
+    if (b->slot_valid[i]) continue;
+    const int slot = (int)(b->h_ctrl[i].step & 1);
+    BCUDA(b, cudaMemsetAsync(&b->d_ctrl[i].slot[slot], 0, sizeof(unsigned long long), b->stream));
+    cudaError_t e = b->precision == FV_PREC_FP64
+                        ? fv::launch_reduce2d(b->G[i], b->wact[i], Current(b, i), b->d_ctrl + i, slot, b->stream)
+                        : fv::launch_reduce2d_mixed(b->G[i], b->wact[i], Current(b, i), b->d_ctrl + i, slot,
+                                                    b->stream);
+    if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "batch dt reduction: %s", cudaGetErrorString(e));
+    b->launches += 1;
+    b->slot_valid[i] = 1;
+  }
+  return FV_OK;
+}
+
+int KernelsPerStep(const fv_batch* b) {
+  return 1 + (int)b->groups.size() * (b->ts == FV_TS_RK2 ? 2 : 1);
+}
+
+// Control + stages of one step for every group.
+int EnqueueStep(fv_batch* b) {
+  const int nq = 2 * (int)b->groups.size();
+  cudaError_t e = fv::launch_batch_control(b->d_ctrl, b->n, b->d_queue, nq, 2, 0.0, b->stream);
+  for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
+    const Group& g = b->groups[gi];
+    unsigned* q = b->d_queue + 2 * gi;
+    if (b->ts == FV_TS_RK2) {
+      e = LaunchStage(b, g, g.d_inst, g.ntiles, g.grid, q, fv::STAGE_RK_1, 0);
+      if (e == cudaSuccess) e = LaunchStage(b, g, g.d_inst, g.ntiles, g.grid, q + 1, fv::STAGE_RK_2, 0);
+    } else {
+      e = LaunchStage(b, g, g.d_inst, g.ntiles, g.grid, q, fv::STAGE_EULER, b->flip);
+    }
+  }
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "batch step launch: %s", cudaGetErrorString(e));
+  if (b->ts != FV_TS_RK2) b->flip ^= 1;
+  return FV_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
-  (void)params;
-  (void)n;
   if (!out) return FV_ERR_PARAM;
-  *out = new fv_batch();
-  return Unsupported(*out);
+  *out = nullptr;
+  fv_batch* b = new fv_batch();
+  *out = b;
+  if (!params || n <= 0) return Fail(b, FV_ERR_PARAM, "need n > 0 parameter sets");
+  b->n = n;
+  b->precision = params[0].precision;
+  b->ts = params[0].time_stepping;
+  if (b->precision != FV_PREC_FP64 && b->precision != FV_PREC_FP32_MIXED)
+    return Fail(b, FV_ERR_PARAM, "unknown precision %d", b->precision);
+  b->p.assign(params, params + n);
+  b->G.resize(n);
+  b->deg_bc.resize(n);
+  b->inv_tc.resize(n);
+  b->inv_visc.resize(n);
+  b->wact.assign(n, 0);
+  b->state_set.assign(n, 0);
+  b->slot_valid.assign(n, 0);
+  std::vector<size_t> off(n);
+  size_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    if (params[i].precision != b->precision || params[i].time_stepping != b->ts)
+      return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: all problems of a batch share precision and time stepping", i);
+    fv_params q = params[i];
+    q.precision = FV_PREC_FP64;  // the grid checks are those of the FP64 handle
+    std::string err;
+    int rc = fv::configure_grid(q, &b->G[i], &b->inv_tc[i], &b->inv_visc[i], &b->deg_bc[i], &err);
+    if (rc) return Fail(b, rc, "problem %d: %s", i, err.c_str());
+    b->wact[i] = params[i].viscosity_active ? 1 : 0;
+    off[i] = total;
+    total += (size_t)10 * b->G[i].fstride;
+    b->max_fstride = std::max(b->max_fstride, b->G[i].fstride);
+  }
+  if (cudaMalloc(&b->buf, total * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&b->scratch, (size_t)5 * b->max_fstride * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&b->d_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
+      cudaMallocHost(&b->h_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
+      cudaMalloc(&b->d_queue, sizeof(unsigned) * 8) != cudaSuccess)
+    return Fail(b, FV_ERR_NOMEM, "batch allocation of %zu bytes failed", total * sizeof(double));
+  cudaMemset(b->buf, 0, total * sizeof(double));
+  cudaMemset(b->d_queue, 0, sizeof(unsigned) * 8);
+  b->A.resize(n);
+  b->B.resize(n);
+  for (int i = 0; i < n; ++i)
+    for (int v = 0; v < 5; ++v) {
+      b->A[i].f[v] = b->buf + off[i] + (size_t)v * b->G[i].fstride;
+      b->B[i].f[v] = b->buf + off[i] + (size_t)(5 + v) * b->G[i].fstride;
+    }
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return Fail(b, FV_ERR_CUDA, "stream creation failed");
+  b->stream = b->own_stream;
+  std::vector<StepCtrl> hc(n);
+  for (int i = 0; i < n; ++i) {
+    std::memset(&hc[i], 0, sizeof(StepCtrl));
+    hc[i].cfl = params[i].CFL;
+    hc[i].inv_tc = b->inv_tc[i];
+    hc[i].inv_visc = b->inv_visc[i];
+    hc[i].epsilon = params[i].epsilon;
+    hc[i].mode = 2;
+  }
+  BCUDA(b, cudaMemcpyAsync(b->d_ctrl, hc.data(), sizeof(StepCtrl) * n, cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return FV_OK;
 }
+
 int fvgpu_batch_destroy(fv_batch* b) {
+  if (!b) return FV_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  ReleaseGroups(b);
+  if (b->buf) cudaFree(b->buf);
+  if (b->scratch) cudaFree(b->scratch);
+  if (b->d_ctrl) cudaFree(b->d_ctrl);
+  if (b->h_ctrl) cudaFreeHost(b->h_ctrl);
+  if (b->d_queue) cudaFree(b->d_queue);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
   return FV_OK;
 }
+
 const char* fvgpu_batch_last_error(const fv_batch* b) { return b ? b->err.c_str() : "null handle"; }
-int fvgpu_batch_set_prim(fv_batch* b, int, const double*, const double*, const double*, const double*,
-                         const double*) {
-  return Unsupported(b);
+
+int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double* u, const double* v,
+                         const double* w, const double* pr) {
+  if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
+  if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);
+  const Grid2D& G = b->G[inst];
+  int slot_of[5];
+  StorageOrder(G.plane, slot_of);
+  const double* ref[5] = {rho, u, v, w, pr};
+  const double* src[5];
+  for (int k = 0; k < 5; ++k) src[slot_of[k]] = ref[k];
+  if (!src[0] || !src[4]) return Fail(b, FV_ERR_PARAM, "density and pressure arrays are required");
+  bool nonzero = false;
+  if (src[3])
+    for (long long c = 0; c < (long long)G.na * G.nb && !nonzero; ++c) nonzero = src[3][c] != 0.0;
+  const bool wact = b->p[inst].viscosity_active || nonzero;
+  if (wact && b->deg_bc[inst] == FV_BC_REFLECTING)
+    return Fail(b, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  if ((bool)b->wact[inst] != wact) b->prepared = false;
+  b->wact[inst] = wact;
+  if (!b->prepared) ReleaseGroups(b);
+  // FP64 values into the staging buffer (the current state for FP64, scratch
+  // for the mixed form), primToCons in place, then split into pairs (mixed)
+  Fields stage = b->precision == FV_PREC_FP64 ? Current(b, inst) : Fields();
+  if (b->precision != FV_PREC_FP64)
+    for (int k = 0; k < 5; ++k) stage.f[k] = b->scratch + (size_t)k * G.fstride;
+  const size_t rowb = (size_t)G.na * sizeof(double);
+  for (int k = 0; k < 5; ++k) {
+    if (src[k])
+      BCUDA(b, cudaMemcpy2DAsync(stage.f[k], (size_t)G.pitch * sizeof(double), src[k], rowb, rowb, G.nb,
+                                 cudaMemcpyHostToDevice, b->stream));
+    else
+      BCUDA(b, cudaMemsetAsync(stage.f[k], 0, (size_t)G.fstride * sizeof(double), b->stream));
+  }
+  cudaError_t e = fv::launch_prim_to_cons2d(G, stage, b->stream);
+  if (e == cudaSuccess && b->precision != FV_PREC_FP64)
+    e = fv::launch_pairs_from_double(G, stage, Current(b, inst), b->stream);
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "set_prim: %s", cudaGetErrorString(e));
+  b->launches += b->precision == FV_PREC_FP64 ? 1 : 2;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  b->state_set[inst] = 1;
+  b->slot_valid[inst] = 0;
+  return FV_OK;
 }
-int fvgpu_batch_get_prim(fv_batch* b, int, double*, double*, double*, double*, double*) { return Unsupported(b); }
-int fvgpu_batch_run(fv_batch* b, long) { return Unsupported(b); }
-int fvgpu_batch_times(fv_batch* b, double*) { return Unsupported(b); }
-int fvgpu_batch_set_stream(fv_batch* b, void*) { return Unsupported(b); }
-int fvgpu_batch_synchronize(fv_batch* b) { return Unsupported(b); }
-int fvgpu_batch_launch_count(const fv_batch* b, long* c) {
-  (void)b;
-  if (c) *c = 0;
+
+int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* v, double* w, double* pr) {
+  if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
+  if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);
+  if (!b->state_set[inst]) return Fail(b, FV_ERR_STATE, "problem %d has no state", inst);
+  const Grid2D& G = b->G[inst];
+  int slot_of[5];
+  StorageOrder(G.plane, slot_of);
+  double* ref[5] = {rho, u, v, w, pr};
+  double* dst[5];
+  for (int k = 0; k < 5; ++k) dst[slot_of[k]] = ref[k];
+  Fields S;
+  for (int k = 0; k < 5; ++k) S.f[k] = b->scratch + (size_t)k * G.fstride;
+  cudaError_t e;
+  if (b->precision == FV_PREC_FP64) {
+    e = fv::launch_cons_to_prim2d(G, Current(b, inst), S, b->stream);
+  } else {
+    e = fv::launch_double_from_pairs(G, Current(b, inst), S, b->stream);
+    if (e == cudaSuccess) e = fv::launch_cons_to_prim2d(G, S, S, b->stream);
+  }
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "get_prim: %s", cudaGetErrorString(e));
+  if (!b->wact[inst]) BCUDA(b, cudaMemsetAsync(S.f[3], 0, (size_t)G.fstride * sizeof(double), b->stream));
+  const size_t rowb = (size_t)G.na * sizeof(double);
+  for (int k = 0; k < 5; ++k)
+    if (dst[k])
+      BCUDA(b, cudaMemcpy2DAsync(dst[k], rowb, S.f[k], (size_t)G.pitch * sizeof(double), rowb, G.nb,
+                                 cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return FV_OK;
+}
+
+int fvgpu_batch_run(fv_batch* b, long nsteps) {
+  if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
+  if (nsteps < 0) return Fail(b, FV_ERR_PARAM, "nsteps must be >= 0");
+  for (int i = 0; i < b->n; ++i)
+    if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "problem %d has no state", i);
+  int rc = Prepare(b);
+  if (rc) return rc;
+  rc = EnsureSlots(b);
+  if (rc) return rc;
+  long done = 0;
+  // Euler ping-pong: graphs are captured for an even start (state in A)
+  if (b->ts != FV_TS_RK2 && b->flip && nsteps > 0) {
+    rc = EnqueueStep(b);
+    if (rc) return rc;
+    b->launches += KernelsPerStep(b);
+    done = 1;
+  }
+  if (nsteps - done >= kGraphSteps) {
+    if (!b->graph) {
+      cudaGraph_t g;
+      const int flip0 = b->flip;
+      BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < kGraphSteps; ++k) {
+        rc = EnqueueStep(b);
+        if (rc) {
+          cudaStreamEndCapture(b->stream, &g);
+          return rc;
+        }
+      }
+      BCUDA(b, cudaStreamEndCapture(b->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+      b->flip = flip0;
+    }
+    while (nsteps - done >= kGraphSteps) {
+      BCUDA(b, cudaGraphLaunch(b->graph, b->stream));
+      b->launches += (long)kGraphSteps * KernelsPerStep(b);
+      done += kGraphSteps;
+    }
+  }
+  for (; done < nsteps; ++done) {
+    rc = EnqueueStep(b);
+    if (rc) return rc;
+    b->launches += KernelsPerStep(b);
+  }
+  return FV_OK;
+}
+
+int fvgpu_batch_times(fv_batch* b, double* t) {
+  if (!b || !t) return b ? Fail(b, FV_ERR_PARAM, "null argument") : FV_ERR_PARAM;
+  int rc = ReadCtrl(b);
+  if (rc) return rc;
+  int bad = -1;
+  for (int i = 0; i < b->n; ++i) {
+    t[i] = b->h_ctrl[i].t;
+    if (b->h_ctrl[i].err && bad < 0) bad = i;
+  }
+  if (bad >= 0) return Fail(b, FV_ERR_NONFINITE, "problem %d met a non-finite state or dt", bad);
+  return FV_OK;
+}
+
+int fvgpu_batch_set_stream(fv_batch* b, void* stream) {
+  if (!b) return FV_ERR_PARAM;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return FV_OK;
+}
+
+int fvgpu_batch_synchronize(fv_batch* b) {
+  if (!b) return FV_ERR_PARAM;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return FV_OK;
+}
+
+int fvgpu_batch_launch_count(const fv_batch* b, long* count) {
+  if (!b || !count) return FV_ERR_PARAM;
+  *count = b->launches;
+  return FV_OK;
+}
+
+int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_groups) {
+  if (!b || !ngroups) return FV_ERR_PARAM;
+  for (int i = 0; i < b->n; ++i)
+    if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "problem %d has no state", i);
+  int rc = Prepare(b);
+  if (rc) return rc;
+  const fv::TileShape* shapes;
+  NumShapes(b->precision, &shapes);
+  *ngroups = (int)b->groups.size();
+  for (int g = 0; g < *ngroups && g < max_groups; ++g) {
+    if (tx) tx[g] = shapes[b->groups[g].shape].tx;
+    if (ty) ty[g] = shapes[b->groups[g].shape].ty;
+  }
   return FV_OK;
 }
 

@@ -1,0 +1,223 @@
+// fv_batch32.cu -- FP32-mixed persistent stage kernel for batches, plus the
+// mixed form's CFL reduction and its (hi, lo) pair conversions.  Built with
+// fast-math (FP32 division / sqrt approximations, FMA contraction), the pair
+// arithmetic of fv_tile32.cuh being written with adds only.
+#include "fv_tile32.cuh"
+
+namespace fv {
+
+namespace {
+
+constexpr TileShape kShapes32[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}};
+constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
+
+__device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts, int ninst, int t,
+                                             BatchInst* s_inst) {
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (insts[mid].tile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(insts + lo);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(s_inst);
+  for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
+}
+
+template <int PLANE, bool WACT, class TL>
+__global__ void __launch_bounds__(kTileThreads)
+batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
+  extern __shared__ float smem_f[];
+  __shared__ unsigned long long s_red[kTileThreads / 32];
+  __shared__ BatchInst s_inst;
+  __shared__ int s_tile;
+  for (;;) {
+    __syncthreads();  // the previous tile is finished with s_tile, s_inst and smem
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    fetch_inst32(insts, ninst, t, &s_inst);
+    __syncthreads();
+    const BatchInst& I = s_inst;
+    const int lt = t - I.tile0;
+    const int bx = lt % I.tiles_x, by = lt / I.tiles_x;
+    MixedFields M;
+    float2* src[5];
+    float2* dst[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      M.un[v] = reinterpret_cast<float2*>(I.A.f[v]);
+      M.us[v] = reinterpret_cast<float*>(I.B.f[v]);
+      float2* a = reinterpret_cast<float2*>(I.A.f[v]);
+      float2* b = reinterpret_cast<float2*>(I.B.f[v]);
+      src[v] = (kind == STAGE_EULER && flip) ? b : a;
+      dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
+    }
+    stage_tile32<PLANE, WACT, TL>(I.G, M, src, dst, I.ctrl, I.rs, kind, bx, by, smem_f, s_red);
+  }
+}
+
+template <int PLANE, bool WACT, int S>
+auto kernel_for() {
+  using TL = Tile<kShapes32[S].tx, kShapes32[S].ty>;
+  return batch_stage32<PLANE, WACT, TL>;
+}
+
+template <int S>
+size_t smem_for(bool wact, bool tc) {
+  using TL = Tile<kShapes32[S].tx, kShapes32[S].ty>;
+  return wact ? TileSmem<float, 5, TL>::bytes(tc) : TileSmem<float, 4, TL>::bytes(tc);
+}
+
+typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
+
+template <int PLANE, bool WACT>
+BatchKernel pick(int shape) {
+  switch (shape) {
+    case 0: return kernel_for<PLANE, WACT, 0>();
+    case 1: return kernel_for<PLANE, WACT, 1>();
+    case 2: return kernel_for<PLANE, WACT, 2>();
+    default: return kernel_for<PLANE, WACT, 3>();
+  }
+}
+
+BatchKernel pick_any(int plane, bool wact, int shape) {
+  if (plane == PLANE_XY) return wact ? pick<PLANE_XY, true>(shape) : pick<PLANE_XY, false>(shape);
+  return wact ? pick<PLANE_XZ, true>(shape) : pick<PLANE_XZ, false>(shape);
+}
+
+size_t smem_any(int shape, bool wact, bool tc) {
+  switch (shape) {
+    case 0: return smem_for<0>(wact, tc);
+    case 1: return smem_for<1>(wact, tc);
+    case 2: return smem_for<2>(wact, tc);
+    default: return smem_for<3>(wact, tc);
+  }
+}
+
+cudaError_t prepare(int plane, bool wact, int shape) {
+  static bool done[2][2][kNumShapes32] = {};
+  bool& flag = done[plane == PLANE_XY ? 0 : 1][wact ? 1 : 0][shape];
+  if (flag) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(pick_any(plane, wact, shape), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_any(shape, wact, true));
+  if (e == cudaSuccess) flag = true;
+  return e;
+}
+
+int grid_for(long long n, int block) {
+  long long b = (n + block - 1) / block;
+  if (b > 152 * 16) b = 152 * 16;
+  return b < 1 ? 1 : (int)b;
+}
+
+// CFL maximum of a state held as (hi, lo) pairs.
+template <int PLANE, bool WACT>
+__global__ void __launch_bounds__(256) reduce2d_mixed(const Grid2D G, const Fields pairs, StepCtrl* ctrl, int slot) {
+  __shared__ unsigned long long s_red[8];
+  float red = 0.0f;
+  bool bad = false;
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+    float u[5], e_lo = 0.0f;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (v == 3 && !WACT) {
+        u[v] = 0.0f;
+        continue;
+      }
+      const float2 w = reinterpret_cast<const float2*>(pairs.f[v])[o];
+      u[v] = v == 4 ? w.x : w.x + w.y;
+      if (v == 4) e_lo = w.y;
+    }
+    const float inv = inv_dt_hyp32<PLANE, WACT>(u, e_lo, G);
+    bad |= !(inv <= 3.0e38f);
+    red = fmaxf(red, inv);
+  }
+  if (bad) atomicOr(&ctrl->err, 1);
+  block_max_atomic((unsigned long long)__double_as_longlong((double)red), &ctrl->slot[slot], s_red);
+}
+
+// FP64 values -> (hi, lo) float pairs: hi = RN32(d), lo = RN32(d - hi).
+__global__ void pairs_from_double(const Grid2D G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double d = src.f[v][o];
+      const float hi = __double2float_rn(d);
+      const float lo = __double2float_rn(d - (double)hi);
+      reinterpret_cast<float2*>(dst.f[v])[o] = make_float2(hi, lo);
+    }
+  }
+}
+
+// (hi, lo) pairs -> FP64 values hi + lo (exact).
+__global__ void double_from_pairs(const Grid2D G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.nb;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const float2 w = reinterpret_cast<const float2*>(src.f[v])[o];
+      dst.f[v][o] = (double)w.x + (double)w.y;
+    }
+  }
+}
+
+}  // namespace
+
+int batch_tile_shapes32(const TileShape** shapes) {
+  *shapes = kShapes32;
+  return kNumShapes32;
+}
+
+int batch_stage_occupancy32(int plane, bool wact, int shape, bool tc) {
+  if (shape < 0 || shape >= kNumShapes32 || prepare(plane, wact, shape) != cudaSuccess) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pick_any(plane, wact, shape), kTileThreads,
+                                                    smem_any(shape, wact, tc)) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchInst* insts, int ninst, int ntiles,
+                                 unsigned* queue, int kind, int flip, int grid, bool tc, cudaStream_t st) {
+  if (shape < 0 || shape >= kNumShapes32) return cudaErrorInvalidValue;
+  cudaError_t e = prepare(plane, wact, shape);
+  if (e != cudaSuccess) return e;
+  pick_any(plane, wact, shape)<<<grid, kTileThreads, smem_any(shape, wact, tc), st>>>(insts, ninst, ntiles, queue,
+                                                                                       kind, flip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce2d_mixed(const Grid2D& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
+                                  cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.nb, 256);
+  if (G.plane == PLANE_XY) {
+    if (wact) reduce2d_mixed<PLANE_XY, true><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
+    else reduce2d_mixed<PLANE_XY, false><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
+  } else {
+    if (wact) reduce2d_mixed<PLANE_XZ, true><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
+    else reduce2d_mixed<PLANE_XZ, false><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_from_double(const Grid2D& G, Fields src, Fields dst_pairs, cudaStream_t st) {
+  pairs_from_double<<<grid_for((long long)G.na * G.nb, 256), 256, 0, st>>>(G, src, dst_pairs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_double_from_pairs(const Grid2D& G, Fields src_pairs, Fields dst, cudaStream_t st) {
+  double_from_pairs<<<grid_for((long long)G.na * G.nb, 256), 256, 0, st>>>(G, src_pairs, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace fv

@@ -49,4 +49,51 @@ cudaError_t launch_cons_to_prim2d(const Grid2D& G, Fields src, Fields dst, cudaS
 cudaError_t launch_totals2d(const Grid2D& G, Fields u, double* partial, int max_blocks, int* nblocks,
                             cudaStream_t stream);
 
+// ---- batches of independent problems ----------------------------------
+
+enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// One problem of a batch as the persistent kernels see it.  FP64: A = U^n,
+// B = U* (Euler: ping-pong).  FP32-mixed: A = U^n as float2 (hi, lo) pairs,
+// B = U* as float (RK2) or the second pair buffer (Euler).
+struct BatchInst {
+  Grid2D G;
+  Fields A, B;
+  StepCtrl* ctrl;
+  int tiles_x;  // tiles along a
+  int tile0;    // first tile of this problem in its group's tile numbering
+  int rs;       // 0 HLL, 1 HLLC
+  int pad;
+};
+
+// Tile shapes the autotuner chooses from (cells along a x along b).
+struct TileShape {
+  int tx, ty;
+};
+int batch_tile_shapes64(const TileShape** shapes);
+int batch_tile_shapes32(const TileShape** shapes);
+
+// Persistent stage kernel over a group of problems sharing plane and third
+// momentum: `grid` CTAs pull tiles from the work-queue counter *queue (reset
+// by launch_batch_control) until `ntiles` are done.  flip selects the Euler
+// ping-pong direction (B -> A when set); tc sizes shared memory for the
+// temperature tile.  Shape indexes batch_tile_shapes64/32.
+cudaError_t launch_batch_stage64(int plane, bool wact, int shape, const BatchInst* insts, int ninst, int ntiles,
+                                 unsigned* queue, int kind, int flip, int grid, bool tc, cudaStream_t stream);
+cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchInst* insts, int ninst, int ntiles,
+                                 unsigned* queue, int kind, int flip, int grid, bool tc, cudaStream_t stream);
+// Resident CTAs per SM of one batch stage kernel (0 on error).
+int batch_stage_occupancy64(int plane, bool wact, int shape, bool tc);
+int batch_stage_occupancy32(int plane, bool wact, int shape, bool tc);
+
+// launch_control for n problems plus a reset of nq work-queue counters.
+cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override, double dt_given,
+                                 cudaStream_t stream);
+
+// FP32-mixed helpers: CFL max of (hi, lo) pairs; pairs <-> FP64 values.
+cudaError_t launch_reduce2d_mixed(const Grid2D& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
+                                  cudaStream_t stream);
+cudaError_t launch_pairs_from_double(const Grid2D& G, Fields src, Fields dst_pairs, cudaStream_t stream);
+cudaError_t launch_double_from_pairs(const Grid2D& G, Fields src_pairs, Fields dst, cudaStream_t stream);
+
 }  // namespace fv

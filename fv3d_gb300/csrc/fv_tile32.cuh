@@ -1,0 +1,307 @@
+// fv_tile32.cuh -- one stage of one tile in the FP32-mixed form.
+//
+// Same algorithm and order as fv_tile64.cuh (the reference's euler_step),
+// with the precision split:
+//   - U^n, the state carried from step to step, is an FP32 (hi, lo) pair per
+//     value (float2, 8 bytes): about 48 significant bits, so accumulating
+//     many small increments loses nothing measurable;
+//   - U*, the RK2 intermediate, is plain FP32 (4 bytes);
+//   - primitives, slopes, face states, the Riemann solvers, gravity, thermal
+//     conduction and viscosity run in FP32 (fast-math division and sqrt);
+//   - the RK2 combination 0.5*(U^n + U* + dU) and every update of U^n are
+//     done on the (hi, lo) pairs with error-free two-sums (Knuth's TwoSum,
+//     Dekker's Fast2Sum);
+//   - the pressure recovery p = (gamma-1)(E - Ek) subtracts Ek from the
+//     (hi, lo) pair of E, so the cancellation at high Mach loses only Ek's own
+//     FP32 rounding;
+//   - the CFL maximum is taken over FP32 cell values and turned into dt in
+//     FP64 by the control kernel; conservation sums run in FP64.
+// Per cell-update the state traffic is 8 (read U^n) + 4 (write U*) + 4 (read
+// U*) + 8 (read U^n) + 8 (write U^n+1) = 32 bytes per stored field.
+#pragma once
+
+#include "fv_tile64.cuh"
+
+namespace fv {
+
+// Storage of one mixed-precision problem: U^n as (hi, lo) pairs, U* FP32.
+struct MixedFields {
+  float2* un[5];
+  float* us[5];
+};
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return make_float2(s, e);
+}
+
+// Dekker's Fast2Sum (|a| >= |b|): s + e == a + b exactly.
+__device__ __forceinline__ float2 fast_two_sum(float a, float b) {
+  const float s = a + b;
+  const float e = b - (s - a);
+  return make_float2(s, e);
+}
+
+// (hi, lo) + x -> normalised (hi, lo).
+__device__ __forceinline__ float2 pair_add(float2 a, float x) {
+  const float2 s = two_sum(a.x, x);
+  return fast_two_sum(s.x, s.y + a.y);
+}
+
+// (hi, lo) + (hi, lo) -> normalised (hi, lo).
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
+  const float2 s = two_sum(a.x, b.x);
+  return fast_two_sum(s.x, s.y + (a.y + b.y));
+}
+
+// consToPrim (States.h:34-45) in FP32 from storage order; E carries its low
+// part so that E - Ek cancels exactly when Ek is close to E.
+template <int PLANE, bool WACT>
+__device__ __forceinline__ void cons_to_prim32(const float u[5], float e_lo, float gm1, float q[5]) {
+  const float r = u[0];
+  const float rinv = 1.0f / r;
+  const float va = u[1] * rinv, vb = u[2] * rinv, vc = WACT ? u[3] * rinv : 0.0f;
+  const float vx = va, vy = PLANE == PLANE_XY ? vb : vc, vz = PLANE == PLANE_XY ? vc : vb;
+  const float Ek = 0.5f * r * (vx * vx + vy * vy + vz * vz);
+  q[0] = r;
+  q[1] = va;
+  q[2] = vb;
+  q[3] = vc;
+  q[4] = ((u[4] - Ek) + e_lo) * gm1;
+}
+
+template <int PLANE, bool WACT>
+__device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, const Grid2D& G) {
+  float q[5];
+  cons_to_prim32<PLANE, WACT>(u, e_lo, (float)G.gm1, q);
+  const float cs = sqrtf(q[4] * (float)G.gamma / q[0]);
+  const float vx = q[1], vy = PLANE == PLANE_XY ? q[2] : q[3], vz = PLANE == PLANE_XY ? q[3] : q[2];
+  return (cs + fabsf(vx)) * (float)G.inv_dx + (cs + fabsf(vy)) * (float)G.inv_dy +
+         (cs + fabsf(vz)) * (float)G.inv_dz;
+}
+
+// One FP32 face: minmod slopes, PLM states, Riemann flux (storage order).
+template <int PLANE, int DIR>
+__device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool plm, bool wb_z, float g_dz,
+                                            float gamma, float out[5]) {
+  float qL[5], qR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    if (plm) {
+      const float d01 = c[1][v] - c[0][v], d12 = c[2][v] - c[1][v], d23 = c[3][v] - c[2][v];
+      qL[v] = c[1][v] + minmod(d01, d12) * 0.5f;
+      qR[v] = c[2][v] - minmod(d12, d23) * 0.5f;
+    } else {
+      qL[v] = c[1][v];
+      qR[v] = c[2][v];
+    }
+  }
+  if (DIR == 1 && wb_z) {  // PCM_WB hydrostatic pressure in z (Update.h:27)
+    qL[4] = qL[4] + qL[0] * g_dz * 0.5f;
+    qR[4] = qR[4] - qR[0] * g_dz * 0.5f;
+  }
+  const Slots<float> L = to_slots<PLANE, DIR>(qL), R = to_slots<PLANE, DIR>(qR);
+  float f[5];
+  if (rs == 0)
+    riemann_hll<float>(L, R, gamma, f);
+  else
+    riemann_hllc<float>(L, R, gamma, f);
+  from_slots<PLANE, DIR>(f, out);
+}
+
+// One mixed-precision stage of tile (bx, by).  Inputs per kind:
+//   STAGE_RK_1 : read U^n (pairs) -> write U* (FP32)
+//   STAGE_RK_2 : read U* (FP32) and U^n (pairs) -> write U^n+1 (pairs, over U^n)
+//   STAGE_EULER: read U^n (pairs in `src`) -> write U^n+1 (pairs in `dst`)
+template <int PLANE, bool WACT, class TL>
+__device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields& M, float2* const src[5],
+                                             float2* const dst[5], StepCtrl* ctrl, int rs, int kind, int bx, int by,
+                                             float* smem, unsigned long long* s_red) {
+  constexpr int NV = WACT ? 5 : 4;
+  constexpr int TX = TL::TX, TY = TL::TY, HX = TL::HX, HY = TL::HY;
+  const TileSmem<float, NV, TL> S{smem};
+  const int tid = threadIdx.x;
+  const int x0 = bx * TX, y0 = by * TY;
+  const int active = ctrl->active;
+  const int parity = ctrl->parity;
+  const bool in_pairs = kind != STAGE_RK_2;
+
+  if (!active) {
+    if (kind == STAGE_EULER) {
+      for (int c = tid; c < TL::CELLS; c += kTileThreads) {
+        const int x = x0 + c % TX, y = y0 + c / TX;
+        if (x < G.na && y < G.nb) {
+          const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            if (WACT || v != 3) dst[v][o] = src[v][o];
+        }
+      }
+    }
+    return;
+  }
+  const float dt = (float)ctrl->dt_cur;
+  const float gamma = (float)G.gamma, gm1 = (float)G.gm1;
+
+  // ---- 1. tile + halo -> primitives (and temperature) ----
+  for (int idx = tid; idx < HX * HY; idx += kTileThreads) {
+    const int hy = idx / HX, hx = idx - hy * HX;
+    bool fa, fb;
+    const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
+    const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
+    const long long o = (long long)sb * G.pitch + sa;
+    float u[5], q[5], e_lo = 0.0f;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (v == 3 && !WACT) {
+        u[v] = 0.0f;
+        continue;
+      }
+      if (in_pairs) {
+        const float2 w = src[v][o];
+        u[v] = w.x + w.y;
+        if (v == 4) {
+          u[v] = w.x;
+          e_lo = w.y;
+        }
+      } else {
+        u[v] = M.us[v][o];
+      }
+    }
+    cons_to_prim32<PLANE, WACT>(u, e_lo, gm1, q);
+    if (fa) q[1] = -q[1];
+    if (fb) q[2] = -q[2];
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3) S.q(v, hy, hx) = q[v];
+    if (G.tc) S.temp(hy, hx) = q[4] / q[0];
+  }
+  __syncthreads();
+
+  // ---- 2. faces ----
+  const bool plm = G.recon == R_PLM;
+  const bool wb_z = PLANE == PLANE_XZ && G.recon == R_PCM_WB;
+  const float g_dz = (float)(G.g * G.dz);
+  for (int it = tid; it < TL::NFA_PAD + TL::NFB; it += kTileThreads) {
+    float c[4][5], f[5];
+    if (it < TL::NFA_PAD) {
+      if (it >= TL::NFA) continue;
+      const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + 2, fx + k) : 0.0f;
+      face_flux32<PLANE, 0>(c, rs, plm, wb_z, g_dz, gamma, f);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) S.fa(v, fy, fx) = f[v];
+    } else {
+      const int j = it - TL::NFA_PAD;
+      const int fy = j / TX, fx = j - fy * TX;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + k, fx + 2) : 0.0f;
+      face_flux32<PLANE, 1>(c, rs, plm, wb_z, g_dz, gamma, f);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) S.fb(v, fy, fx) = f[v];
+    }
+  }
+  __syncthreads();
+
+  // ---- 3-5. increments, accumulation on pairs, CFL term ----
+  const float dtdx = dt * (float)G.inv_dx;
+  const float dtdb = dt * (float)(PLANE == PLANE_XY ? G.inv_dy : G.inv_dz);
+  float red = 0.0f;
+  bool bad = false;
+#pragma unroll 1
+  for (int cidx = tid; cidx < TL::CELLS; cidx += kTileThreads) {
+    const int cx = cidx % TX, cy = cidx / TX;
+    const int x = x0 + cx, y = y0 + cy;
+    if (x >= G.na || y >= G.nb) continue;
+    const long long o = (long long)y * G.pitch + x;
+    float du[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      du[v] = (S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dtdx + (S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dtdb;
+    if (PLANE == PLANE_XZ && G.gravity) {
+      du[2] += dt * S.q(0, cy + 2, cx + 2) * (float)G.g;
+      du[4] += dt * 0.5f * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * (float)G.g;
+    }
+    // stage input at this cell, as a pair
+    float2 base[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (v == 3 && !WACT) continue;
+      base[v] = in_pairs ? src[v][o] : make_float2(M.us[v][o], 0.0f);
+    }
+    // density floor on the hydro update (Update.h:160), before TC / viscosity
+    {
+      const float2 rho = pair_add(base[0], du[0]);
+      if (rho.x + rho.y < 1.0e-6f) {
+        base[0] = make_float2(1.0e-6f, 0.0f);
+        du[0] = 0.0f;
+      }
+    }
+    if (G.tc) {
+      const float kf = (float)G.kappa;
+      const int hy = cy + 2, hx = cx + 2;
+      const float TC = S.temp(hy, hx);
+      const float FL = kf * (TC - S.temp(hy, hx - 1)) * (float)G.inv_dx;
+      const float FR = kf * (S.temp(hy, hx + 1) - TC) * (float)G.inv_dx;
+      const float ib = (float)(PLANE == PLANE_XY ? G.inv_dy : G.inv_dz);
+      const float FU = kf * (TC - S.temp(hy - 1, hx)) * ib;
+      const float FD = kf * (S.temp(hy + 1, hx) - TC) * ib;
+      du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
+    }
+    if (WACT && G.visc) {
+      PlaneStencil<PLANE, TileSmem<float, NV, TL>> st{S, cy + 2, cx + 2};
+      float vf[3][5];
+      viscous_fluxes<float>(st, (float)G.dx, (float)G.dy, (float)G.dz, (float)G.mu, vf);
+#pragma unroll
+      for (int var = 1; var < 5; ++var) {
+        const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
+        du[sv] += (vf[0][var] + vf[1][var] + vf[2][var]) * dt;
+      }
+    }
+    float fin[5], e_lo = 0.0f;
+    if (kind == STAGE_RK_1) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        if (v == 3 && !WACT) continue;
+        const float us = base[v].x + (base[v].y + du[v]);
+        M.us[v][o] = us;
+      }
+      continue;
+    }
+    // RK2 stage 2: U^n+1 = 0.5 * (U^n + U* + dU); Euler: U^n+1 = U^n + dU
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (v == 3 && !WACT) continue;
+      float2 r;
+      if (kind == STAGE_RK_2) {
+        r = pair_add(pair_add(M.un[v][o], base[v].x), du[v]);
+        r = make_float2(0.5f * r.x, 0.5f * r.y);
+      } else {
+        r = pair_add(base[v], du[v]);
+      }
+      dst[v][o] = r;
+      fin[v] = r.x;
+      if (v == 4) e_lo = r.y;
+    }
+    if (!WACT) fin[3] = 0.0f;
+    const float inv = inv_dt_hyp32<PLANE, WACT>(fin, e_lo, G);
+    bad |= !(inv <= 3.0e38f);  // NaN / inf: reported through the error flag
+    red = fmaxf(red, inv);
+  }
+  if (kind != STAGE_RK_1) {
+    if (bad) atomicOr(&ctrl->err, 1);
+    block_max_atomic((unsigned long long)__double_as_longlong((double)red), &ctrl->slot[parity ^ 1], s_red);
+  }
+}
+
+}  // namespace fv

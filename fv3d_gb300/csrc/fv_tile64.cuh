@@ -1,0 +1,412 @@
+// fv_tile64.cuh -- one FP64 stage of one tile: the body shared by the
+// single-problem kernel (fv_stage2d.cu) and the persistent batch kernel
+// (fv_batch64.cu).
+//
+// stage_tile64 performs a whole reference euler_step (Update.h:164-178) on a
+// TX x TY tile of cells with 256 threads:
+//   1. load the tile plus a 2-cell halo of the stage's input conserved state,
+//      synthesising ghost cells by index remapping (the X-then-Y ghost fill of
+//      BoundaryConditions.h:146-192, corners included), and convert to
+//      primitives (consToPrim, States.h:34-45) in shared memory;
+//   2. for every face of the tile: minmod slopes and PLM face states
+//      (Update.h:14-33,55-88) and one Riemann solve (RiemannSolvers.h) -- the
+//      reference solves every face twice, from each side, with equal inputs;
+//   3. the conservative update in the reference's X, Y, Z order with
+//      (F*dt)/d increments, gravity on the z sweep and the density floor
+//      (Update.h:145-160), then thermal conduction (ThermalConduction.h:38-96)
+//      and viscosity (Viscosity.h:127-253) from the same primitive tile;
+//   4. for RK2 stage 2 the SSP average 0.5*(U^n + U**) (Update.h:198-204);
+//   5. for the last stage of a step, consToPrim of the result and the
+//      hyperbolic CFL term of ComputeDt.h:28-54, reduced to one atomic max
+//      per tile (the TC/viscous terms are constants folded in by the control
+//      kernel).
+//
+// Rounding: every file including this one is compiled without FMA
+// contraction, every operation follows the reference's order, and the
+// cheaper exact forms of fv_exact64.cuh / fv_riemann64.cuh replace divisions
+// and comparisons, so the result is bit-identical to the reference's FP64 CPU
+// arithmetic.
+//
+// The degenerate third axis (one cell whose ghost layers equal it) adds
+// exactly zero to every flux difference in the reference arithmetic, so its
+// sweep is skipped; its cell size still enters dt.
+#pragma once
+
+#include "fv_kernels.h"
+#include "fv_plane2d.cuh"
+#include "fv_riemann64.cuh"
+
+namespace fv {
+
+constexpr int kTileThreads = 256;
+
+// Geometry of a TX x TY tile handled by kTileThreads threads.
+template <int TX_, int TY_>
+struct Tile {
+  static constexpr int TX = TX_, TY = TY_;
+  static constexpr int HX = TX + 4, HY = TY + 4;         // tile + 2-cell halo
+  static constexpr int NFA = (TX + 1) * TY;              // a-faces
+  static constexpr int NFA_PAD = (NFA + 31) / 32 * 32;   // keeps each warp on one face kind
+  static constexpr int NFB = TX * (TY + 1);              // b-faces
+  static constexpr int CELLS = TX * TY;
+  static_assert(CELLS % kTileThreads == 0, "tile cells must split evenly over the threads");
+};
+
+// Shared-memory layout for NV stored variables of element type T:
+//   Q [NV][HY][HX]   primitives of tile + halo
+//   FA[NV][TY][TX+1] a-face fluxes (storage order)
+//   FB[NV][TY+1][TX] b-face fluxes (storage order)
+//   TT[HY][HX]       temperature p/rho (thermal conduction only)
+template <class T, int NV, class TL>
+struct TileSmem {
+  T* base;
+  static constexpr int kQ = 0;
+  static constexpr int kFA = NV * TL::HY * TL::HX;
+  static constexpr int kFB = kFA + NV * TL::TY * (TL::TX + 1);
+  static constexpr int kT = kFB + NV * (TL::TY + 1) * TL::TX;
+  static constexpr int kEnd = kT;
+  static constexpr size_t bytes(bool tc) { return sizeof(T) * (size_t)(kEnd + (tc ? TL::HY * TL::HX : 0)); }
+  // storage variable (0 r, 1 a, 2 b, 3 c, 4 E/p) -> shared-memory slot
+  __device__ static constexpr int sv(int v) { return NV == 5 ? v : (v == 4 ? 3 : v); }
+  __device__ T& q(int v, int hy, int hx) const { return base[kQ + (sv(v) * TL::HY + hy) * TL::HX + hx]; }
+  __device__ T& fa(int v, int fy, int fx) const { return base[kFA + (sv(v) * TL::TY + fy) * (TL::TX + 1) + fx]; }
+  __device__ T& fb(int v, int fy, int fx) const { return base[kFB + (sv(v) * (TL::TY + 1) + fy) * TL::TX + fx]; }
+  __device__ T& temp(int hy, int hx) const { return base[kT + hy * TL::HX + hx]; }
+};
+
+// 3x3x3 stencil of the reference's viscosity over a 2-D plane: offsets along
+// the degenerate axis return the centre layer (its ghosts are copies of it).
+template <int PLANE, class SM>
+struct PlaneStencil {
+  SM s;
+  int hy, hx;
+  __device__ __forceinline__ auto operator()(int dk, int dj, int di, int var) const {
+    const int ob = PLANE == PLANE_XY ? dj - 1 : dk - 1;
+    return s.q(phys_slot<PLANE>(var), hy + ob, hx + di - 1);
+  }
+};
+
+// Viscous flux of Viscosity.h:149-243 for the three directions through a
+// 3x3x3 stencil accessor st(dk, dj, di, var) with var 1/2/3 = u/v/w, as the
+// reference writes it (including its z-branch index and field mix-ups).
+template <class T, class ST>
+__device__ __forceinline__ void viscous_fluxes(const ST& st, T dx, T dy, T dz, T mu, T vf[3][5]) {
+  const T four_thirds = T(4.0 / 3.0);
+  const T two_thirds = T(2.0 / 3.0);
+  const T one_over_dx = T(1) / dx;
+  const T one_over_dy = T(1) / dy;
+  const T one_over_dz = T(1) / dz;
+  const int IU = 1, IV = 2, IW = 3;
+#pragma unroll
+  for (int dir = 0; dir < 3; ++dir) {
+    T flux[5] = {T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int side = 1; side < 3; ++side) {
+      const T sign = (side == 1 ? T(-1) : T(1));
+      if (dir == 0) {
+        const T qiu = (st(1, 1, side, IU) + st(1, 1, side - 1, IU)) * T(0.5);
+        const T qiv = (st(1, 1, side, IV) + st(1, 1, side - 1, IV)) * T(0.5);
+        const T qiw = (st(1, 1, side, IW) + st(1, 1, side - 1, IW)) * T(0.5);
+        const T dudx = one_over_dx * (st(1, 1, side, IU) - st(1, 1, side - 1, IU));
+        const T dvdx = one_over_dx * (st(1, 1, side, IV) - st(1, 1, side - 1, IV));
+        const T dwdx = one_over_dx * (st(1, 1, side, IW) - st(1, 1, side - 1, IW));
+        const T dudy = T(0.25) * one_over_dy * (st(1, 2, side, IU) - st(1, 0, side, IU)
+                                              + st(1, 2, side - 1, IU) - st(1, 0, side - 1, IU));
+        const T dvdy = T(0.25) * one_over_dy * (st(1, 2, side, IV) - st(1, 0, side, IV)
+                                              + st(1, 2, side - 1, IV) - st(1, 0, side - 1, IV));
+        const T dudz = T(0.25) * one_over_dz * (st(2, 1, side, IU) - st(0, 1, side, IU)
+                                              + st(2, 1, side - 1, IU) - st(0, 1, side - 1, IU));
+        const T dwdz = T(0.25) * one_over_dz * (st(2, 1, side, IW) - st(0, 1, side, IW)
+                                              + st(2, 1, side - 1, IW) - st(0, 1, side - 1, IW));
+        const T tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
+        const T tau_xy = dvdx + dudy;
+        const T tau_xz = dwdx + dudz;
+        flux[1] += sign * mu * tau_xx;
+        flux[2] += sign * mu * tau_xy;
+        flux[3] += sign * mu * tau_xz;
+        flux[4] += sign * mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+      } else if (dir == 1) {
+        const T qiu = (st(1, side, 1, IU) + st(1, side - 1, 1, IU)) * T(0.5);
+        const T qiv = (st(1, side, 1, IV) + st(1, side - 1, 1, IV)) * T(0.5);
+        const T qiw = (st(1, side, 1, IW) + st(1, side - 1, 1, IW)) * T(0.5);
+        const T dudy = one_over_dy * (st(1, side, 1, IU) - st(1, side - 1, 1, IU));
+        const T dvdy = one_over_dy * (st(1, side, 1, IV) - st(1, side - 1, 1, IV));
+        const T dwdy = one_over_dy * (st(1, side, 1, IW) - st(1, side - 1, 1, IW));
+        const T dudx = T(0.25) * one_over_dx * (st(1, side, 2, IU) - st(1, side, 0, IU)
+                                              + st(1, side - 1, 2, IU) - st(1, side - 1, 0, IU));
+        const T dvdx = T(0.25) * one_over_dx * (st(1, side, 2, IV) - st(1, side, 0, IV)
+                                              + st(1, side - 1, 2, IV) - st(1, side - 1, 0, IV));
+        const T dwdz = T(0.25) * one_over_dz * (st(2, side, 1, IW) - st(0, side, 1, IW)
+                                              + st(2, side - 1, 1, IW) - st(0, side - 1, 1, IW));
+        const T dvdz = T(0.25) * one_over_dz * (st(2, side, 1, IV) - st(0, side, 1, IV)
+                                              + st(2, side - 1, 1, IV) - st(0, side - 1, 1, IV));
+        const T tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
+        const T tau_xy = dvdx + dudy;
+        const T tau_yz = dvdz + dwdy;
+        flux[1] += sign * mu * tau_xy;
+        flux[2] += sign * mu * tau_yy;
+        flux[3] += sign * mu * tau_yz;
+        flux[4] += sign * mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+      } else {
+        const T qiu = (st(side, 1, 1, IU) + st(side - 1, 1, 1, IU)) * T(0.5);
+        const T qiv = (st(side, 1, 1, IV) + st(side - 1, 1, 1, IV)) * T(0.5);
+        const T qiw = (st(side, 1, 1, IW) + st(side - 1, 1, 1, IW)) * T(0.5);
+        const T dudz = one_over_dz * (st(side, 1, 1, IU) - st(side - 1, 1, 1, IU));
+        const T dvdz = one_over_dz * (st(side, 1, 1, IV) - st(side - 1, 1, 1, IV));
+        const T dwdz = one_over_dz * (st(side, 1, 1, IW) - st(side - 1, 1, 1, IW));
+        const T dudx = T(0.25) * one_over_dx * (st(side, 1, 2, IU) - st(1, side, 0, IU)
+                                              + st(side - 1, 1, 2, IU) - st(1, side - 1, 0, IU));
+        const T dwdx = T(0.25) * one_over_dx * (st(side, 1, 2, IV) - st(1, side, 0, IW)
+                                              + st(side - 1, 1, 2, IV) - st(1, side - 1, 0, IW));
+        const T dvdy = T(0.25) * one_over_dz * (st(side, 2, 1, IW) - st(side, 0, 1, IV)
+                                              + st(side - 1, 2, 1, IW) - st(side - 1, 0, 1, IV));
+        const T dwdy = T(0.25) * one_over_dz * (st(side, 2, 1, IV) - st(side, 0, 1, IW)
+                                              + st(side - 1, 2, 1, IV) - st(side - 1, 0, 1, IW));
+        const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+        const T tau_xz = dudz + dwdx;
+        const T tau_yz = dvdz + dwdy;
+        flux[1] += sign * mu * tau_xz;
+        flux[2] += sign * mu * tau_yz;
+        flux[3] += sign * mu * tau_zz;
+        flux[4] += sign * mu * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) vf[dir][v] = flux[v];
+  }
+}
+
+// Slots of a sweep (swap_component, States.h:104-111) from storage order
+// (r, a, b, c, p): DIR 0 = reference IX (u, v, w); DIR 1 = IY (v, u, w) in
+// the x-y plane or IZ (w, v, u) in the x-z plane.
+template <int PLANE, int DIR, class T>
+__device__ __forceinline__ Slots<T> to_slots(const T q[5]) {
+  Slots<T> s;
+  s.r = q[0];
+  s.p = q[4];
+  if (DIR == 0) {
+    s.un = q[1];
+    s.t1 = PLANE == PLANE_XY ? q[2] : q[3];
+    s.t2 = PLANE == PLANE_XY ? q[3] : q[2];
+  } else {
+    s.un = q[2];
+    s.t1 = PLANE == PLANE_XY ? q[1] : q[3];
+    s.t2 = PLANE == PLANE_XY ? q[3] : q[1];
+  }
+  return s;
+}
+
+// Flux in slot order -> storage order (the inverse swap).
+template <int PLANE, int DIR, class T>
+__device__ __forceinline__ void from_slots(const T f[5], T out[5]) {
+  out[0] = f[0];
+  out[4] = f[4];
+  if (DIR == 0) {
+    out[1] = f[1];
+    out[2] = PLANE == PLANE_XY ? f[2] : f[3];
+    out[3] = PLANE == PLANE_XY ? f[3] : f[2];
+  } else {
+    out[2] = f[1];
+    out[1] = PLANE == PLANE_XY ? f[2] : f[3];
+    out[3] = PLANE == PLANE_XY ? f[3] : f[2];
+  }
+}
+
+// One FP64 face: slopes, face states and the Riemann flux, in storage order.
+// c[k][v] holds variable v of the four cells around the face (left-left,
+// left, right, right-right).
+template <int PLANE, bool WACT, int DIR>
+__device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool plm, bool wb_z, const Grid2D& G,
+                                            const Consts64& K, double out[5]) {
+  constexpr int ZS = WACT ? 0 : (PLANE == PLANE_XY ? 2 : 1);
+  double qL[5], qR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    if (v == 3 && !WACT) {
+      qL[v] = 0.0;
+      qR[v] = 0.0;
+      continue;
+    }
+    if (plm) {
+      const double d01 = c[1][v] - c[0][v], d12 = c[2][v] - c[1][v], d23 = c[3][v] - c[2][v];
+      qL[v] = recon_plus(c[1][v], minmod_exact(d01, d12));
+      qR[v] = recon_minus(c[2][v], minmod_exact(d12, d23));
+    } else {
+      qL[v] = c[1][v];
+      qR[v] = c[2][v];
+    }
+  }
+  if (DIR == 1 && wb_z) {  // PCM_WB hydrostatic pressure in z (Update.h:27)
+    qL[4] = qL[4] + 1.0 * qL[0] * G.g * G.dz * 0.5;
+    qR[4] = qR[4] + -1.0 * qR[0] * G.g * G.dz * 0.5;
+  }
+  const Slots<double> L = to_slots<PLANE, DIR>(qL), R = to_slots<PLANE, DIR>(qR);
+  double f[5];
+  if (rs == 0)
+    hll64<ZS>(L, R, K, f);
+  else
+    hllc64<ZS>(L, R, K, f);
+  from_slots<PLANE, DIR>(f, out);
+}
+
+// One stage of one tile (bx, by) of problem G; see the file comment.
+// rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
+// smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
+template <int PLANE, bool WACT, class TL>
+__device__ __forceinline__ void stage_tile64(const Grid2D& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                             StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
+                                             unsigned long long* s_red) {
+  constexpr int NV = WACT ? 5 : 4;
+  constexpr int TX = TL::TX, TY = TL::TY, HX = TL::HX, HY = TL::HY;
+  const TileSmem<double, NV, TL> S{smem};
+  const int tid = threadIdx.x;
+  const int x0 = bx * TX, y0 = by * TY;
+  const int active = ctrl->active;
+  const double dt = ctrl->dt_cur;
+  const int parity = ctrl->parity;
+
+  if (!active) {
+    // An inactive Euler step still hands its state on (ping-pong buffers);
+    // RK2 stages leave everything in place.
+    if (kind == STAGE_EULER) {
+      for (int c = tid; c < TL::CELLS; c += kTileThreads) {
+        const int x = x0 + c % TX, y = y0 + c / TX;
+        if (x < G.na && y < G.nb) {
+          const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            if (WACT || v != 3) uout.f[v][o] = uin.f[v][o];
+        }
+      }
+    }
+    return;
+  }
+
+  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+
+  // ---- 1. tile + halo -> primitives (and temperature) in shared memory ----
+  for (int idx = tid; idx < HX * HY; idx += kTileThreads) {
+    const int hy = idx / HX, hx = idx - hy * HX;
+    bool fa, fb;
+    const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
+    const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
+    const long long o = (long long)sb * G.pitch + sa;
+    double u[5], q[5], y;
+    u[0] = uin.f[0][o];
+    u[1] = uin.f[1][o];
+    u[2] = uin.f[2][o];
+    u[3] = WACT ? uin.f[3][o] : 0.0;
+    u[4] = uin.f[4][o];
+    cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+    if (fa) q[1] = -q[1];
+    if (fb) q[2] = -q[2];
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3) S.q(v, hy, hx) = q[v];
+    if (G.tc) S.temp(hy, hx) = div_by_rcp(q[4], q[0], y);
+  }
+  __syncthreads();
+
+  // ---- 2. every face of the tile: a faces first, then b faces ----
+  const bool plm = G.recon == R_PLM;
+  const bool wb_z = PLANE == PLANE_XZ && G.recon == R_PCM_WB;
+  for (int it = tid; it < TL::NFA_PAD + TL::NFB; it += kTileThreads) {
+    double c[4][5], f[5];
+    if (it < TL::NFA_PAD) {
+      if (it >= TL::NFA) continue;
+      const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + 2, fx + k) : 0.0;
+      face_flux64<PLANE, WACT, 0>(c, rs, plm, wb_z, G, K, f);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) S.fa(v, fy, fx) = f[v];
+    } else {
+      const int j = it - TL::NFA_PAD;
+      const int fy = j / TX, fx = j - fy * TX;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + k, fx + 2) : 0.0;
+      face_flux64<PLANE, WACT, 1>(c, rs, plm, wb_z, G, K, f);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) S.fb(v, fy, fx) = f[v];
+    }
+  }
+  __syncthreads();
+
+  // ---- 3-5. conservative update, sources, RK2 combination, CFL term ----
+  const double db = PLANE == PLANE_XY ? G.dy : G.dz;
+  const double inv_db = PLANE == PLANE_XY ? G.inv_dy : G.inv_dz;
+  const bool pow2_b = PLANE == PLANE_XY ? G.pow2_y : G.pow2_z;
+  unsigned long long red = 0ull;
+#pragma unroll 1
+  for (int cidx = tid; cidx < TL::CELLS; cidx += kTileThreads) {
+    const int cx = cidx % TX, cy = cidx / TX;
+    const int x = x0 + cx, y = y0 + cy;
+    if (x >= G.na || y >= G.nb) continue;
+    const long long o = (long long)y * G.pitch + x;
+    double un[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) un[v] = (WACT || v != 3) ? uin.f[v][o] : 0.0;
+
+    // IX sweep: un += (F(i-1/2) - F(i+1/2)) * dt / dx
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3)
+        un[v] = un[v] + div_cell((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx, G.pow2_x);
+    // IY sweep (x-y plane) or IZ sweep (x-z plane), gravity on IZ
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3)
+        un[v] = un[v] + div_cell((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, db, inv_db, pow2_b);
+    if (PLANE == PLANE_XZ && G.gravity) {
+      un[2] = un[2] + dt * S.q(0, cy + 2, cx + 2) * G.g;
+      un[4] = un[4] + dt * 0.5 * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g;
+    }
+    un[0] = fmax(1.0e-6, un[0]);
+
+    if (G.tc) {  // ThermalConduction.h:47-95, constant kappa, 2-D
+      const double kf = 0.5 * (G.kappa + G.kappa);
+      const int hy = cy + 2, hx = cx + 2;
+      const double TC = S.temp(hy, hx);
+      const double FL = div_cell(kf * (TC - S.temp(hy, hx - 1)), G.dx, G.inv_dx, G.pow2_x);
+      const double FR = div_cell(kf * (S.temp(hy, hx + 1) - TC), G.dx, G.inv_dx, G.pow2_x);
+      const double FU = div_cell(kf * (TC - S.temp(hy - 1, hx)), db, inv_db, pow2_b);
+      const double FD = div_cell(kf * (S.temp(hy + 1, hx) - TC), db, inv_db, pow2_b);
+      const double dtdx = div_cell(dt, G.dx, G.inv_dx, G.pow2_x);
+      const double dtdb = div_cell(dt, db, inv_db, pow2_b);
+      un[4] = un[4] + (dtdx * (FR - FL) + dtdb * (FD - FU));
+    }
+    if (WACT && G.visc) {  // Viscosity.h:245-251
+      PlaneStencil<PLANE, TileSmem<double, NV, TL>> st{S, cy + 2, cx + 2};
+      double vf[3][5];
+      viscous_fluxes<double>(st, G.dx, G.dy, G.dz, G.mu, vf);
+#pragma unroll
+      for (int var = 1; var < 5; ++var) {
+        const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
+        un[sv] = un[sv] + (vf[0][var] + vf[1][var] + vf[2][var]) * dt;
+      }
+    }
+    if (kind == STAGE_RK_2) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) un[v] = 0.5 * (u0.f[v][o] + un[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3) uout.f[v][o] = un[v];
+    if (kind != STAGE_RK_1) {
+      const double inv = inv_dt_hyp64<PLANE, WACT>(un, G);
+      const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
+      red = b > red ? b : red;
+      if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+    }
+  }
+  if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+}  // namespace fv

@@ -1,0 +1,178 @@
+"""Batches: many independent problems in one persistent launch per stage.
+
+FP64 batches must reproduce, bit for bit, each problem advanced alone (which
+itself reproduces the reference bit for bit), whatever tile shape the
+autotuner picks.  The FP32-mixed form must stay within a relative L1 density
+error of 1e-5 of the FP64 result.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import fv3d_gb300 as fv
+from fv3d_gb300 import problems
+from _helpers import rel_l1, rel_l1_fields
+
+pytestmark = pytest.mark.gpu
+
+MIXED_L1_RHO = 1e-5
+
+
+def mixed_set():
+    """Uneven sizes (some not powers of two), several gammas, both planes,
+    conduction/viscosity in one x-z problem (a second group)."""
+    return [
+        problems.sod(64, "x", gamma=1.3, nx_other=48),
+        problems.sedov(96, gamma=1.5, tend=1.0e30),
+        problems.sod(48, "y", gamma=1.62, nx_other=40),
+        problems.rayleigh_taylor(32, 96, kappa=1e-3, mu=1e-3, tend=1.0e30),
+        problems.sedov(64, gamma=1.2, tend=1.0e30),
+        problems.rayleigh_taylor(48, 144, riemann="hllc", tend=1.0e30),
+    ]
+
+
+def run_singles(probs, nsteps):
+    out, times = [], []
+    for pr in probs:
+        s = fv.Simulation(pr.params)
+        s.set_prim(*pr.prim)
+        t, n = s.advance(1.0e30, max_steps=nsteps)
+        assert n == nsteps
+        out.append(s.get_prim())
+        times.append(t)
+        s.close()
+    return out, times
+
+
+@pytest.mark.parametrize("nsteps", [3, 11])
+def test_fp64_batch_bitwise_equals_single(nsteps):
+    probs = mixed_set()
+    b = fv.Batch([p.params for p in probs])
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    b.run(nsteps)
+    t = b.times()
+    ref, ref_t = run_singles(probs, nsteps)
+    for i in range(len(probs)):
+        assert t[i] == ref_t[i], (i, t[i], ref_t[i])
+        for k, (x, y) in enumerate(zip(b.get_prim(i), ref[i])):
+            np.testing.assert_array_equal(x, y, err_msg="problem %d field %d" % (i, k))
+    assert len(set(t.tolist())) == len(probs)  # every problem has its own dt
+    assert b.launch_count() > 0
+    assert len(b.tiling()) == 3  # x-y; x-z with conduction/viscosity; x-z without
+
+
+def _run_forced_tile(tile, nsteps):
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+        "import fv3d_gb300 as fv\n"
+        "from test_gpu_batch import mixed_set\n"
+        "probs = mixed_set()\n"
+        "b = fv.Batch([p.params for p in probs])\n"
+        "[b.set_prim(i, *pr.prim) for i, pr in enumerate(probs)]\n"
+        "b.run(%d)\n"
+        "np.save(sys.argv[1], np.concatenate([np.stack(b.get_prim(i)).ravel() for i in range(len(probs))]))\n"
+        "print(b.tiling())\n"
+    ) % (os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.path.dirname(os.path.abspath(__file__)),
+         nsteps)
+    return code
+
+
+@pytest.mark.parametrize("tile", ["32x8", "16x16"])
+def test_fp64_batch_independent_of_tile_shape(tile, tmp_path):
+    """Forcing another tile shape (FV3D_TILE) gives the same bits."""
+    nsteps = 5
+    probs = mixed_set()
+    ref, _ = run_singles(probs, nsteps)
+    want = np.concatenate([np.stack(r).ravel() for r in ref])
+    out = str(tmp_path / "x.npy")
+    env = dict(os.environ, FV3D_TILE=tile)
+    r = subprocess.run([sys.executable, "-c", _run_forced_tile(tile, nsteps), out], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "(%s, %s)" % tuple(tile.split("x")) in r.stdout
+    np.testing.assert_array_equal(np.load(out), want)
+
+
+def test_fp64_batch_euler_pingpong():
+    probs = [problems.sod(64, "x"), problems.sedov(48, tend=1.0e30), problems.sod(40, "y")]
+    for pr in probs:
+        pr.params.time_stepping = fv._abi.FV_TS_EULER
+    b = fv.Batch([p.params for p in probs])
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    b.run(5)    # odd: the state ends in the second buffer
+    b.run(9)    # starts with one step to realign, then one graph replay
+    ref, ref_t = run_singles(probs, 14)
+    t = b.times()
+    for i in range(len(probs)):
+        assert t[i] == ref_t[i]
+        for x, y in zip(b.get_prim(i), ref[i]):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_mixed_batch_l1_against_fp64():
+    """FP32-mixed vs FP64 after 200 steps: density L1 <= 1e-5 (stated per
+    field in the assertion message)."""
+    probs = [problems.sod(128, "x", nx_other=32), problems.sedov(96, tend=1.0e30),
+             problems.sod(64, "y", gamma=1.6, nx_other=48), problems.sedov(128, gamma=1.3, tend=1.0e30)]
+    nsteps = 200
+    ref, ref_t = run_singles(probs, nsteps)
+    params = []
+    for pr in probs:
+        q = pr.params.copy()
+        q.precision = fv._abi.FV_PREC_FP32_MIXED
+        params.append(q)
+    b = fv.Batch(params)
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    b.run(nsteps)
+    t = b.times()
+    for i in range(len(probs)):
+        got = b.get_prim(i)
+        errs = rel_l1_fields(got, ref[i])
+        assert errs[0] <= MIXED_L1_RHO, (i, errs)
+        assert abs(t[i] - ref_t[i]) <= 1e-4 * ref_t[i], (i, t[i], ref_t[i])
+
+
+def test_mixed_batch_rt_with_diffusion():
+    probs = [problems.rayleigh_taylor(64, 192, kappa=1e-4, mu=1e-4, tend=1.0e30),
+             problems.rayleigh_taylor(32, 96, g=-0.15, ratio=2.5, kappa=1e-4, mu=1e-4, tend=1.0e30)]
+    nsteps = 100
+    ref, _ = run_singles(probs, nsteps)
+    params = []
+    for pr in probs:
+        q = pr.params.copy()
+        q.precision = fv._abi.FV_PREC_FP32_MIXED
+        params.append(q)
+    b = fv.Batch(params)
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    b.run(nsteps)
+    for i in range(len(probs)):
+        assert rel_l1(b.get_prim(i)[0], ref[i][0]) <= MIXED_L1_RHO
+
+
+def test_batch_nonfinite_reported():
+    probs = [problems.sedov(64, tend=1.0e30), problems.sod(64, "x")]
+    prim = [a.copy() for a in probs[1].prim]
+    prim[4][0, 3, 5] = -1.0
+    b = fv.Batch([p.params for p in probs])
+    b.set_prim(0, *probs[0].prim)
+    b.set_prim(1, *prim)
+    b.run(2)
+    with pytest.raises(fv.FvError) as e:
+        b.times()
+    assert e.value.status == 4
+
+
+def test_batch_rejects_mixed_settings():
+    a = problems.sod(32, "x").params
+    c = problems.sod(32, "x").params
+    c.time_stepping = fv._abi.FV_TS_EULER
+    with pytest.raises(fv.FvError) as e:
+        fv.Batch([a, c])
+    assert e.value.status == 2
