@@ -285,12 +285,130 @@ def run_gpu(args):
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(local),
             "rel_l1_vs_oracle_one_step": dict(zip(["rho", "u", "v", "w", "p"], l1))}
     if rank == 0:
+        if not args.no_variants:
+            line["variants"] = run_variants(torch, args, flush)
         line["cpu_baseline"] = cpu_sample(pr)
         print(json.dumps(line))
     sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _mixed(params):
+    import fv3d_gb300 as fv
+    q = params.copy()
+    q.precision = fv._abi.FV_PREC_FP32_MIXED
+    return q
+
+
+def _rel_l1(a, b):
+    den = float(np.abs(b).sum())
+    return float(np.abs(a - b).sum()) / den if den else 0.0
+
+
+def time_batch(torch, params_list, prims, nsteps, warmup, flush_each=None):
+    """Mcell-updates/s of a batch (CUDA events on its stream); with
+    flush_each, the L2 is flushed before every timed step (small states)."""
+    import fv3d_gb300 as fv
+    b = fv.Batch(params_list)
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    for i, pr in enumerate(prims):
+        b.set_prim(i, *pr)
+    tiles = b.tiling()
+    b.run(warmup)
+    b.synchronize()
+    l0 = b.launch_count()
+    cells = sum(int(np.prod(pr[0].shape)) for pr in prims)
+    if flush_each is None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(nsteps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    else:
+        ms = 0.0
+        for _ in range(nsteps):
+            with torch.cuda.stream(stream):
+                flush_each.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run(1)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+    b.times()  # surfaces any error
+    return b, {"mcell_updates_per_s": cells * nsteps / (ms / 1e3) / 1e6, "ms_per_step": ms / nsteps,
+               "cells": cells, "instances": len(params_list), "tiles": tiles,
+               "gpu_launches": b.launch_count() - l0}
+
+
+def l1_vs_fp64(torch, probs, nsteps, params_mixed):
+    """Per-field relative L1 (worst instance) of the mixed batch against the
+    bit-exact FP64 batch after nsteps steps."""
+    import fv3d_gb300 as fv
+    res = []
+    for plist in ([p.params for p in probs], params_mixed):
+        b = fv.Batch(plist)
+        for i, pr in enumerate(probs):
+            b.set_prim(i, *pr.prim)
+        b.run(nsteps)
+        res.append((b, b.times()))
+    worst = [0.0] * 5
+    for i in range(len(probs)):
+        a = res[1][0].get_prim(i)
+        r = res[0][0].get_prim(i)
+        for k in range(5):
+            worst[k] = max(worst[k], _rel_l1(a[k], r[k]))
+    tdrift = float(np.max(np.abs(res[1][1] - res[0][1]) / np.maximum(res[0][1], 1e-300)))
+    return {"steps": nsteps, "rel_l1_worst_instance": dict(zip(["rho", "u", "v", "w", "p"], worst)),
+            "rel_time_diff_max": tdrift}
+
+
+def run_variants(torch, args, flush):
+    """The other BASELINE configurations, timed on the same GPU."""
+    from fv3d_gb300 import problems
+    hbm_peak, _ = peaks()
+    out = {}
+
+    def add(name, r, bytes_per_cell_update, l1=None):
+        achieved = bytes_per_cell_update * r["mcell_updates_per_s"] * 1e6 / 1e9
+        r = dict(r)
+        r["roofline"] = {"bound": "hbm", "algo_bytes_per_cell_update": bytes_per_cell_update,
+                         "achieved_gbs": achieved, "frac": achieved / hbm_peak}
+        if l1 is not None:
+            r["vs_fp64"] = l1
+        out[name] = r
+
+    # FP32-mixed Rayleigh-Taylor 512x1536 (a batch of one)
+    rt = problem()
+    _, r = time_batch(torch, [_mixed(rt.params)], [rt.prim], args.steps, 5, flush_each=flush)
+    add("rayleigh_taylor_512x1536_fp32_mixed", r, 128, l1_vs_fp64(torch, [rt], 100, [_mixed(rt.params)]))
+
+    # config 3: 512 Sod / Sedov instances, sides 64..256, 200 steps, FP64 and mixed
+    b3 = problems.batch_sod_sedov(512)
+    _, r = time_batch(torch, [p.params for p in b3], [p.prim for p in b3], 16, 8)
+    add("batch512_sod_sedov_fp64", r, 160)
+    _, r = time_batch(torch, [_mixed(p.params) for p in b3], [p.prim for p in b3], 64, 8)
+    add("batch512_sod_sedov_fp32_mixed", r, 128, l1_vs_fp64(torch, b3, 200, [_mixed(p.params) for p in b3]))
+
+    # config 4: 64 Rayleigh-Taylor instances 256x768 .. 1024x3072 with kappa = mu = 1e-4
+    b4 = problems.batch_rt(64)
+    _, r = time_batch(torch, [p.params for p in b4], [p.prim for p in b4], 8, 3)
+    add("batch64_rt_fp64", r, 200)
+    _, r = time_batch(torch, [_mixed(p.params) for p in b4], [p.prim for p in b4], 32, 8)
+    add("batch64_rt_fp32_mixed", r, 160, l1_vs_fp64(torch, b4, args.rt_batch_l1_steps,
+                                                    [_mixed(p.params) for p in b4]))
+
+    # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
+    sh = problems.shear_layer(4096)
+    _, r = time_batch(torch, [sh.params], [sh.prim], 8, 3)
+    add("shear_layer_4096_fp64", r, 200)
+    _, r = time_batch(torch, [_mixed(sh.params)], [sh.prim], 32, 8)
+    add("shear_layer_4096_fp32_mixed", r, 160, l1_vs_fp64(torch, [sh], 50, [_mixed(sh.params)]))
+    return out
 
 
 def run_profile_case(args):
@@ -315,6 +433,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the workload's steps (for ncu); prints no JSON")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the other configurations (mixed, batched, shear layer)")
+    ap.add_argument("--rt-batch-l1-steps", type=int, default=50,
+                    help="steps of the 64-instance Rayleigh-Taylor batch compared with FP64 (the "
+                         "configuration asks for 500)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
