@@ -109,10 +109,8 @@ class Clocks:
 
 
 def dist_info():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from fv3d_gb300 import replicas
+    return replicas.dist_info()
 
 
 def cpu_sample(pr, seconds=15.0, max_steps=20, use_ref=False):
@@ -177,11 +175,10 @@ def run_gpu(args):
     import torch
     import fv3d_gb300 as fv
 
+    from fv3d_gb300 import replicas
     world, rank, local = dist_info()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    replicas.init("nccl")
     pr = problem()
     sim = fv.Simulation(pr.params)
     stream = torch.cuda.Stream()
@@ -198,8 +195,7 @@ def run_gpu(args):
     sim.synchronize()
     launches0 = sim.launch_count()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else tempfile.mkdtemp(),
                               "bench_clocks.csv"))
@@ -212,12 +208,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
     launches = sim.launch_count() - launches0
     ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(sum(ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = pr.cells * args.steps * world / (total_ms / 1e3) / 1e6
+    rate, slowest_s = replicas.aggregate_rate(pr.cells * args.steps, world, float(sum(ms)) / 1e3, device="cuda")
+    total_ms = slowest_s * 1e3
+    value = rate / 1e6
     sim.get_prim()  # surfaces any error of the timed steps
 
     # Dominant kernel: per-launch CUDA events (profile mode), L2 flushed per step.
@@ -290,8 +283,7 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu_sample(pr)
         print(json.dumps(line))
     sim.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.shutdown()
     return 0
 
 
@@ -412,16 +404,34 @@ def run_variants(torch, args, flush):
 
 
 def run_profile_case(args):
-    """Only the workload's steps (warm-up + steps), for launch lists and ncu
-    captures: no timing, no CPU baseline, no e2e."""
+    """Only a workload's steps (warm-up + steps), for launch lists and ncu
+    captures: no timing, no CPU baseline, no e2e.  Cases: fp64_rt (the bench
+    workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
+    batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
+    512-instance set, to keep captures small)."""
     import fv3d_gb300 as fv
-    pr = problem()
-    sim = fv.Simulation(pr.params)
-    sim.set_prim(*pr.prim)
-    sim.enqueue_steps(args.warmup + args.steps)
-    sim.synchronize()
-    sim.get_prim()
-    print("profile case done: %d steps of %s" % (args.warmup + args.steps, WORKLOAD))
+    from fv3d_gb300 import problems
+    case = args.profile_case
+    n = args.warmup + args.steps
+    if case == "fp64_rt":
+        pr = problem()
+        sim = fv.Simulation(pr.params)
+        sim.set_prim(*pr.prim)
+        sim.enqueue_steps(n)
+        sim.synchronize()
+        sim.get_prim()
+    else:
+        if case == "mixed_rt":
+            probs = [problem()]
+        else:
+            probs = problems.batch_sod_sedov(64)
+        plist = [p.params if case.endswith("fp64") else _mixed(p.params) for p in probs]
+        b = fv.Batch(plist)
+        for i, p in enumerate(probs):
+            b.set_prim(i, *p.prim)
+        b.run(n)
+        b.times()
+    print("profile case done: %d steps of %s" % (n, case))
     return 0
 
 
@@ -431,8 +441,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--profile-case", action="store_true",
-                    help="run only the workload's steps (for ncu); prints no JSON")
+    ap.add_argument("--profile-case", nargs="?", const="fp64_rt", default=None,
+                    choices=["fp64_rt", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64"],
+                    help="run only a workload's steps (for ncu); prints no JSON")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other configurations (mixed, batched, shear layer)")
     ap.add_argument("--rt-batch-l1-steps", type=int, default=50,

@@ -147,11 +147,12 @@ int main(int argc, char** argv) {
   double t = 0.0, dt = 0.0, next_save = 0.0;
   int ite = 0, next_log = 0;
   long steps = 0;
-  auto save = [&](double tt) {
+  // the loop announces its saves (main.cpp:64); the final one is silent (main.cpp:76)
+  auto save = [&](double tt, bool announce) {
     fvgpu_get_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data());
     char name[512];
     std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite++);
-    std::printf(" - Saving at time %g\n", tt);
+    if (announce) std::printf(" - Saving at time %g\n", tt);
     WriteRaw(name, q);
   };
   while (t + p.epsilon < p.tend) {
@@ -166,7 +167,7 @@ int main(int argc, char** argv) {
       next_log--;
     }
     if (save_needed) {
-      save(t);
+      save(t, true);
       next_save += p.save_freq;
     }
     if (device_loop) {
@@ -186,7 +187,7 @@ int main(int argc, char** argv) {
       ++steps;
     }
   }
-  save(t);
+  save(t, false);
   std::printf("done: %ld steps, t = %.17g\n", steps, t);
   fvgpu_destroy(s);
   return 0;

@@ -111,6 +111,18 @@ void SetExactConstants(Grid2D& G) {
   G.pow2_z = PowerOfTwo(G.dz);
   G.gm1 = G.gamma - 1.0;
   G.inv_gm1 = 1.0 / G.gm1;
+  G.gamma_f = (float)G.gamma;
+  G.gm1_f = (float)G.gm1;
+  G.g_f = (float)G.g;
+  G.kappa_f = (float)G.kappa;
+  G.mu_f = (float)G.mu;
+  G.g_dz_f = (float)(G.g * G.dz);
+  G.dx_f = (float)G.dx;
+  G.dy_f = (float)G.dy;
+  G.dz_f = (float)G.dz;
+  G.inv_dx_f = (float)G.inv_dx;
+  G.inv_dy_f = (float)G.inv_dy;
+  G.inv_dz_f = (float)G.inv_dz;
 }
 
 // Checks that the parameter set is one this build runs and fills the grid.

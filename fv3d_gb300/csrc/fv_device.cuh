@@ -52,6 +52,10 @@ struct Grid2D {
   double inv_dx, inv_dy, inv_dz;   // RN(1/d)
   int pow2_x, pow2_y, pow2_z;      // d is a power of two (1/d exact)
   double gm1, inv_gm1;             // gamma - 1, RN(1/(gamma - 1))
+  // FP32 copies for the mixed form (a double->float conversion runs on the
+  // slow FP64 pipe, so kernels never convert per cell).
+  float gamma_f, gm1_f, g_f, kappa_f, mu_f, g_dz_f;
+  float dx_f, dy_f, dz_f, inv_dx_f, inv_dy_f, inv_dz_f;
 };
 
 // Maps a cell index g (may be a ghost, -2 <= g < n+2) along an axis with n

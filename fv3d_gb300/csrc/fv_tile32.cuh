@@ -76,11 +76,10 @@ __device__ __forceinline__ void cons_to_prim32(const float u[5], float e_lo, flo
 template <int PLANE, bool WACT>
 __device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, const Grid2D& G) {
   float q[5];
-  cons_to_prim32<PLANE, WACT>(u, e_lo, (float)G.gm1, q);
-  const float cs = sqrtf(q[4] * (float)G.gamma / q[0]);
+  cons_to_prim32<PLANE, WACT>(u, e_lo, G.gm1_f, q);
+  const float cs = sqrtf(q[4] * G.gamma_f / q[0]);
   const float vx = q[1], vy = PLANE == PLANE_XY ? q[2] : q[3], vz = PLANE == PLANE_XY ? q[3] : q[2];
-  return (cs + fabsf(vx)) * (float)G.inv_dx + (cs + fabsf(vy)) * (float)G.inv_dy +
-         (cs + fabsf(vz)) * (float)G.inv_dz;
+  return (cs + fabsf(vx)) * G.inv_dx_f + (cs + fabsf(vy)) * G.inv_dy_f + (cs + fabsf(vz)) * G.inv_dz_f;
 }
 
 // One FP32 face: minmod slopes, PLM states, Riemann flux (storage order).
@@ -143,8 +142,8 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
     }
     return;
   }
-  const float dt = (float)ctrl->dt_cur;
-  const float gamma = (float)G.gamma, gm1 = (float)G.gm1;
+  const float dt = (float)ctrl->dt_cur;  // the one FP64 -> FP32 conversion per tile
+  const float gamma = G.gamma_f, gm1 = G.gm1_f;
 
   // ---- 1. tile + halo -> primitives (and temperature) ----
   for (int idx = tid; idx < HX * HY; idx += kTileThreads) {
@@ -184,7 +183,7 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
   // ---- 2. faces ----
   const bool plm = G.recon == R_PLM;
   const bool wb_z = PLANE == PLANE_XZ && G.recon == R_PCM_WB;
-  const float g_dz = (float)(G.g * G.dz);
+  const float g_dz = G.g_dz_f;
   for (int it = tid; it < TL::NFA_PAD + TL::NFB; it += kTileThreads) {
     float c[4][5], f[5];
     if (it < TL::NFA_PAD) {
@@ -214,8 +213,9 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
   __syncthreads();
 
   // ---- 3-5. increments, accumulation on pairs, CFL term ----
-  const float dtdx = dt * (float)G.inv_dx;
-  const float dtdb = dt * (float)(PLANE == PLANE_XY ? G.inv_dy : G.inv_dz);
+  const float inv_db = PLANE == PLANE_XY ? G.inv_dy_f : G.inv_dz_f;
+  const float dtdx = dt * G.inv_dx_f;
+  const float dtdb = dt * inv_db;
   float red = 0.0f;
   bool bad = false;
 #pragma unroll 1
@@ -229,8 +229,8 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
     for (int v = 0; v < 5; ++v)
       du[v] = (S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dtdx + (S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dtdb;
     if (PLANE == PLANE_XZ && G.gravity) {
-      du[2] += dt * S.q(0, cy + 2, cx + 2) * (float)G.g;
-      du[4] += dt * 0.5f * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * (float)G.g;
+      du[2] += dt * S.q(0, cy + 2, cx + 2) * G.g_f;
+      du[4] += dt * 0.5f * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g_f;
     }
     // stage input at this cell, as a pair
     float2 base[5];
@@ -248,20 +248,19 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
       }
     }
     if (G.tc) {
-      const float kf = (float)G.kappa;
+      const float kf = G.kappa_f;
       const int hy = cy + 2, hx = cx + 2;
       const float TC = S.temp(hy, hx);
-      const float FL = kf * (TC - S.temp(hy, hx - 1)) * (float)G.inv_dx;
-      const float FR = kf * (S.temp(hy, hx + 1) - TC) * (float)G.inv_dx;
-      const float ib = (float)(PLANE == PLANE_XY ? G.inv_dy : G.inv_dz);
-      const float FU = kf * (TC - S.temp(hy - 1, hx)) * ib;
-      const float FD = kf * (S.temp(hy + 1, hx) - TC) * ib;
+      const float FL = kf * (TC - S.temp(hy, hx - 1)) * G.inv_dx_f;
+      const float FR = kf * (S.temp(hy, hx + 1) - TC) * G.inv_dx_f;
+      const float FU = kf * (TC - S.temp(hy - 1, hx)) * inv_db;
+      const float FD = kf * (S.temp(hy + 1, hx) - TC) * inv_db;
       du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
     }
     if (WACT && G.visc) {
       PlaneStencil<PLANE, TileSmem<float, NV, TL>> st{S, cy + 2, cx + 2};
       float vf[3][5];
-      viscous_fluxes<float>(st, (float)G.dx, (float)G.dy, (float)G.dz, (float)G.mu, vf);
+      viscous_fluxes<float>(st, G.dx_f, G.dy_f, G.dz_f, G.mu_f, vf);
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
