@@ -258,9 +258,9 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
       du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
     }
     if (WACT && G.visc) {
-      PlaneStencil<PLANE, TileSmem<float, NV, TL>> st{S, cy + 2, cx + 2};
+      PlaneVel<PLANE, TileSmem<float, NV, TL>> P{S, cy + 2, cx + 2};
       float vf[3][5];
-      viscous_fluxes<float>(st, G.dx_f, G.dy_f, G.dz_f, G.mu_f, vf);
+      viscous_plane<PLANE, float>(P, G.dx_f, G.dy_f, G.dz_f, G.mu_f, vf);
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);

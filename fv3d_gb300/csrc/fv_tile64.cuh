@@ -74,107 +74,137 @@ struct TileSmem {
   __device__ T& temp(int hy, int hx) const { return base[kT + hy * TL::HX + hx]; }
 };
 
-// 3x3x3 stencil of the reference's viscosity over a 2-D plane: offsets along
-// the degenerate axis return the centre layer (its ghosts are copies of it).
-template <int PLANE, class SM>
-struct PlaneStencil {
-  SM s;
-  int hy, hx;
-  __device__ __forceinline__ auto operator()(int dk, int dj, int di, int var) const {
-    const int ob = PLANE == PLANE_XY ? dj - 1 : dk - 1;
-    return s.q(phys_slot<PLANE>(var), hy + ob, hx + di - 1);
-  }
-};
-
-// Viscous flux of Viscosity.h:149-243 for the three directions through a
-// 3x3x3 stencil accessor st(dk, dj, di, var) with var 1/2/3 = u/v/w, as the
-// reference writes it (including its z-branch index and field mix-ups).
-template <class T, class ST>
-__device__ __forceinline__ void viscous_fluxes(const ST& st, T dx, T dy, T dz, T mu, T vf[3][5]) {
+// Viscous fluxes of Viscosity.h:149-243 for a 2-D plane, with the reference's
+// arithmetic (including its z-branch index and field mix-ups) on every term
+// that is not an exact zero.  The stencil's offsets along the
+// one-cell axis read the centre layer, so in the literal formula every
+// derivative along that axis is c*((a - a) + b) - b) = 0 and the IY branch of
+// an x-z run cancels to (-mu*t) + mu*t = 0; dropping those terms returns the
+// same values (at most the sign of an exact zero differs).  P(r, c, var) reads
+// velocity var (1 u, 2 v, 3 w) of the cell at offset (r-1, c-1) along (b, a).
+// vf receives the per-direction fluxes of components u, v, w, E (index 1..4).
+template <int PLANE, class T, class PA>
+__device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T mu, T vf[3][5]) {
   const T four_thirds = T(4.0 / 3.0);
   const T two_thirds = T(2.0 / 3.0);
-  const T one_over_dx = T(1) / dx;
-  const T one_over_dy = T(1) / dy;
-  const T one_over_dz = T(1) / dz;
-  const int IU = 1, IV = 2, IW = 3;
+  const T odx = T(1) / dx, ody = T(1) / dy, odz = T(1) / dz;
+  const T c4x = T(0.25) * odx, c4y = T(0.25) * ody, c4z = T(0.25) * odz;
+  const int U = 1, V = 2, W = 3;
 #pragma unroll
-  for (int dir = 0; dir < 3; ++dir) {
-    T flux[5] = {T(0), T(0), T(0), T(0), T(0)};
+  for (int d = 0; d < 3; ++d)
 #pragma unroll
-    for (int side = 1; side < 3; ++side) {
-      const T sign = (side == 1 ? T(-1) : T(1));
-      if (dir == 0) {
-        const T qiu = (st(1, 1, side, IU) + st(1, 1, side - 1, IU)) * T(0.5);
-        const T qiv = (st(1, 1, side, IV) + st(1, 1, side - 1, IV)) * T(0.5);
-        const T qiw = (st(1, 1, side, IW) + st(1, 1, side - 1, IW)) * T(0.5);
-        const T dudx = one_over_dx * (st(1, 1, side, IU) - st(1, 1, side - 1, IU));
-        const T dvdx = one_over_dx * (st(1, 1, side, IV) - st(1, 1, side - 1, IV));
-        const T dwdx = one_over_dx * (st(1, 1, side, IW) - st(1, 1, side - 1, IW));
-        const T dudy = T(0.25) * one_over_dy * (st(1, 2, side, IU) - st(1, 0, side, IU)
-                                              + st(1, 2, side - 1, IU) - st(1, 0, side - 1, IU));
-        const T dvdy = T(0.25) * one_over_dy * (st(1, 2, side, IV) - st(1, 0, side, IV)
-                                              + st(1, 2, side - 1, IV) - st(1, 0, side - 1, IV));
-        const T dudz = T(0.25) * one_over_dz * (st(2, 1, side, IU) - st(0, 1, side, IU)
-                                              + st(2, 1, side - 1, IU) - st(0, 1, side - 1, IU));
-        const T dwdz = T(0.25) * one_over_dz * (st(2, 1, side, IW) - st(0, 1, side, IW)
-                                              + st(2, 1, side - 1, IW) - st(0, 1, side - 1, IW));
-        const T tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
-        const T tau_xy = dvdx + dudy;
-        const T tau_xz = dwdx + dudz;
-        flux[1] += sign * mu * tau_xx;
-        flux[2] += sign * mu * tau_xy;
-        flux[3] += sign * mu * tau_xz;
-        flux[4] += sign * mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
-      } else if (dir == 1) {
-        const T qiu = (st(1, side, 1, IU) + st(1, side - 1, 1, IU)) * T(0.5);
-        const T qiv = (st(1, side, 1, IV) + st(1, side - 1, 1, IV)) * T(0.5);
-        const T qiw = (st(1, side, 1, IW) + st(1, side - 1, 1, IW)) * T(0.5);
-        const T dudy = one_over_dy * (st(1, side, 1, IU) - st(1, side - 1, 1, IU));
-        const T dvdy = one_over_dy * (st(1, side, 1, IV) - st(1, side - 1, 1, IV));
-        const T dwdy = one_over_dy * (st(1, side, 1, IW) - st(1, side - 1, 1, IW));
-        const T dudx = T(0.25) * one_over_dx * (st(1, side, 2, IU) - st(1, side, 0, IU)
-                                              + st(1, side - 1, 2, IU) - st(1, side - 1, 0, IU));
-        const T dvdx = T(0.25) * one_over_dx * (st(1, side, 2, IV) - st(1, side, 0, IV)
-                                              + st(1, side - 1, 2, IV) - st(1, side - 1, 0, IV));
-        const T dwdz = T(0.25) * one_over_dz * (st(2, side, 1, IW) - st(0, side, 1, IW)
-                                              + st(2, side - 1, 1, IW) - st(0, side - 1, 1, IW));
-        const T dvdz = T(0.25) * one_over_dz * (st(2, side, 1, IV) - st(0, side, 1, IV)
-                                              + st(2, side - 1, 1, IV) - st(0, side - 1, 1, IV));
-        const T tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
-        const T tau_xy = dvdx + dudy;
-        const T tau_yz = dvdz + dwdy;
-        flux[1] += sign * mu * tau_xy;
-        flux[2] += sign * mu * tau_yy;
-        flux[3] += sign * mu * tau_yz;
-        flux[4] += sign * mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
-      } else {
-        const T qiu = (st(side, 1, 1, IU) + st(side - 1, 1, 1, IU)) * T(0.5);
-        const T qiv = (st(side, 1, 1, IV) + st(side - 1, 1, 1, IV)) * T(0.5);
-        const T qiw = (st(side, 1, 1, IW) + st(side - 1, 1, 1, IW)) * T(0.5);
-        const T dudz = one_over_dz * (st(side, 1, 1, IU) - st(side - 1, 1, 1, IU));
-        const T dvdz = one_over_dz * (st(side, 1, 1, IV) - st(side - 1, 1, 1, IV));
-        const T dwdz = one_over_dz * (st(side, 1, 1, IW) - st(side - 1, 1, 1, IW));
-        const T dudx = T(0.25) * one_over_dx * (st(side, 1, 2, IU) - st(1, side, 0, IU)
-                                              + st(side - 1, 1, 2, IU) - st(1, side - 1, 0, IU));
-        const T dwdx = T(0.25) * one_over_dx * (st(side, 1, 2, IV) - st(1, side, 0, IW)
-                                              + st(side - 1, 1, 2, IV) - st(1, side - 1, 0, IW));
-        const T dvdy = T(0.25) * one_over_dz * (st(side, 2, 1, IW) - st(side, 0, 1, IV)
-                                              + st(side - 1, 2, 1, IW) - st(side - 1, 0, 1, IV));
-        const T dwdy = T(0.25) * one_over_dz * (st(side, 2, 1, IV) - st(side, 0, 1, IW)
-                                              + st(side - 1, 2, 1, IV) - st(side - 1, 0, 1, IW));
-        const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
-        const T tau_xz = dudz + dwdx;
-        const T tau_yz = dvdz + dwdy;
-        flux[1] += sign * mu * tau_xz;
-        flux[2] += sign * mu * tau_yz;
-        flux[3] += sign * mu * tau_zz;
-        flux[4] += sign * mu * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
-      }
+    for (int v = 0; v < 5; ++v) vf[d][v] = T(0);
+  if (PLANE == PLANE_XY) {
+#pragma unroll
+    for (int s = 1; s < 3; ++s) {  // IX (Viscosity.h:163-186), z-derivatives vanish
+      const T sign = s == 1 ? T(-1) : T(1);
+      const T qiu = (P(1, s, U) + P(1, s - 1, U)) * T(0.5);
+      const T qiv = (P(1, s, V) + P(1, s - 1, V)) * T(0.5);
+      const T qiw = (P(1, s, W) + P(1, s - 1, W)) * T(0.5);
+      const T dudx = odx * (P(1, s, U) - P(1, s - 1, U));
+      const T dvdx = odx * (P(1, s, V) - P(1, s - 1, V));
+      const T dwdx = odx * (P(1, s, W) - P(1, s - 1, W));
+      const T dudy = c4y * (P(2, s, U) - P(0, s, U) + P(2, s - 1, U) - P(0, s - 1, U));
+      const T dvdy = c4y * (P(2, s, V) - P(0, s, V) + P(2, s - 1, V) - P(0, s - 1, V));
+      const T tau_xx = four_thirds * dudx - two_thirds * dvdy;
+      const T tau_xy = dvdx + dudy;
+      const T tau_xz = dwdx;
+      vf[0][1] += sign * mu * tau_xx;
+      vf[0][2] += sign * mu * tau_xy;
+      vf[0][3] += sign * mu * tau_xz;
+      vf[0][4] += sign * mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
     }
 #pragma unroll
-    for (int v = 0; v < 5; ++v) vf[dir][v] = flux[v];
+    for (int s = 1; s < 3; ++s) {  // IY (Viscosity.h:188-213), z-derivatives vanish
+      const T sign = s == 1 ? T(-1) : T(1);
+      const T qiu = (P(s, 1, U) + P(s - 1, 1, U)) * T(0.5);
+      const T qiv = (P(s, 1, V) + P(s - 1, 1, V)) * T(0.5);
+      const T qiw = (P(s, 1, W) + P(s - 1, 1, W)) * T(0.5);
+      const T dudy = ody * (P(s, 1, U) - P(s - 1, 1, U));
+      const T dvdy = ody * (P(s, 1, V) - P(s - 1, 1, V));
+      const T dwdy = ody * (P(s, 1, W) - P(s - 1, 1, W));
+      const T dudx = c4x * (P(s, 2, U) - P(s, 0, U) + P(s - 1, 2, U) - P(s - 1, 0, U));
+      const T dvdx = c4x * (P(s, 2, V) - P(s, 0, V) + P(s - 1, 2, V) - P(s - 1, 0, V));
+      const T tau_yy = four_thirds * dvdy - two_thirds * dudx;
+      const T tau_xy = dvdx + dudy;
+      const T tau_yz = dwdy;
+      vf[1][1] += sign * mu * tau_xy;
+      vf[1][2] += sign * mu * tau_yy;
+      vf[1][3] += sign * mu * tau_yz;
+      vf[1][4] += sign * mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+    }
+    // IZ (Viscosity.h:214-239) on the one-cell axis: qi is the centre, the z
+    // derivatives vanish, and its y terms do not depend on the side.
+    const T cu = P(1, 1, U), cv = P(1, 1, V), cw = P(1, 1, W);
+    const T dvdy = c4z * (P(2, 1, W) - P(0, 1, V) + P(2, 1, W) - P(0, 1, V));
+    const T dwdy = c4z * (P(2, 1, V) - P(0, 1, W) + P(2, 1, V) - P(0, 1, W));
+#pragma unroll
+    for (int s = 1; s < 3; ++s) {
+      const T sign = s == 1 ? T(-1) : T(1);
+      const T dudx = c4x * (P(1, 2, U) - P(s, 0, U) + P(1, 2, U) - P(s - 1, 0, U));
+      const T dwdx = c4x * (P(1, 2, V) - P(s, 0, W) + P(1, 2, V) - P(s - 1, 0, W));
+      const T tau_zz = -(two_thirds * (dudx + dvdy));
+      const T tau_xz = dwdx;
+      const T tau_yz = dwdy;
+      vf[2][1] += sign * mu * tau_xz;
+      vf[2][2] += sign * mu * tau_yz;
+      vf[2][3] += sign * mu * tau_zz;
+      vf[2][4] += sign * mu * (tau_xz * cu + tau_yz * cv + tau_zz * cw);
+    }
+  } else {
+#pragma unroll
+    for (int s = 1; s < 3; ++s) {  // IX, y-derivatives vanish
+      const T sign = s == 1 ? T(-1) : T(1);
+      const T qiu = (P(1, s, U) + P(1, s - 1, U)) * T(0.5);
+      const T qiv = (P(1, s, V) + P(1, s - 1, V)) * T(0.5);
+      const T qiw = (P(1, s, W) + P(1, s - 1, W)) * T(0.5);
+      const T dudx = odx * (P(1, s, U) - P(1, s - 1, U));
+      const T dvdx = odx * (P(1, s, V) - P(1, s - 1, V));
+      const T dwdx = odx * (P(1, s, W) - P(1, s - 1, W));
+      const T dudz = c4z * (P(2, s, U) - P(0, s, U) + P(2, s - 1, U) - P(0, s - 1, U));
+      const T dwdz = c4z * (P(2, s, W) - P(0, s, W) + P(2, s - 1, W) - P(0, s - 1, W));
+      const T tau_xx = four_thirds * dudx - two_thirds * dwdz;
+      const T tau_xy = dvdx;
+      const T tau_xz = dwdx + dudz;
+      vf[0][1] += sign * mu * tau_xx;
+      vf[0][2] += sign * mu * tau_xy;
+      vf[0][3] += sign * mu * tau_xz;
+      vf[0][4] += sign * mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+    }
+    // IY on the one-cell axis: every term is side-independent and cancels.
+#pragma unroll
+    for (int s = 1; s < 3; ++s) {  // IZ, with the reference's index/field mix-ups
+      const T sign = s == 1 ? T(-1) : T(1);
+      const T qiu = (P(s, 1, U) + P(s - 1, 1, U)) * T(0.5);
+      const T qiv = (P(s, 1, V) + P(s - 1, 1, V)) * T(0.5);
+      const T qiw = (P(s, 1, W) + P(s - 1, 1, W)) * T(0.5);
+      const T dudz = odz * (P(s, 1, U) - P(s - 1, 1, U));
+      const T dvdz = odz * (P(s, 1, V) - P(s - 1, 1, V));
+      const T dwdz = odz * (P(s, 1, W) - P(s - 1, 1, W));
+      const T dudx = c4x * (P(s, 2, U) - P(1, 0, U) + P(s - 1, 2, U) - P(1, 0, U));
+      const T dwdx = c4x * (P(s, 2, V) - P(1, 0, W) + P(s - 1, 2, V) - P(1, 0, W));
+      const T dvdy = c4z * (P(s, 1, W) - P(s, 1, V) + P(s - 1, 1, W) - P(s - 1, 1, V));
+      const T dwdy = c4z * (P(s, 1, V) - P(s, 1, W) + P(s - 1, 1, V) - P(s - 1, 1, W));
+      const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+      const T tau_xz = dudz + dwdx;
+      const T tau_yz = dvdz + dwdy;
+      vf[2][1] += sign * mu * tau_xz;
+      vf[2][2] += sign * mu * tau_yz;
+      vf[2][3] += sign * mu * tau_zz;
+      vf[2][4] += sign * mu * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+    }
   }
 }
+
+// Plane accessor for viscous_plane over a TileSmem primitive tile.
+template <int PLANE, class SM>
+struct PlaneVel {
+  SM s;
+  int hy, hx;
+  __device__ __forceinline__ auto operator()(int r, int c, int var) const {
+    return s.q(phys_slot<PLANE>(var), hy + r - 1, hx + c - 1);
+  }
+};
 
 // Slots of a sweep (swap_component, States.h:104-111) from storage order
 // (r, a, b, c, p): DIR 0 = reference IX (u, v, w); DIR 1 = IY (v, u, w) in
@@ -382,9 +412,9 @@ __device__ __forceinline__ void stage_tile64(const Grid2D& G, const Fields& uin,
       un[4] = un[4] + (dtdx * (FR - FL) + dtdb * (FD - FU));
     }
     if (WACT && G.visc) {  // Viscosity.h:245-251
-      PlaneStencil<PLANE, TileSmem<double, NV, TL>> st{S, cy + 2, cx + 2};
+      PlaneVel<PLANE, TileSmem<double, NV, TL>> P{S, cy + 2, cx + 2};
       double vf[3][5];
-      viscous_fluxes<double>(st, G.dx, G.dy, G.dz, G.mu, vf);
+      viscous_plane<PLANE, double>(P, G.dx, G.dy, G.dz, G.mu, vf);
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
