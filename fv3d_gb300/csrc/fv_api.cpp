@@ -113,6 +113,7 @@ void SetExactConstants(Grid2D& G) {
   G.inv_gm1 = 1.0 / G.gm1;
   G.gamma_f = (float)G.gamma;
   G.gm1_f = (float)G.gm1;
+  G.inv_gm1_f = (float)G.inv_gm1;
   G.g_f = (float)G.g;
   G.kappa_f = (float)G.kappa;
   G.mu_f = (float)G.mu;

@@ -24,8 +24,14 @@ __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts
   for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
 }
 
+#if FV_MIXED_MIN_CTAS > 0
+#define FV_MIXED_BOUNDS __launch_bounds__(kTileThreads, FV_MIXED_MIN_CTAS)
+#else
+#define FV_MIXED_BOUNDS __launch_bounds__(kTileThreads)
+#endif
+
 template <int PLANE, bool WACT, class TL>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void FV_MIXED_BOUNDS
 batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ float smem_f[];
   __shared__ unsigned long long s_red[kTileThreads / 32];

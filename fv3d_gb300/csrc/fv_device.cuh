@@ -54,7 +54,7 @@ struct Grid2D {
   double gm1, inv_gm1;             // gamma - 1, RN(1/(gamma - 1))
   // FP32 copies for the mixed form (a double->float conversion runs on the
   // slow FP64 pipe, so kernels never convert per cell).
-  float gamma_f, gm1_f, g_f, kappa_f, mu_f, g_dz_f;
+  float gamma_f, gm1_f, inv_gm1_f, g_f, kappa_f, mu_f, g_dz_f;
   float dx_f, dy_f, dz_f, inv_dx_f, inv_dy_f, inv_dz_f;
 };
 

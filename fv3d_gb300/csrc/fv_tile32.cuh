@@ -22,6 +22,16 @@
 
 #include "fv_tile64.cuh"
 
+// Cells whose loads one thread issues before converting any of them (phase 1).
+#ifndef FV_MIXED_LOAD_BATCH
+#define FV_MIXED_LOAD_BATCH 2
+#endif
+// Minimum resident CTAs per SM requested from the register allocator
+// (0: no bound beyond the 256 threads of a tile).
+#ifndef FV_MIXED_MIN_CTAS
+#define FV_MIXED_MIN_CTAS 4
+#endif
+
 namespace fv {
 
 // Storage of one mixed-precision problem: U^n as (hi, lo) pairs, U* FP32.
@@ -82,17 +92,104 @@ __device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, cons
   return (cs + fabsf(vx)) * G.inv_dx_f + (cs + fabsf(vy)) * G.inv_dy_f + (cs + fabsf(vz)) * G.inv_dz_f;
 }
 
+// minmod (Update.h:73-80) in FP32: 0 when the signs differ, else the argument
+// of smaller magnitude (ties to the second).
+__device__ __forceinline__ float minmod32(float a, float b) {
+  const float m = fabsf(a) < fabsf(b) ? a : b;
+  return a * b < 0.0f ? 0.0f : m;
+}
+
+// Per-state quantities of the FP32 solvers: sound speed, total energy and
+// the Euler flux (States.h:114-127) in the sweep's slot order.
+struct State32 {
+  float r, un, t1, t2, p, c, E, F[5];
+};
+
+__device__ __forceinline__ State32 state32(const Slots<float>& q, float gamma, float inv_gm1) {
+  State32 s;
+  s.r = q.r; s.un = q.un; s.t1 = q.t1; s.t2 = q.t2; s.p = q.p;
+  const float rinv = 1.0f / q.r;
+  s.c = sqrtf(gamma * q.p * rinv);
+  s.E = q.p * inv_gm1 + 0.5f * q.r * (q.un * q.un + q.t1 * q.t1 + q.t2 * q.t2);
+  s.F[0] = q.r * q.un;
+  s.F[1] = s.F[0] * q.un + q.p;
+  s.F[2] = s.F[0] * q.t1;
+  s.F[3] = s.F[0] * q.t2;
+  s.F[4] = (q.p + s.E) * q.un;
+  return s;
+}
+
+// HLL with Davis wave speeds (RiemannSolvers.h:6-36) in FP32.  The conserved
+// states of the star formula are (r, F0 = r un, r t1, r t2, E).
+__device__ __forceinline__ void hll32(const Slots<float>& qL, const Slots<float>& qR, float gamma, float inv_gm1,
+                                      float flux[5]) {
+  const State32 L = state32(qL, gamma, inv_gm1), R = state32(qR, gamma, inv_gm1);
+  const float SL = fminf(L.un - L.c, R.un - R.c);
+  const float SR = fmaxf(L.un + L.c, R.un + R.c);
+  if (SL >= 0.0f) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) flux[v] = L.F[v];
+  } else if (SR <= 0.0f) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) flux[v] = R.F[v];
+  } else {
+    const float uL[5] = {L.r, L.F[0], L.r * L.t1, L.r * L.t2, L.E};
+    const float uR[5] = {R.r, R.F[0], R.r * R.t1, R.r * R.t2, R.E};
+    const float inv = 1.0f / (SR - SL);
+    const float slsr = SL * SR;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) flux[v] = (SR * L.F[v] - SL * R.F[v] + slsr * (uR[v] - uL[v])) * inv;
+  }
+}
+
+// HLLC (RiemannSolvers.h:39-112) in FP32; the energy uses the normal and
+// first transverse velocity only, as the reference does.
+__device__ __forceinline__ void hllc32(const Slots<float>& L, const Slots<float>& R, float gamma, float inv_gm1,
+                                       float flux[5]) {
+  const float EL = 0.5f * L.r * (L.un * L.un + L.t1 * L.t1) + L.p * inv_gm1;
+  const float ER = 0.5f * R.r * (R.un * R.un + R.t1 * R.t1) + R.p * inv_gm1;
+  const float cmax = sqrtf(gamma * fmaxf(L.p / L.r, R.p / R.r));
+  const float SL = fminf(L.un, R.un) - cmax;
+  const float SR = fmaxf(L.un, R.un) + cmax;
+  const float rcL = L.r * (L.un - SL);
+  const float rcR = R.r * (SR - R.un);
+  const float iD = 1.0f / (rcR + rcL);
+  const float uS = (rcR * R.un + rcL * L.un + (L.p - R.p)) * iD;
+  const float pS = (rcR * L.p + rcL * R.p + rcL * rcR * (L.un - R.un)) * iD;
+  float sr, su, st1, st2, sp, E;
+  if (SL > 0.0f) {
+    sr = L.r; su = L.un; st1 = L.t1; st2 = L.t2; sp = L.p; E = EL;
+  } else if (uS > 0.0f || SR > 0.0f) {
+    const bool left = uS > 0.0f;
+    const float rK = left ? L.r : R.r, uK = left ? L.un : R.un, pK = left ? L.p : R.p, EK = left ? EL : ER;
+    const float SK = left ? SL : SR;
+    const float inv = 1.0f / (SK - uS);
+    sr = rK * (SK - uK) * inv;
+    E = ((SK - uK) * EK - pK * uK + pS * uS) * inv;
+    su = uS; sp = pS;
+    st1 = left ? L.t1 : R.t1;
+    st2 = left ? L.t2 : R.t2;
+  } else {
+    sr = R.r; su = R.un; st1 = R.t1; st2 = R.t2; sp = R.p; E = ER;
+  }
+  flux[0] = sr * su;
+  flux[1] = flux[0] * su + sp;
+  flux[2] = flux[0] * st1;
+  flux[3] = flux[0] * st2;
+  flux[4] = (E + sp) * su;
+}
+
 // One FP32 face: minmod slopes, PLM states, Riemann flux (storage order).
 template <int PLANE, int DIR>
 __device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool plm, bool wb_z, float g_dz,
-                                            float gamma, float out[5]) {
+                                            float gamma, float inv_gm1, float out[5]) {
   float qL[5], qR[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     if (plm) {
       const float d01 = c[1][v] - c[0][v], d12 = c[2][v] - c[1][v], d23 = c[3][v] - c[2][v];
-      qL[v] = c[1][v] + minmod(d01, d12) * 0.5f;
-      qR[v] = c[2][v] - minmod(d12, d23) * 0.5f;
+      qL[v] = c[1][v] + minmod32(d01, d12) * 0.5f;
+      qR[v] = c[2][v] - minmod32(d12, d23) * 0.5f;
     } else {
       qL[v] = c[1][v];
       qR[v] = c[2][v];
@@ -105,9 +202,9 @@ __device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool pl
   const Slots<float> L = to_slots<PLANE, DIR>(qL), R = to_slots<PLANE, DIR>(qR);
   float f[5];
   if (rs == 0)
-    riemann_hll<float>(L, R, gamma, f);
+    hll32(L, R, gamma, inv_gm1, f);
   else
-    riemann_hllc<float>(L, R, gamma, f);
+    hllc32(L, R, gamma, inv_gm1, f);
   from_slots<PLANE, DIR>(f, out);
 }
 
@@ -146,37 +243,43 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
   const float gamma = G.gamma_f, gm1 = G.gm1_f;
 
   // ---- 1. tile + halo -> primitives (and temperature) ----
-  for (int idx = tid; idx < HX * HY; idx += kTileThreads) {
-    const int hy = idx / HX, hx = idx - hy * HX;
-    bool fa, fb;
-    const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
-    const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
-    const long long o = (long long)sb * G.pitch + sa;
-    float u[5], q[5], e_lo = 0.0f;
+  // Batches of KB cells per thread: every load of a batch is issued before
+  // any of them is used, to keep many requests in flight.
+  constexpr int NCELL = HX * HY, KB = FV_MIXED_LOAD_BATCH;
+  for (int base = 0; base < NCELL; base += KB * kTileThreads) {
+    float2 w[KB][5];
+    bool ok[KB], fa[KB], fb[KB];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      if (v == 3 && !WACT) {
-        u[v] = 0.0f;
-        continue;
-      }
-      if (in_pairs) {
-        const float2 w = src[v][o];
-        u[v] = w.x + w.y;
-        if (v == 4) {
-          u[v] = w.x;
-          e_lo = w.y;
-        }
-      } else {
-        u[v] = M.us[v][o];
+    for (int k = 0; k < KB; ++k) {
+      const int idx = base + tid + k * kTileThreads;
+      ok[k] = idx < NCELL;
+      const int hy = idx / HX, hx = idx - hy * HX;
+      const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa[k]);
+      const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb[k]);
+      const long long o = (long long)sb * G.pitch + sa;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        w[k][v] = make_float2(0.0f, 0.0f);
+        if (!ok[k] || (v == 3 && !WACT)) continue;
+        w[k][v] = in_pairs ? src[v][o] : make_float2(M.us[v][o], 0.0f);
       }
     }
-    cons_to_prim32<PLANE, WACT>(u, e_lo, gm1, q);
-    if (fa) q[1] = -q[1];
-    if (fb) q[2] = -q[2];
 #pragma unroll
-    for (int v = 0; v < 5; ++v)
-      if (WACT || v != 3) S.q(v, hy, hx) = q[v];
-    if (G.tc) S.temp(hy, hx) = q[4] / q[0];
+    for (int k = 0; k < KB; ++k) {
+      if (!ok[k]) continue;
+      const int idx = base + tid + k * kTileThreads;
+      const int hy = idx / HX, hx = idx - hy * HX;
+      float u[5], q[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) u[v] = v == 4 ? w[k][v].x : w[k][v].x + w[k][v].y;
+      cons_to_prim32<PLANE, WACT>(u, w[k][4].y, gm1, q);
+      if (fa[k]) q[1] = -q[1];
+      if (fb[k]) q[2] = -q[2];
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) S.q(v, hy, hx) = q[v];
+      if (G.tc) S.temp(hy, hx) = q[4] / q[0];
+    }
   }
   __syncthreads();
 
@@ -193,7 +296,7 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
       for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + 2, fx + k) : 0.0f;
-      face_flux32<PLANE, 0>(c, rs, plm, wb_z, g_dz, gamma, f);
+      face_flux32<PLANE, 0>(c, rs, plm, wb_z, g_dz, gamma, G.inv_gm1_f, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
         if (WACT || v != 3) S.fa(v, fy, fx) = f[v];
@@ -204,7 +307,7 @@ __device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields&
       for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + k, fx + 2) : 0.0f;
-      face_flux32<PLANE, 1>(c, rs, plm, wb_z, g_dz, gamma, f);
+      face_flux32<PLANE, 1>(c, rs, plm, wb_z, g_dz, gamma, G.inv_gm1_f, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
         if (WACT || v != 3) S.fb(v, fy, fx) = f[v];
