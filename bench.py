@@ -25,6 +25,7 @@ Multi-GPU (torchrun, one rank per GPU): independent replicas, no collective
 on the data path; value = total cell-updates of all ranks / max rank time.
 """
 import argparse
+import math
 import json
 import os
 import subprocess
@@ -363,14 +364,29 @@ def l1_vs_fp64(torch, probs, nsteps, params_mixed):
         b.run(nsteps)
         res.append((b, b.times()))
     worst = [0.0] * 5
-    for i in range(len(probs)):
+    drift = {"fp64": [0.0, 0.0], "mixed": [0.0, 0.0]}
+    for i, pr in enumerate(probs):
         a = res[1][0].get_prim(i)
         r = res[0][0].get_prim(i)
         for k in range(5):
             worst[k] = max(worst[k], _rel_l1(a[k], r[k]))
+        m0, e0 = _mass_energy(pr.prim, pr.params.gamma0)
+        for key, st in (("fp64", r), ("mixed", a)):
+            m1, e1 = _mass_energy(st, pr.params.gamma0)
+            drift[key][0] = max(drift[key][0], abs(m1 - m0) / abs(m0))
+            drift[key][1] = max(drift[key][1], abs(e1 - e0) / abs(e0))
     tdrift = float(np.max(np.abs(res[1][1] - res[0][1]) / np.maximum(res[0][1], 1e-300)))
     return {"steps": nsteps, "rel_l1_worst_instance": dict(zip(["rho", "u", "v", "w", "p"], worst)),
-            "rel_time_diff_max": tdrift}
+            "rel_time_diff_max": tdrift,
+            "rel_drift_worst_instance": {k: {"mass": v[0], "energy": v[1]} for k, v in drift.items()}}
+
+
+def _mass_energy(prim, gamma):
+    """Sum over cells of rho and of E = p/(gamma-1) + rho |u|^2 / 2 (FP64,
+    cell volume omitted: the drift is relative)."""
+    rho, u, v, w, p = (np.asarray(a, dtype=np.float64) for a in prim)
+    E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w)
+    return float(math.fsum(rho.ravel())), float(math.fsum(E.ravel()))
 
 
 def run_variants(torch, args, flush):
@@ -408,6 +424,20 @@ def run_variants(torch, args, flush):
     add("batch64_rt_fp32_mixed", r, 160, l1_vs_fp64(torch, b4, args.rt_batch_l1_steps,
                                                     [_mixed(p.params) for p in b4]))
 
+    # config 0: Sedov 256^2 (HLLC, absorbing), FP64 and mixed
+    se = problems.sedov(256)
+    _, r = time_batch(torch, [se.params], [se.prim], 64, 8)
+    add("sedov_256_fp64", r, 160)
+    _, r = time_batch(torch, [_mixed(se.params)], [se.prim], 64, 8)
+    add("sedov_256_fp32_mixed", r, 128, l1_vs_fp64(torch, [se], 200, [_mixed(se.params)]))
+
+    # config 1b: thermal pulse 1024^2 with conduction and viscosity, 200 fixed steps
+    tp = problems.thermal_pulse(1024)
+    _, r = time_batch(torch, [tp.params], [tp.prim], 16, 4)
+    add("thermal_pulse_1024_fp64", r, 200)
+    _, r = time_batch(torch, [_mixed(tp.params)], [tp.prim], 64, 8)
+    add("thermal_pulse_1024_fp32_mixed", r, 160, l1_vs_fp64(torch, [tp], 200, [_mixed(tp.params)]))
+
     # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
     sh = problems.shear_layer(4096)
     _, r = time_batch(torch, [sh.params], [sh.prim], 8, 3)
@@ -422,7 +452,8 @@ def run_profile_case(args):
     captures: no timing, no CPU baseline, no e2e.  Cases: fp64_rt (the bench
     workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
     batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
-    512-instance set, to keep captures small)."""
+    512-instance set, to keep captures small), shear_mixed / shear_fp64 (the
+    4096^2 shear layer, a state larger than L2)."""
     import fv3d_gb300 as fv
     from fv3d_gb300 import problems
     case = args.profile_case
@@ -437,6 +468,8 @@ def run_profile_case(args):
     else:
         if case == "mixed_rt":
             probs = [problem()]
+        elif case.startswith("shear"):
+            probs = [problems.shear_layer(4096)]
         else:
             probs = problems.batch_sod_sedov(64)
         plist = [p.params if case.endswith("fp64") else _mixed(p.params) for p in probs]
@@ -456,7 +489,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-case", nargs="?", const="fp64_rt", default=None,
-                    choices=["fp64_rt", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64"],
+                    choices=["fp64_rt", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64", "shear_mixed",
+                             "shear_fp64"],
                     help="run only a workload's steps (for ncu); prints no JSON")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other configurations (mixed, batched, shear layer)")
