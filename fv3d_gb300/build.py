@@ -12,7 +12,10 @@ operation, so every FP64 operation rounds exactly as in the reference's FP64
 CPU build and the plain path reproduces it bit for bit.  Fused operations in
 those files are written out explicitly (fma()) only where they are exact by
 construction.  ``variant="fmad"`` lets the compiler contract them too (faster,
-no longer bit-exact), for comparison.
+no longer bit-exact), for comparison.  Host code is compiled with
+``-ffp-contract=off`` everywhere: the host computes constants the kernels use
+(the B02 conductivity table, the CFL constants) with the reference's rounding
+on both x86-64 and aarch64 hosts.
 """
 import concurrent.futures as cf
 import os
@@ -25,10 +28,10 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["fv_stage2d.cu", "fv_batch64.cu", "fv_batch32.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp",
+LIB_SOURCES = ["fv_stage2d.cu", "fv_stage3d.cu", "fv_batch64.cu", "fv_batch32.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp",
                "fv_batch.cpp", "fv_noalloc.cu"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
-FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_batch64.cu", "fv_aux.cu"}
+FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_stage3d.cu", "fv_batch64.cu", "fv_aux.cu"}
 # the FP32-mixed kernels: approximate FP32 division/sqrt, FMA contraction
 FAST_MATH_SOURCES = {"fv_batch32.cu"}
 
@@ -62,7 +65,7 @@ def _stale(target, deps):
 
 
 def _compile(src, obj, fmad):
-    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
            "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj + ".tmp"]
     if not fmad:
         cmd.insert(1, "-fmad=false")

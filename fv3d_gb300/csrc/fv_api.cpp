@@ -20,7 +20,7 @@
 #include "fv_kernels.h"
 
 using fv::Fields;
-using fv::Grid2D;
+using fv::Grid;
 using fv::StepCtrl;
 
 namespace {
@@ -34,9 +34,11 @@ enum KernelClass { KC_STAGE = 0, KC_DT = 1, KC_CONV = 2 };
 
 struct fv_sim {
   fv_params p{};
-  Grid2D G{};
+  Grid G{};
   bool wact = false;          // third momentum component carried
-  int deg_bc = FV_BC_PERIODIC;
+  int deg_bc = FV_BC_PERIODIC;  // boundary of the one-cell axis (2-D kernels)
+  int refl_deg = 0;             // bit a: axis a has one cell and reflects
+  double* d_kappa_z = nullptr;  // B02 face conductivities per z layer
   double* buf = nullptr;      // 3 states x 5 fields x fstride doubles
   Fields A{}, B{}, S{};       // A: state, B: U* / ping-pong, S: scratch
   int cur = 0;                // Euler ping-pong: state in A (0) or B (1)
@@ -80,16 +82,51 @@ int Fail(fv_sim* s, int code, const char* fmt, ...) {
       return Fail((s), FV_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
   } while (0)
 
-// Cell sizes and loop constants of ComputeDt.h:36-47 (constant kappa / mu).
+// computeKappa (ThermalConduction.h:8-21) of the B02 profile at height z.
+// Host arithmetic is compiled without contraction, so this rounds as the
+// reference's CPU build does.
+double KappaB02(const fv_params& p, double z) {
+  const double tr = (std::tanh((z - p.b02_zmid) / p.b02_thickness) + 1.0) * 0.5;
+  return p.kappa * (p.b02_kappa1 * (1.0 - tr) + p.b02_kappa2 * tr);
+}
+
+bool B02(const fv_params& p) { return p.thermal_conductivity_active && p.thermal_conductivity_mode == FV_TCM_B02; }
+
+// The constant TC / viscous terms of ComputeDt.h:36-47, maximised over the
+// domain.  The reference passes cell indices as coordinates to computeKappa
+// (ComputeDt.h:39), so with B02 the term depends on the padded index k only.
 void DtConstants(const fv_params& p, double* inv_tc, double* inv_visc) {
   *inv_tc = p.epsilon;
-  if (p.thermal_conductivity_active)
-    *inv_tc = std::fmax(std::fmax(2.0 * p.kappa / (p.dx * p.dx), 2.0 * p.kappa / (p.dy * p.dy)),
-                        2.0 * p.kappa / (p.dz * p.dz));
+  if (p.thermal_conductivity_active) {
+    auto term = [&](double kap) {
+      return std::fmax(std::fmax(2.0 * kap / (p.dx * p.dx), 2.0 * kap / (p.dy * p.dy)), 2.0 * kap / (p.dz * p.dz));
+    };
+    if (B02(p)) {
+      double m = -HUGE_VAL;
+      for (int k = p.Ng; k < p.Ng + p.Nz; ++k) m = std::fmax(m, term(KappaB02(p, (double)k)));
+      *inv_tc = m;
+    } else {
+      *inv_tc = term(p.kappa);
+    }
+  }
   *inv_visc = p.epsilon;
   if (p.viscosity_active)
     *inv_visc = std::fmax(std::fmax(2.0 * p.mu / (p.dx * p.dx), 2.0 * p.mu / (p.dy * p.dy)),
                           2.0 * p.mu / (p.dz * p.dz));
+}
+
+// Face conductivities per interior z layer for B02 (ThermalConduction.h:45-50
+// with getPos, SimInfo.h:163-167): in-plane faces, face below, face above.
+std::vector<double> KappaTable(const fv_params& p) {
+  std::vector<double> t(3 * (size_t)p.Nz);
+  for (int k = 0; k < p.Nz; ++k) {
+    const double z = p.zmin + ((double)k + 0.5) * p.dz;
+    const double kc = KappaB02(p, z);
+    t[3 * k] = 0.5 * (kc + kc);
+    t[3 * k + 1] = 0.5 * (kc + KappaB02(p, z - p.dz));
+    t[3 * k + 2] = 0.5 * (kc + KappaB02(p, z + p.dz));
+  }
+  return t;
 }
 
 int DevBC(int bc) { return bc == FV_BC_ABSORBING ? fv::DBC_ABSORBING : bc == FV_BC_REFLECTING ? fv::DBC_REFLECTING : fv::DBC_PERIODIC; }
@@ -102,7 +139,7 @@ bool PowerOfTwo(double d) {
 
 // Reciprocals and flags the kernels use to replace divisions by the cell
 // sizes and by gamma - 1 with operations that round identically.
-void SetExactConstants(Grid2D& G) {
+void SetExactConstants(Grid& G) {
   G.inv_dx = 1.0 / G.dx;
   G.inv_dy = 1.0 / G.dy;
   G.inv_dz = 1.0 / G.dz;
@@ -127,6 +164,10 @@ void SetExactConstants(Grid2D& G) {
 }
 
 // Checks that the parameter set is one this build runs and fills the grid.
+// 2-D runs without z-boundary physics use the plane kernels; everything else
+// (true 3-D grids, gravity in the x-y plane, the well-balanced / C91 z
+// boundaries, B02 conductivity, fixed-temperature / gradient conduction
+// boundaries) uses the 3-D kernel.
 int Configure(fv_sim* s) {
   const fv_params& p = s->p;
   if (p.Nx < 1 || p.Ny < 1 || p.Nz < 1) return Fail(s, FV_ERR_PARAM, "Nx, Ny, Nz must be >= 1");
@@ -135,35 +176,62 @@ int Configure(fv_sim* s) {
   if (!(p.gamma0 > 1.0)) return Fail(s, FV_ERR_PARAM, "gamma0 must be > 1");
   if (p.precision != FV_PREC_FP64)
     return Fail(s, FV_ERR_UNSUPPORTED, "fvgpu_create runs the FP64 form; the FP32-mixed form is batch-only");
-  Grid2D& G = s->G;
-  int plane;
-  if (p.Nz == 1 && p.Ny >= 2 && p.Nx >= 2) {
+  if (p.thermal_conductivity_active && p.thermal_conductivity_mode != FV_TCM_CONSTANT && !B02(p))
+    return Fail(s, FV_ERR_UNSUPPORTED, "unknown thermal conductivity mode");
+  const bool tc_z = p.thermal_conductivity_active && (B02(p) || p.bctc_zmin != FV_BCTC_NONE ||
+                                                      p.bctc_zmax != FV_BCTC_NONE);
+  const bool z_physics = p.well_balanced_flux_at_z_bc || p.boundary_z == FV_BC_C91 || tc_z;
+  Grid& G = s->G;
+  G = Grid{};
+  int plane = -1;
+  if (!z_physics && !p.gravity && p.Nz == 1 && p.Ny >= 2 && p.Nx >= 2) {
     plane = fv::PLANE_XY;
     s->deg_bc = p.boundary_z;
-  } else if (p.Ny == 1 && p.Nz >= 2 && p.Nx >= 2) {
+  } else if (!z_physics && p.Ny == 1 && p.Nz >= 2 && p.Nx >= 2) {
     plane = fv::PLANE_XZ;
     s->deg_bc = p.boundary_y;
-  } else {
-    return Fail(s, FV_ERR_UNSUPPORTED, "only 2-D runs (Nz == 1 or Ny == 1, other axes >= 2) are built");
   }
-  if (plane == fv::PLANE_XY && p.gravity)
-    return Fail(s, FV_ERR_UNSUPPORTED, "gravity acts along z only (Update.h:148); use the x-z plane (Ny = 1)");
-  if (p.well_balanced_flux_at_z_bc) return Fail(s, FV_ERR_UNSUPPORTED, "well_balanced_flux_at_z_bc is not built");
-  if (p.boundary_z == FV_BC_C91) return Fail(s, FV_ERR_UNSUPPORTED, "the C91 z boundary is not built");
-  if (p.thermal_conductivity_active && p.thermal_conductivity_mode != FV_TCM_CONSTANT)
-    return Fail(s, FV_ERR_UNSUPPORTED, "only constant thermal conductivity is built");
-  if (p.thermal_conductivity_active && (p.bctc_zmin != FV_BCTC_NONE || p.bctc_zmax != FV_BCTC_NONE))
-    return Fail(s, FV_ERR_UNSUPPORTED, "fixed-temperature/gradient z boundaries of conduction are not built");
-  if (p.viscosity_active && s->deg_bc == FV_BC_REFLECTING)
-    return Fail(s, FV_ERR_UNSUPPORTED, "viscosity with a reflecting degenerate axis is not built");
-
-  G.plane = plane;
-  G.na = p.Nx;
-  G.nb = plane == fv::PLANE_XY ? p.Ny : p.Nz;
+  // One-cell reflecting axes: the reference's outer ghost layer there is a
+  // stale copy of the previous stage, harmless only while the velocity along
+  // the axis is zero and no viscous stencil reads it.
+  const int n_ax[3] = {p.Nx, p.Ny, p.Nz};
+  const int bc_ax[3] = {p.boundary_x, p.boundary_y, p.boundary_z};
+  s->refl_deg = 0;
+  for (int a = 0; a < 3; ++a)
+    if (n_ax[a] == 1 && bc_ax[a] == FV_BC_REFLECTING) s->refl_deg |= 1 << a;
+  if (p.viscosity_active && s->refl_deg)
+    return Fail(s, FV_ERR_UNSUPPORTED, "viscosity with a reflecting one-cell axis is not built");
+  G.rows = 0;
+  if (plane >= 0) {
+    G.ndim = 2;
+    G.plane = plane;
+    G.na = p.Nx;
+    G.nb = plane == fv::PLANE_XY ? p.Ny : p.Nz;
+    G.nc = 1;
+    G.bc_a = DevBC(p.boundary_x);
+    G.bc_b = DevBC(plane == fv::PLANE_XY ? p.boundary_y : p.boundary_z);
+    G.bc_c = DevBC(s->deg_bc);
+    G.da = p.dx;
+    G.db = plane == fv::PLANE_XY ? p.dy : p.dz;
+    G.dc = plane == fv::PLANE_XY ? p.dz : p.dy;
+  } else {
+    if (p.boundary_z == FV_BC_C91 && p.Nz < 2)
+      return Fail(s, FV_ERR_UNSUPPORTED, "the C91 z boundary needs Nz >= 2 (its mirror cell)");
+    G.ndim = 3;
+    G.plane = fv::PLANE_XY;  // storage order rho, m_x, m_y, m_z, E
+    G.na = p.Nx;
+    G.nb = p.Ny;
+    G.nc = p.Nz;
+    G.bc_a = DevBC(p.boundary_x);
+    G.bc_b = DevBC(p.boundary_y);
+    G.bc_c = p.boundary_z == FV_BC_C91 ? fv::DBC_C91 : DevBC(p.boundary_z);
+    G.da = p.dx;
+    G.db = p.dy;
+    G.dc = p.dz;
+  }
+  G.rows = G.nb * G.nc;
   G.pitch = (G.na + 15) / 16 * 16;  // 128-byte rows
-  G.fstride = ((long long)G.pitch * G.nb + 31) / 32 * 32;
-  G.bc_a = DevBC(p.boundary_x);
-  G.bc_b = DevBC(plane == fv::PLANE_XY ? p.boundary_y : p.boundary_z);
+  G.fstride = ((long long)G.pitch * G.rows + 31) / 32 * 32;
   G.recon = p.reconstruction;
   G.gravity = p.gravity ? 1 : 0;
   G.tc = p.thermal_conductivity_active ? 1 : 0;
@@ -171,13 +239,19 @@ int Configure(fv_sim* s) {
   G.dx = p.dx;
   G.dy = p.dy;
   G.dz = p.dz;
-  G.da = p.dx;
-  G.db = plane == fv::PLANE_XY ? p.dy : p.dz;
-  G.dc = plane == fv::PLANE_XY ? p.dz : p.dy;
   G.gamma = p.gamma0;
   G.g = p.g;
   G.kappa = p.kappa;
   G.mu = p.mu;
+  G.wb_flux_z = p.well_balanced_flux_at_z_bc ? 1 : 0;
+  G.gravity_flag = p.gravity ? 1 : 0;
+  G.bctc_zmin = p.thermal_conductivity_active ? p.bctc_zmin : FV_BCTC_NONE;
+  G.bctc_zmax = p.thermal_conductivity_active ? p.bctc_zmax : FV_BCTC_NONE;
+  G.bctc_zmin_value = p.bctc_zmin_value;
+  G.bctc_zmax_value = p.bctc_zmax_value;
+  G.zmin = p.zmin;
+  G.theta1 = p.theta1;
+  G.kappa_z = nullptr;  // B02 table: set by fvgpu_create
   SetExactConstants(G);
   DtConstants(p, &s->inv_tc, &s->inv_visc);
   return FV_OK;
@@ -235,13 +309,13 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
   if (s->p.time_stepping == FV_TS_RK2) {
     {
       Timed t(s, KC_STAGE);
-      cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream);
+      cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream);
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 1 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
     {
       Timed t(s, KC_STAGE);
-      cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream);
+      cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream);
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 2 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
@@ -249,7 +323,7 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
     Timed t(s, KC_STAGE);
     const Fields& in = Current(s);
     const Fields& out = s->cur == 0 ? s->B : s->A;
-    cudaError_t e = fv::launch_stage2d(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream);
+    cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream);
     if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "euler stage launch: %s", cudaGetErrorString(e));
     if (counting) t.done();
     s->cur ^= 1;
@@ -295,7 +369,7 @@ int CopyIn(fv_sim* s, const Fields& dst, const double* const src[5], bool zero_m
   const size_t rowb = (size_t)s->G.na * sizeof(double);
   for (int v = 0; v < 5; ++v) {
     if (src[v]) {
-      CUDA_TRY(s, cudaMemcpy2DAsync(dst.f[v], (size_t)s->G.pitch * sizeof(double), src[v], rowb, rowb, s->G.nb,
+      CUDA_TRY(s, cudaMemcpy2DAsync(dst.f[v], (size_t)s->G.pitch * sizeof(double), src[v], rowb, rowb, s->G.rows,
                                     cudaMemcpyHostToDevice, s->stream));
     } else if (zero_missing) {
       CUDA_TRY(s, cudaMemsetAsync(dst.f[v], 0, (size_t)s->G.fstride * sizeof(double), s->stream));
@@ -308,7 +382,7 @@ int CopyOut(fv_sim* s, const Fields& src, double* const dst[5]) {
   const size_t rowb = (size_t)s->G.na * sizeof(double);
   for (int v = 0; v < 5; ++v) {
     if (!dst[v]) continue;
-    CUDA_TRY(s, cudaMemcpy2DAsync(dst[v], rowb, src.f[v], (size_t)s->G.pitch * sizeof(double), rowb, s->G.nb,
+    CUDA_TRY(s, cudaMemcpy2DAsync(dst[v], rowb, src.f[v], (size_t)s->G.pitch * sizeof(double), rowb, s->G.rows,
                                   cudaMemcpyDeviceToHost, s->stream));
   }
   CUDA_TRY(s, cudaStreamSynchronize(s->stream));
@@ -329,10 +403,17 @@ int SetState(fv_sim* s, const double* const ref_fields[5], bool prim) {
   const double* src[5];
   for (int v = 0; v < 5; ++v) src[slot_of[v]] = ref_fields[v];
   if (!src[0] || !src[4]) return Fail(s, FV_ERR_PARAM, "density and pressure/energy arrays are required");
-  const long long ncell = (long long)s->G.na * s->G.nb;
-  s->wact = s->p.viscosity_active || AnyNonzero(src[3], ncell);
-  if (s->wact && s->deg_bc == FV_BC_REFLECTING)
-    return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  const long long ncell = (long long)s->G.na * s->G.rows;
+  if (s->G.ndim == 3) {
+    s->wact = true;
+    for (int a = 0; a < 3; ++a)
+      if ((s->refl_deg >> a & 1) && AnyNonzero(src[1 + a], ncell))
+        return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting one-cell axis is not built");
+  } else {
+    s->wact = s->p.viscosity_active || AnyNonzero(src[3], ncell);
+    if (s->wact && s->deg_bc == FV_BC_REFLECTING)
+      return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  }
   ResetGraph(s);
   s->cur = 0;
   int rc = CopyIn(s, s->A, src, true);
@@ -355,7 +436,7 @@ namespace fv {
 
 // The parameter checks and grid set-up of fvgpu_create, without allocating:
 // fills G and the constant CFL terms, or returns a status with a message.
-int configure_grid(const fv_params& p, Grid2D* G, double* inv_tc, double* inv_visc, int* deg_bc,
+int configure_grid(const fv_params& p, Grid* G, double* inv_tc, double* inv_visc, int* deg_bc,
                    std::string* err) {
   fv_sim s;
   s.p = p;
@@ -392,6 +473,16 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
     return Fail(s, FV_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
   }
   cudaMemset(s->buf, 0, bytes);
+  if (B02(s->p)) {
+    const std::vector<double> table = KappaTable(s->p);
+    if (cudaMalloc(&s->d_kappa_z, table.size() * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(s->d_kappa_z, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+      *out = s;
+      return Fail(s, FV_ERR_NOMEM, "conductivity table allocation failed");
+    }
+    s->G.kappa_z = s->d_kappa_z;
+  }
   s->A = StateAt(s->buf, s->G.fstride);
   s->B = StateAt(s->buf + 5 * s->G.fstride, s->G.fstride);
   s->S = StateAt(s->buf + 10 * s->G.fstride, s->G.fstride);
@@ -424,6 +515,7 @@ int fvgpu_destroy(fv_sim* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   ResetGraph(s);
   if (s->buf) cudaFree(s->buf);
+  if (s->d_kappa_z) cudaFree(s->d_kappa_z);
   if (s->d_ctrl) cudaFree(s->d_ctrl);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
   if (s->d_partial) cudaFree(s->d_partial);
@@ -481,7 +573,7 @@ int fvgpu_get_cons(fv_sim* s, double* rho, double* mx, double* my, double* mz, d
   for (int k = 0; k < 5; ++k) dst[slot_of[k]] = ref[k];
   if (!s->wact) {
     // the third momentum is identically zero and not stored by the stages
-    if (dst[3]) std::memset(dst[3], 0, sizeof(double) * (size_t)s->G.na * s->G.nb);
+    if (dst[3]) std::memset(dst[3], 0, sizeof(double) * (size_t)s->G.na * s->G.rows);
     dst[3] = nullptr;
   }
   return CopyOut(s, Current(s), dst);

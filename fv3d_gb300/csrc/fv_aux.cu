@@ -17,10 +17,10 @@ int grid_for(long long n, int block) {
 
 // ComputeDt.h:28-54 over the interior: max inv_dt_hyp into ctrl->slot[slot].
 template <int PLANE, bool WACT>
-__global__ void __launch_bounds__(256) reduce2d_fp64(const Grid2D G, const Fields u, StepCtrl* ctrl, int slot) {
+__global__ void __launch_bounds__(256) reduce2d_fp64(const Grid G, const Fields u, StepCtrl* ctrl, int slot) {
   __shared__ unsigned long long s_red[8];
   unsigned long long red = 0ull;
-  const long long n = (long long)G.na * G.nb;
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -84,8 +84,8 @@ __global__ void batch_control_kernel(StepCtrl* ctrl, int n, unsigned* queue, int
 
 // primToCons in place (States.h:20-31).  Storage order in and out.
 template <int PLANE>
-__global__ void prim_to_cons2d(const Grid2D G, const Fields u) {
-  const long long n = (long long)G.na * G.nb;
+__global__ void prim_to_cons2d(const Grid G, const Fields u) {
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -104,8 +104,8 @@ __global__ void prim_to_cons2d(const Grid2D G, const Fields u) {
 
 // consToPrim (States.h:34-45); src and dst may alias.
 template <int PLANE>
-__global__ void cons_to_prim2d(const Grid2D G, const Fields src, const Fields dst) {
-  const long long n = (long long)G.na * G.nb;
+__global__ void cons_to_prim2d(const Grid G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -131,10 +131,10 @@ __device__ __forceinline__ void kadd(double& s, double& c, double x) {
   s = t;
 }
 
-__global__ void __launch_bounds__(256) totals2d(const Grid2D G, const Fields u, double* partial) {
+__global__ void __launch_bounds__(256) totals2d(const Grid G, const Fields u, double* partial) {
   __shared__ double s_sum[5][256], s_cmp[5][256];
   double s[5] = {0, 0, 0, 0, 0}, cc[5] = {0, 0, 0, 0, 0};
-  const long long n = (long long)G.na * G.nb;
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -161,8 +161,8 @@ __global__ void __launch_bounds__(256) totals2d(const Grid2D G, const Fields u, 
 
 }  // namespace
 
-cudaError_t launch_reduce2d(const Grid2D& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t st) {
-  const int grid = grid_for((long long)G.na * G.nb, 256);
+cudaError_t launch_reduce2d(const Grid& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.rows, 256);
   if (G.plane == PLANE_XY) {
     if (wact) reduce2d_fp64<PLANE_XY, true><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
     else reduce2d_fp64<PLANE_XY, false><<<grid, 256, 0, st>>>(G, u, ctrl, slot);
@@ -185,23 +185,23 @@ cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq,
   return cudaGetLastError();
 }
 
-cudaError_t launch_prim_to_cons2d(const Grid2D& G, Fields u, cudaStream_t st) {
-  const int grid = grid_for((long long)G.na * G.nb, 256);
+cudaError_t launch_prim_to_cons2d(const Grid& G, Fields u, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.rows, 256);
   if (G.plane == PLANE_XY) prim_to_cons2d<PLANE_XY><<<grid, 256, 0, st>>>(G, u);
   else prim_to_cons2d<PLANE_XZ><<<grid, 256, 0, st>>>(G, u);
   return cudaGetLastError();
 }
 
-cudaError_t launch_cons_to_prim2d(const Grid2D& G, Fields src, Fields dst, cudaStream_t st) {
-  const int grid = grid_for((long long)G.na * G.nb, 256);
+cudaError_t launch_cons_to_prim2d(const Grid& G, Fields src, Fields dst, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.rows, 256);
   if (G.plane == PLANE_XY) cons_to_prim2d<PLANE_XY><<<grid, 256, 0, st>>>(G, src, dst);
   else cons_to_prim2d<PLANE_XZ><<<grid, 256, 0, st>>>(G, src, dst);
   return cudaGetLastError();
 }
 
-cudaError_t launch_totals2d(const Grid2D& G, Fields u, double* partial, int max_blocks, int* nblocks,
+cudaError_t launch_totals2d(const Grid& G, Fields u, double* partial, int max_blocks, int* nblocks,
                             cudaStream_t st) {
-  int grid = grid_for((long long)G.na * G.nb, 256);
+  int grid = grid_for((long long)G.na * G.rows, 256);
   if (grid > max_blocks) grid = max_blocks;
   *nblocks = grid;
   totals2d<<<grid, 256, 0, st>>>(G, u, partial);

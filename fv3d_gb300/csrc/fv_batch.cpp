@@ -32,13 +32,13 @@
 #include "fv_kernels.h"
 
 namespace fv {
-int configure_grid(const fv_params& p, Grid2D* G, double* inv_tc, double* inv_visc, int* deg_bc,
+int configure_grid(const fv_params& p, Grid* G, double* inv_tc, double* inv_visc, int* deg_bc,
                    std::string* err);
 }
 
 using fv::BatchInst;
 using fv::Fields;
-using fv::Grid2D;
+using fv::Grid;
 using fv::StepCtrl;
 
 namespace {
@@ -63,7 +63,7 @@ struct fv_batch {
   int precision = FV_PREC_FP64;
   int ts = FV_TS_RK2;
   std::vector<fv_params> p;
-  std::vector<Grid2D> G;
+  std::vector<Grid> G;
   std::vector<int> deg_bc;
   std::vector<double> inv_tc, inv_visc;
   std::vector<char> wact, state_set, slot_valid;
@@ -437,6 +437,9 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
     std::string err;
     int rc = fv::configure_grid(q, &b->G[i], &b->inv_tc[i], &b->inv_visc[i], &b->deg_bc[i], &err);
     if (rc) return Fail(b, rc, "problem %d: %s", i, err.c_str());
+    if (b->G[i].ndim != 2)
+      return Fail(b, FV_ERR_UNSUPPORTED,
+                  "problem %d: batches run 2-D problems without z-boundary physics; use fvgpu_create", i);
     b->wact[i] = params[i].viscosity_active ? 1 : 0;
     off[i] = total;
     total += (size_t)10 * b->G[i].fstride;
@@ -494,7 +497,7 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
                          const double* w, const double* pr) {
   if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
   if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);
-  const Grid2D& G = b->G[inst];
+  const Grid& G = b->G[inst];
   int slot_of[5];
   StorageOrder(G.plane, slot_of);
   const double* ref[5] = {rho, u, v, w, pr};
@@ -538,7 +541,7 @@ int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* 
   if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
   if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);
   if (!b->state_set[inst]) return Fail(b, FV_ERR_STATE, "problem %d has no state", inst);
-  const Grid2D& G = b->G[inst];
+  const Grid& G = b->G[inst];
   int slot_of[5];
   StorageOrder(G.plane, slot_of);
   double* ref[5] = {rho, u, v, w, pr};

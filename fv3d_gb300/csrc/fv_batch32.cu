@@ -120,11 +120,11 @@ int grid_for(long long n, int block) {
 
 // CFL maximum of a state held as (hi, lo) pairs.
 template <int PLANE, bool WACT>
-__global__ void __launch_bounds__(256) reduce2d_mixed(const Grid2D G, const Fields pairs, StepCtrl* ctrl, int slot) {
+__global__ void __launch_bounds__(256) reduce2d_mixed(const Grid G, const Fields pairs, StepCtrl* ctrl, int slot) {
   __shared__ unsigned long long s_red[8];
   float red = 0.0f;
   bool bad = false;
-  const long long n = (long long)G.na * G.nb;
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -148,8 +148,8 @@ __global__ void __launch_bounds__(256) reduce2d_mixed(const Grid2D G, const Fiel
 }
 
 // FP64 values -> (hi, lo) float pairs: hi = RN32(d), lo = RN32(d - hi).
-__global__ void pairs_from_double(const Grid2D G, const Fields src, const Fields dst) {
-  const long long n = (long long)G.na * G.nb;
+__global__ void pairs_from_double(const Grid G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -164,8 +164,8 @@ __global__ void pairs_from_double(const Grid2D G, const Fields src, const Fields
 }
 
 // (hi, lo) pairs -> FP64 values hi + lo (exact).
-__global__ void double_from_pairs(const Grid2D G, const Fields src, const Fields dst) {
-  const long long n = (long long)G.na * G.nb;
+__global__ void double_from_pairs(const Grid G, const Fields src, const Fields dst) {
+  const long long n = (long long)G.na * G.rows;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
@@ -203,9 +203,9 @@ cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchIns
   return cudaGetLastError();
 }
 
-cudaError_t launch_reduce2d_mixed(const Grid2D& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
+cudaError_t launch_reduce2d_mixed(const Grid& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
                                   cudaStream_t st) {
-  const int grid = grid_for((long long)G.na * G.nb, 256);
+  const int grid = grid_for((long long)G.na * G.rows, 256);
   if (G.plane == PLANE_XY) {
     if (wact) reduce2d_mixed<PLANE_XY, true><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
     else reduce2d_mixed<PLANE_XY, false><<<grid, 256, 0, st>>>(G, pairs, ctrl, slot);
@@ -216,13 +216,13 @@ cudaError_t launch_reduce2d_mixed(const Grid2D& G, bool wact, Fields pairs, Step
   return cudaGetLastError();
 }
 
-cudaError_t launch_pairs_from_double(const Grid2D& G, Fields src, Fields dst_pairs, cudaStream_t st) {
-  pairs_from_double<<<grid_for((long long)G.na * G.nb, 256), 256, 0, st>>>(G, src, dst_pairs);
+cudaError_t launch_pairs_from_double(const Grid& G, Fields src, Fields dst_pairs, cudaStream_t st) {
+  pairs_from_double<<<grid_for((long long)G.na * G.rows, 256), 256, 0, st>>>(G, src, dst_pairs);
   return cudaGetLastError();
 }
 
-cudaError_t launch_double_from_pairs(const Grid2D& G, Fields src_pairs, Fields dst, cudaStream_t st) {
-  double_from_pairs<<<grid_for((long long)G.na * G.nb, 256), 256, 0, st>>>(G, src_pairs, dst);
+cudaError_t launch_double_from_pairs(const Grid& G, Fields src_pairs, Fields dst, cudaStream_t st) {
+  double_from_pairs<<<grid_for((long long)G.na * G.rows, 256), 256, 0, st>>>(G, src_pairs, dst);
   return cudaGetLastError();
 }
 

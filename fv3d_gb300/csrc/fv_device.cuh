@@ -12,8 +12,8 @@ namespace fv {
 
 // Boundary kinds as seen by the kernels (BC_C91 on x/y behaves as periodic in
 // the reference's default branch, BoundaryConditions.h:165,186; the host maps
-// it before launch).
-enum DevBC : int { DBC_ABSORBING = 0, DBC_REFLECTING = 1, DBC_PERIODIC = 2 };
+// it before launch).  DBC_C91 only occurs along z of the 3-D kernel.
+enum DevBC : int { DBC_ABSORBING = 0, DBC_REFLECTING = 1, DBC_PERIODIC = 2, DBC_C91 = 3 };
 enum Recon : int { R_PCM = 0, R_PCM_WB = 1, R_PLM = 2 };
 enum StageKind : int { STAGE_EULER = 0, STAGE_RK_1 = 1, STAGE_RK_2 = 2 };
 // The two active axes of a 2-D run: a = x always; b = y (XY plane, Nz == 1)
@@ -36,13 +36,21 @@ struct StepCtrl {
   int err;             // sticky: bit0 non-finite/negative state seen
 };
 
-// Geometry and physics of one 2-D problem as the kernels need it.
-struct Grid2D {
+// Geometry and physics of one problem as the kernels need it.  A 2-D run
+// (ndim 2) has axes a, b and a one-cell axis c; a 3-D run (ndim 3) has
+// a = x, b = y, c = z, stored like the x-y plane (rho, m_x, m_y, m_z, E).
+// Field arrays hold `rows` = nb * nc rows of `pitch` elements, row index
+// k * nb + j.
+struct Grid {
   int na, nb;          // interior cells along a and b
+  int nc;              // interior cells along c (1 in 2-D)
+  int rows;            // nb * nc
+  int ndim;            // 2 or 3
   int pitch;           // row pitch in elements
-  int plane;           // Plane
-  long long fstride;   // elements per field array (pitch * nb)
+  int plane;           // Plane (PLANE_XY for 3-D)
+  long long fstride;   // elements per field array (>= pitch * rows)
   int bc_a, bc_b;      // DevBC along a / b
+  int bc_c;            // DevBC along c (3-D kernel)
   int recon;           // Recon
   int gravity, tc, visc;
   double da, db, dc;   // cell size along a, b and the degenerate axis
@@ -56,6 +64,17 @@ struct Grid2D {
   // slow FP64 pipe, so kernels never convert per cell).
   float gamma_f, gm1_f, inv_gm1_f, g_f, kappa_f, mu_f, g_dz_f;
   float dx_f, dy_f, dz_f, inv_dx_f, inv_dy_f, inv_dz_f;
+  // z-boundary physics of the 3-D kernel (Update.h:131-143,
+  // BoundaryConditions.h:87-134, ThermalConduction.h:78-92):
+  int wb_flux_z;                   // well_balanced_flux_at_z_bc
+  int gravity_flag;                // params.gravity as the C91 ghost uses it (0/1)
+  int bctc_zmin, bctc_zmax;        // fv_bctc_mode
+  double bctc_zmin_value, bctc_zmax_value;
+  double zmin, theta1;             // C91 ghost temperature profile
+  // Face conductivities per interior z layer when kappa varies with z
+  // (B02): kappa_z[3k + {0,1,2}] = in-plane faces, face k-1/2, face k+1/2.
+  // Null for constant kappa.
+  const double* kappa_z;
 };
 
 // Maps a cell index g (may be a ghost, -2 <= g < n+2) along an axis with n

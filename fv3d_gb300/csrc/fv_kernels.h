@@ -25,11 +25,24 @@ constexpr int kTileY = 16;
 // dt and the active flag come from ctrl (set by launch_control); STAGE_EULER
 // and STAGE_RK_2 also reduce max inv_dt_hyp of their output into
 // ctrl->slot[parity ^ 1].
-cudaError_t launch_stage2d(const Grid2D& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
+cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                            Fields uout, StepCtrl* ctrl, cudaStream_t stream);
 
+// The same stage over a 3-D grid (G.ndim == 3): one CTA per 16 x 16 block of
+// columns and stage3d_layers_per_cta(G) z layers; always carries w.
+cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
+                           StepCtrl* ctrl, cudaStream_t stream);
+int stage3d_layers_per_cta(const Grid& G);
+
+// The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
+inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
+                                Fields uout, StepCtrl* ctrl, cudaStream_t stream) {
+  if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream);
+  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream);
+}
+
 // Reduce max inv_dt_hyp of state u into ctrl->slot[slot] (caller zeroes it).
-cudaError_t launch_reduce2d(const Grid2D& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t stream);
+cudaError_t launch_reduce2d(const Grid& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t stream);
 
 // Per-step control for n problems: choose dt (CFL from the reduced max, or
 // dt_given when mode_override == 0), set active and parity, advance t and the
@@ -40,13 +53,13 @@ cudaError_t launch_control(StepCtrl* ctrl, int n, int mode_override, double dt_g
 // In-place conversions on a state whose arrays hold primitive / conserved
 // values in storage order (primToCons / consToPrim, States.h:20-45, with the
 // reference's rounding: no contraction).
-cudaError_t launch_prim_to_cons2d(const Grid2D& G, Fields u, cudaStream_t stream);
-cudaError_t launch_cons_to_prim2d(const Grid2D& G, Fields src, Fields dst, cudaStream_t stream);
+cudaError_t launch_prim_to_cons2d(const Grid& G, Fields u, cudaStream_t stream);
+cudaError_t launch_cons_to_prim2d(const Grid& G, Fields src, Fields dst, cudaStream_t stream);
 
 // Compensated per-block partial sums of the five conserved fields:
 // partial[(blk*5 + v)*2 + {0,1}] = (sum, compensation).  Returns the block
 // count through nblocks.
-cudaError_t launch_totals2d(const Grid2D& G, Fields u, double* partial, int max_blocks, int* nblocks,
+cudaError_t launch_totals2d(const Grid& G, Fields u, double* partial, int max_blocks, int* nblocks,
                             cudaStream_t stream);
 
 // ---- batches of independent problems ----------------------------------
@@ -57,7 +70,7 @@ enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
 // B = U* (Euler: ping-pong).  FP32-mixed: A = U^n as float2 (hi, lo) pairs,
 // B = U* as float (RK2) or the second pair buffer (Euler).
 struct BatchInst {
-  Grid2D G;
+  Grid G;
   Fields A, B;
   StepCtrl* ctrl;
   int tiles_x;  // tiles along a
@@ -91,9 +104,9 @@ cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq,
                                  cudaStream_t stream);
 
 // FP32-mixed helpers: CFL max of (hi, lo) pairs; pairs <-> FP64 values.
-cudaError_t launch_reduce2d_mixed(const Grid2D& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
+cudaError_t launch_reduce2d_mixed(const Grid& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,
                                   cudaStream_t stream);
-cudaError_t launch_pairs_from_double(const Grid2D& G, Fields src, Fields dst_pairs, cudaStream_t stream);
-cudaError_t launch_double_from_pairs(const Grid2D& G, Fields src_pairs, Fields dst, cudaStream_t stream);
+cudaError_t launch_pairs_from_double(const Grid& G, Fields src, Fields dst_pairs, cudaStream_t stream);
+cudaError_t launch_double_from_pairs(const Grid& G, Fields src_pairs, Fields dst, cudaStream_t stream);
 
 }  // namespace fv

@@ -38,7 +38,7 @@
 #include "fv_kernels.h"
 
 namespace fv {
-int configure_grid(const fv_params& p, Grid2D* G, double* inv_tc, double* inv_visc, int* deg_bc,
+int configure_grid(const fv_params& p, Grid* G, double* inv_tc, double* inv_visc, int* deg_bc,
                    std::string* err);
 }
 
@@ -100,11 +100,11 @@ cudaError_t ScratchAddress(void** out) {
 extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[5], long pitch, double dt,
                                   double* next_dt, void* stream, char* errbuf, size_t errlen) {
   using fv::Fields;
-  using fv::Grid2D;
+  using fv::Grid;
   using fv::StepCtrl;
   if (errbuf && errlen) errbuf[0] = '\0';
   if (!params || !fields) return Message(errbuf, errlen, FV_ERR_PARAM, "null params or fields");
-  Grid2D G;
+  Grid G;
   double inv_tc = 0.0, inv_visc = 0.0;
   int deg_bc = 0;
   std::string err;
@@ -119,20 +119,32 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
   if (!A.f[0] || !A.f[1] || !A.f[2] || !A.f[4])
     return Message(errbuf, errlen, FV_ERR_PARAM, "density, energy and in-plane momenta are required");
   const bool wact = A.f[3] != nullptr;
-  if (!wact && params->viscosity_active)
-    return Message(errbuf, errlen, FV_ERR_PARAM, "viscosity drives the third momentum: pass its array");
-  if (wact && deg_bc == FV_BC_REFLECTING)
+  if (!wact && (params->viscosity_active || G.ndim == 3))
+    return Message(errbuf, errlen, FV_ERR_PARAM,
+                   G.ndim == 3 ? "a 3-D step needs all five fields"
+                               : "viscosity drives the third momentum: pass its array");
+  if (G.ndim == 2 && wact && deg_bc == FV_BC_REFLECTING)
     return Message(errbuf, errlen, FV_ERR_UNSUPPORTED,
                    "a third momentum with a reflecting degenerate axis is not built");
+  if (G.ndim == 3) {
+    // device arrays cannot be checked for a zero velocity along such an axis
+    const int n_ax[3] = {params->Nx, params->Ny, params->Nz};
+    const int bc_ax[3] = {params->boundary_x, params->boundary_y, params->boundary_z};
+    for (int a = 0; a < 3; ++a)
+      if (n_ax[a] == 1 && bc_ax[a] == FV_BC_REFLECTING)
+        return Message(errbuf, errlen, FV_ERR_UNSUPPORTED, "a reflecting one-cell axis needs fvgpu_create");
+    if (params->thermal_conductivity_active && params->thermal_conductivity_mode == FV_TCM_B02)
+      return Message(errbuf, errlen, FV_ERR_UNSUPPORTED, "B02 conductivity needs fvgpu_create (a device table)");
+  }
 
   G.pitch = (int)pitch;
-  G.fstride = (long long)pitch * G.nb;
+  G.fstride = (long long)pitch * G.rows;
   const size_t need = kCtrlBytes + (size_t)5 * (size_t)G.fstride * sizeof(double);
   if (need > kScratchBytes)
     return Message(errbuf, errlen, FV_ERR_PARAM,
                    "problem needs %zu bytes of step scratch, more than the fixed %zu (5 fields x pitch %ld x %d "
                    "rows x 8 B + %zu); use fvgpu_create for larger problems",
-                   need, kScratchBytes, pitch, G.nb, kCtrlBytes);
+                   need, kScratchBytes, pitch, G.rows, kCtrlBytes);
 
   void* base = nullptr;
   cudaError_t e = ScratchAddress(&base);
@@ -150,14 +162,14 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
   if (e == cudaSuccess) e = fv::launch_control(ctrl, 1, 0, dt, st);
   const int rs = params->riemann_solver == FV_HLL ? 0 : 1;
   if (params->time_stepping == FV_TS_RK2) {
-    if (e == cudaSuccess) e = fv::launch_stage2d(G, rs, fv::STAGE_RK_1, wact, A, A, B, ctrl, st);
-    if (e == cudaSuccess) e = fv::launch_stage2d(G, rs, fv::STAGE_RK_2, wact, B, A, A, ctrl, st);
+    if (e == cudaSuccess) e = fv::launch_stage(G, rs, fv::STAGE_RK_1, wact, A, A, B, ctrl, st);
+    if (e == cudaSuccess) e = fv::launch_stage(G, rs, fv::STAGE_RK_2, wact, B, A, A, ctrl, st);
   } else {
-    if (e == cudaSuccess) e = fv::launch_stage2d(G, rs, fv::STAGE_EULER, wact, A, A, B, ctrl, st);
+    if (e == cudaSuccess) e = fv::launch_stage(G, rs, fv::STAGE_EULER, wact, A, A, B, ctrl, st);
     for (int v = 0; v < 5 && e == cudaSuccess; ++v) {
       if (v == 3 && !wact) continue;
       e = cudaMemcpy2DAsync(A.f[v], (size_t)pitch * sizeof(double), B.f[v], (size_t)pitch * sizeof(double),
-                            (size_t)G.na * sizeof(double), G.nb, cudaMemcpyDeviceToDevice, st);
+                            (size_t)G.na * sizeof(double), G.rows, cudaMemcpyDeviceToDevice, st);
     }
   }
   if (e != cudaSuccess) return Message(errbuf, errlen, FV_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));

@@ -50,7 +50,7 @@ __device__ __forceinline__ void cons_to_prim64(const double u[5], double gm1, do
 // Hyperbolic inverse time step of one cell, ComputeDt.h:49-52:
 // (cs + |u|)/dx + (cs + |v|)/dy + (cs + |w|)/dz with cs = sqrt(p*gamma/rho).
 template <int PLANE, bool WACT>
-__device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid2D& G) {
+__device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid& G) {
   double q[5], y;
   cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
   const double cs = sqrt(div_by_rcp(__dmul_rn(q[4], G.gamma), q[0], y));

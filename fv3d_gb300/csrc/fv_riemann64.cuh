@@ -49,9 +49,11 @@ __device__ __forceinline__ void prim_to_cons64(const Slots<double>& q, double e,
 }
 
 // HLL with Davis wave speeds, RiemannSolvers.h:6-36.
+// pout, when given, receives the interface pressure of RiemannSolvers.h:24-33
+// (used only by the z-boundary flux overrides of Update.h:131-143).
 template <int ZS>
 __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double>& R, const Consts64& K,
-                                      double flux[5]) {
+                                      double flux[5], double* pout = nullptr) {
   const double aL = sqrt(L.p * K.gamma / L.r);
   const double aR = sqrt(R.p * K.gamma / R.r);
   const double SL = fmin(L.un - aL, R.un - aR);
@@ -64,10 +66,13 @@ __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double
   if (SL >= 0.0) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) flux[v] = FL[v];
+    if (pout) *pout = L.p;
   } else if (SR <= 0.0) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) flux[v] = FR[v];
+    if (pout) *pout = R.p;
   } else {
+    if (pout) *pout = 0.5 * (L.p + R.p);
     double uL[5], uR[5];
     prim_to_cons64<ZS>(L, eL, uL);
     prim_to_cons64<ZS>(R, eR, uR);
@@ -87,9 +92,10 @@ __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double
 
 // HLLC, RiemannSolvers.h:39-112; the kinetic energy uses un and t1 only, as
 // the reference does.
+// pout as for hll64 (RiemannSolvers.h:81-104: pL, p*, p*, pR by region).
 template <int ZS>
 __device__ __forceinline__ void hllc64(const Slots<double>& L, const Slots<double>& R, const Consts64& K,
-                                       double flux[5]) {
+                                       double flux[5], double* pout = nullptr) {
   const double rL = L.r, uL = L.un, pL = L.p;
   const double rR = R.r, uR = R.un, pR = R.p;
   const double kL = ZS == 1 ? uL * uL : uL * uL + L.t1 * L.t1;
@@ -127,6 +133,7 @@ __device__ __forceinline__ void hllc64(const Slots<double>& L, const Slots<doubl
   } else {
     sr = rR; su = uR; st1 = R.t1; st2 = R.t2; sp = pR; E = ER;
   }
+  if (pout) *pout = sp;
   flux[0] = sr * su;
   flux[1] = flux[0] * su + sp;
   flux[2] = ZS == 1 ? 0.0 : flux[0] * st1;

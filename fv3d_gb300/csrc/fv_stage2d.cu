@@ -11,14 +11,14 @@ using SingleTile = Tile<kTileX, kTileY>;
 
 template <int PLANE, int RS, int KIND, bool WACT>
 __global__ void __launch_bounds__(kTileThreads, WACT ? 2 : 3)
-stage2d_fp64(const Grid2D G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl) {
+stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
   stage_tile64<PLANE, WACT, SingleTile>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw, s_red);
 }
 
 template <int PLANE, int RS, int KIND, bool WACT>
-cudaError_t launch_one(const Grid2D& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, cudaStream_t st) {
+cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, cudaStream_t st) {
   using SM = TileSmem<double, WACT ? 5 : 4, SingleTile>;
   auto kern = stage2d_fp64<PLANE, RS, KIND, WACT>;
   static bool attr_set = false;  // per instantiation, once per process
@@ -33,7 +33,7 @@ cudaError_t launch_one(const Grid2D& G, Fields uin, Fields u0, Fields uout, Step
 }
 
 template <int PLANE, int RS, bool WACT>
-cudaError_t launch_kind(const Grid2D& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
+cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
                         cudaStream_t st) {
   switch (kind) {
     case STAGE_EULER: return launch_one<PLANE, RS, STAGE_EULER, WACT>(G, uin, u0, uout, ctrl, st);
@@ -43,7 +43,7 @@ cudaError_t launch_kind(const Grid2D& G, int kind, Fields uin, Fields u0, Fields
 }
 
 template <int PLANE, int RS>
-cudaError_t launch_w(const Grid2D& G, int kind, bool wact, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
+cudaError_t launch_w(const Grid& G, int kind, bool wact, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
                      cudaStream_t st) {
   return wact ? launch_kind<PLANE, RS, true>(G, kind, uin, u0, uout, ctrl, st)
               : launch_kind<PLANE, RS, false>(G, kind, uin, u0, uout, ctrl, st);
@@ -51,7 +51,7 @@ cudaError_t launch_w(const Grid2D& G, int kind, bool wact, Fields uin, Fields u0
 
 }  // namespace
 
-cudaError_t launch_stage2d(const Grid2D& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
+cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                            Fields uout, StepCtrl* ctrl, cudaStream_t st) {
   if (G.plane == PLANE_XY)
     return riemann_solver == 0 ? launch_w<PLANE_XY, 0>(G, kind, wact, uin, u0, uout, ctrl, st)

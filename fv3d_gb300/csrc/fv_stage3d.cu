@@ -1,0 +1,543 @@
+// fv_stage3d.cu -- the FP64 fused stage kernel of a 3-D problem.
+//
+// One CTA owns a 16 x 16 block of (x, y) columns and marches up a chunk of
+// z layers.  A ring of four z layers of primitives (each with a 2-cell
+// in-plane halo) sits in shared memory; layer k+2 is loaded while the x and y
+// faces of layer k are solved, then every thread solves the z face above its
+// own column and updates its cell.  The z flux below the cell is the one the
+// same thread solved one layer earlier (kept in registers), so every face of
+// the grid is solved exactly once.  Per layer:
+//   1. load layer k+2 (ghost layers synthesised from the boundary
+//      conditions, C91 ghosts computed by BoundaryConditions.h:87-134) and
+//      convert to primitives (consToPrim, States.h:34-45); solve the x and y
+//      faces of layer k (minmod slopes, PLM/PCM/PCM_WB states, HLL/HLLC);
+//   2. per column: the z face k+1/2, then the update of Update.h:90-162 in
+//      the reference's X, Y, Z order with gravity, the well-balanced / C91
+//      z-boundary flux overrides and the density floor, thermal conduction
+//      (ThermalConduction.h:38-96, with the fixed-temperature / fixed-gradient
+//      z boundaries and z-dependent B02 conductivity), viscosity
+//      (Viscosity.h:22-155, literal formula), the RK2 average and the CFL
+//      term of ComputeDt.h:28-54 for the last stage of a step.
+// Ghost cells follow the reference's fill order (x, then y over the full x
+// range, then z over the full x-y range), which for index-mapped boundaries
+// is the composition of the three per-axis maps.
+//
+// Compiled without FMA contraction, operation order as in the reference, the
+// exact replacements of fv_exact64.cuh: bit-identical to the reference's FP64
+// CPU arithmetic.
+#include "fv_tile64.cuh"
+
+namespace fv {
+
+namespace {
+
+constexpr int kTX = 16, kTY = 16;                // columns per CTA
+constexpr int kThreads = kTX * kTY;              // one thread per column
+constexpr int kHX = kTX + 4, kHY = kTY + 4;      // layer with halo
+constexpr int kLayer = kHX * kHY;
+constexpr int kRing = 4;                         // z layers held
+constexpr int kNFA = (kTX + 1) * kTY;            // x faces per layer
+constexpr int kNFA_PAD = (kNFA + 31) / 32 * 32;  // keeps each warp on one face kind
+constexpr int kNFB = kTX * (kTY + 1);            // y faces per layer
+static_assert(kThreads == 256, "one thread per column");
+
+// Shared memory: Q[ring][v][hy][hx] primitives, FA[v][fy][fx] x-face and
+// FB[v][fy][fx] y-face fluxes of the current layer, TT[ring][hy][hx]
+// temperature p/rho (conduction only).
+struct Smem3 {
+  double* base;
+  static constexpr int kFA = kRing * 5 * kLayer;
+  static constexpr int kFB = kFA + 5 * kTY * (kTX + 1);
+  static constexpr int kT = kFB + 5 * (kTY + 1) * kTX;
+  static constexpr size_t bytes(bool tc) { return sizeof(double) * (size_t)(kT + (tc ? kRing * kLayer : 0)); }
+  __device__ double& q(int s, int v, int hy, int hx) const { return base[((s * 5 + v) * kHY + hy) * kHX + hx]; }
+  __device__ double& fa(int v, int fy, int fx) const { return base[kFA + (v * kTY + fy) * (kTX + 1) + fx]; }
+  __device__ double& fb(int v, int fy, int fx) const { return base[kFB + (v * (kTY + 1) + fy) * kTX + fx]; }
+  __device__ double& temp(int s, int hy, int hx) const { return base[kT + (s * kHY + hy) * kHX + hx]; }
+};
+
+// Ring slot of z layer kg (kg >= -2).
+__device__ __forceinline__ int slot_of(int kg) { return (kg + 4) & 3; }
+
+// consToPrim of one stored cell (x, y, z storage order), RN(1/rho) in y.
+__device__ __forceinline__ void load_prim(const Fields& u, long long o, double gm1, double q[5], double& y) {
+  double w[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) w[v] = u.f[v][o];
+  cons_to_prim64<PLANE_XY, true>(w, gm1, q, y);
+}
+
+// fillC91 (BoundaryConditions.h:87-134) for ghost layer kg of column (sa, sb)
+// (already mapped through the x / y boundaries, with their velocity flips).
+// Note the reference scales the hydrostatic term by params.gravity, the
+// boolean, not by g.
+__device__ __forceinline__ void c91_ghost(const Grid& G, const Fields& u, long long col, bool fa, bool fb, int kg,
+                                          double res[5]) {
+  const int kref = kg < 0 ? 0 : G.nc - 1;
+  const int ksym = kg < 0 ? -kg - 1 : 2 * G.nc - kg - 1;
+  double qref[5], qsym[5], y;
+  load_prim(u, (long long)kref * G.nb * G.pitch + col, G.gm1, qref, y);
+  load_prim(u, (long long)ksym * G.nb * G.pitch + col, G.gm1, qsym, y);
+  if (fa) {
+    qref[1] = -qref[1];
+    qsym[1] = -qsym[1];
+  }
+  if (fb) {
+    qref[2] = -qref[2];
+    qsym[2] = -qsym[2];
+  }
+  const double grav = G.gravity_flag ? 1.0 : 0.0;
+  const double posz = G.zmin + ((double)kg + 0.5) * G.dz;
+  if (kg < 0) {
+    const double dz = posz - 0.5 * G.dz;
+    const double T = 1.0 + posz * G.theta1;
+    double p = qref[4] + dz * qref[0] * grav;
+    double r = p / T;
+    p = fmax(p, 1.0e-6);
+    r = fmax(r, 1.0e-6);
+    const double dratio = qsym[0] / r;
+    res[0] = r;
+    res[1] = qsym[1];
+    res[2] = qsym[2];
+    res[3] = -qsym[3] * dratio;
+    res[4] = p;
+  } else {
+    const double Tref = qref[4] / qref[0];
+    const double dz = posz - (1.0 - 0.5 * G.dz);
+    const double T = Tref + dz * G.theta1;
+    const double P = qref[4] + dz * qref[0] * grav;
+    const double rho = P / T;
+    res[4] = fmax(P, 1.0e-6);
+    res[0] = fmax(rho, 1.0e-6);
+    const double dratio = qsym[0] / rho;
+    res[1] = qsym[1] * dratio;
+    res[2] = qsym[2] * dratio;
+    res[3] = -qsym[3] * dratio;
+  }
+}
+
+// Loads z layer kg of the tile at (x0, y0) into ring slot slot_of(kg).
+__device__ __forceinline__ void load_layer(const Grid& G, const Fields& u, int x0, int y0, int kg, const Smem3& S,
+                                           int tid) {
+  const int s = slot_of(kg);
+  const bool c91 = G.bc_c == DBC_C91 && (kg < 0 || kg >= G.nc);
+  bool fz = false;
+  const int sz = c91 ? 0 : bc_source(kg, G.nc, G.bc_c, fz);
+  const long long zoff = (long long)sz * G.nb * G.pitch;
+  for (int idx = tid; idx < kLayer; idx += kThreads) {
+    const int hy = idx / kHX, hx = idx - hy * kHX;
+    bool fa, fb;
+    const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
+    const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
+    const long long col = (long long)sb * G.pitch + sa;
+    double q[5];
+    double T = 0.0;
+    if (!c91) {
+      double y;
+      load_prim(u, zoff + col, G.gm1, q, y);
+      if (fa) q[1] = -q[1];
+      if (fb) q[2] = -q[2];
+      if (fz) q[3] = -q[3];
+      if (G.tc) T = div_by_rcp(q[4], q[0], y);
+    } else {
+      c91_ghost(G, u, col, fa, fb, kg, q);
+      if (G.tc) T = q[4] / q[0];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) S.q(s, v, hy, hx) = q[v];
+    if (G.tc) S.temp(s, hy, hx) = T;
+  }
+}
+
+// Slots of a sweep from (r, u, v, w, p): IX (u, v, w), IY (v, u, w),
+// IZ (w, v, u) -- swap_component, States.h:104-111.
+template <int DIR>
+__device__ __forceinline__ Slots<double> slots3(const double q[5]) {
+  Slots<double> s;
+  s.r = q[0];
+  s.p = q[4];
+  s.un = DIR == 0 ? q[1] : (DIR == 1 ? q[2] : q[3]);
+  s.t1 = DIR == 1 ? q[1] : q[2];
+  s.t2 = DIR == 2 ? q[1] : q[3];
+  return s;
+}
+
+template <int DIR>
+__device__ __forceinline__ void unslot3(const double f[5], double out[5]) {
+  out[0] = f[0];
+  out[4] = f[4];
+  if (DIR == 0) {
+    out[1] = f[1]; out[2] = f[2]; out[3] = f[3];
+  } else if (DIR == 1) {
+    out[2] = f[1]; out[1] = f[2]; out[3] = f[3];
+  } else {
+    out[3] = f[1]; out[2] = f[2]; out[1] = f[3];
+  }
+}
+
+// One face along DIR from the four cells around it (c[0..3]: left-left,
+// left, right, right-right), in storage order; pout as in hll64 / hllc64.
+// The z slopes take minmod(forward, backward) (Update.h:84), x and y
+// minmod(backward, forward); the two orders differ only in the sign of a
+// zero slope.
+template <int DIR>
+__device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, const Grid& G, const Consts64& K,
+                                      double out[5], double* pout) {
+  double qL[5], qR[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    if (recon == R_PLM) {
+      const double d01 = c[1][v] - c[0][v], d12 = c[2][v] - c[1][v], d23 = c[3][v] - c[2][v];
+      const double sL = DIR == 2 ? minmod_exact(d12, d01) : minmod_exact(d01, d12);
+      const double sR = DIR == 2 ? minmod_exact(d23, d12) : minmod_exact(d12, d23);
+      qL[v] = recon_plus(c[1][v], sL);
+      qR[v] = recon_minus(c[2][v], sR);
+    } else {
+      qL[v] = c[1][v];
+      qR[v] = c[2][v];
+    }
+  }
+  if (DIR == 2 && recon == R_PCM_WB) {  // Update.h:27
+    qL[4] = qL[4] + 1.0 * qL[0] * G.g * G.dz * 0.5;
+    qR[4] = qR[4] + -1.0 * qR[0] * G.g * G.dz * 0.5;
+  }
+  const Slots<double> L = slots3<DIR>(qL), R = slots3<DIR>(qR);
+  double f[5];
+  if (rs == 0)
+    hll64<0>(L, R, K, f, pout);
+  else
+    hllc64<0>(L, R, K, f, pout);
+  unslot3<DIR>(f, out);
+}
+
+// Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
+// including its z-branch index and field mix-ups.  P(dk, dj, di, var) reads
+// velocity var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x),
+// i.e. stencil[dk][dj][di][var].
+template <class PA>
+__device__ __forceinline__ void viscous3d(const PA& P, double dx, double dy, double dz, double mu, double vf[3][5]) {
+  const double four_thirds = 4.0 / 3.0;
+  const double two_thirds = 2.0 / 3.0;
+  const double odx = 1.0 / dx, ody = 1.0 / dy, odz = 1.0 / dz;
+  const double c4x = 0.25 * odx, c4y = 0.25 * ody, c4z = 0.25 * odz;
+  const int U = 1, V = 2, W = 3;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) vf[d][v] = 0.0;
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IX
+    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
+    const double qiu = 0.5 * (P(1, 1, s, U) + P(1, 1, s - 1, U));
+    const double qiv = 0.5 * (P(1, 1, s, V) + P(1, 1, s - 1, V));
+    const double qiw = 0.5 * (P(1, 1, s, W) + P(1, 1, s - 1, W));
+    const double dudx = odx * (P(1, 1, s, U) - P(1, 1, s - 1, U));
+    const double dvdx = odx * (P(1, 1, s, V) - P(1, 1, s - 1, V));
+    const double dwdx = odx * (P(1, 1, s, W) - P(1, 1, s - 1, W));
+    const double dudy = c4y * (P(1, 2, s, U) - P(1, 0, s, U) + P(1, 2, s - 1, U) - P(1, 0, s - 1, U));
+    const double dvdy = c4y * (P(1, 2, s, V) - P(1, 0, s, V) + P(1, 2, s - 1, V) - P(1, 0, s - 1, V));
+    const double dudz = c4z * (P(2, 1, s, U) - P(0, 1, s, U) + P(2, 1, s - 1, U) - P(0, 1, s - 1, U));
+    const double dwdz = c4z * (P(2, 1, s, W) - P(0, 1, s, W) + P(2, 1, s - 1, W) - P(0, 1, s - 1, W));
+    const double tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
+    const double tau_xy = dvdx + dudy;
+    const double tau_xz = dwdx + dudz;
+    vf[0][1] += sm * tau_xx;
+    vf[0][2] += sm * tau_xy;
+    vf[0][3] += sm * tau_xz;
+    vf[0][4] += sm * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+  }
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IY
+    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
+    const double qiu = 0.5 * (P(1, s, 1, U) + P(1, s - 1, 1, U));
+    const double qiv = 0.5 * (P(1, s, 1, V) + P(1, s - 1, 1, V));
+    const double qiw = 0.5 * (P(1, s, 1, W) + P(1, s - 1, 1, W));
+    const double dudy = ody * (P(1, s, 1, U) - P(1, s - 1, 1, U));
+    const double dvdy = ody * (P(1, s, 1, V) - P(1, s - 1, 1, V));
+    const double dwdy = ody * (P(1, s, 1, W) - P(1, s - 1, 1, W));
+    const double dudx = c4x * (P(1, s, 2, U) - P(1, s, 0, U) + P(1, s - 1, 2, U) - P(1, s - 1, 0, U));
+    const double dvdx = c4x * (P(1, s, 2, V) - P(1, s, 0, V) + P(1, s - 1, 2, V) - P(1, s - 1, 0, V));
+    const double dwdz = c4z * (P(2, s, 1, W) - P(0, s, 1, W) + P(2, s - 1, 1, W) - P(0, s - 1, 1, W));
+    const double dvdz = c4z * (P(2, s, 1, V) - P(0, s, 1, V) + P(2, s - 1, 1, V) - P(0, s - 1, 1, V));
+    const double tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
+    const double tau_xy = dvdx + dudy;
+    const double tau_yz = dvdz + dwdy;
+    vf[1][1] += sm * tau_xy;
+    vf[1][2] += sm * tau_yy;
+    vf[1][3] += sm * tau_yz;
+    vf[1][4] += sm * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+  }
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IZ, with the reference's mix-ups
+    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
+    const double qiu = 0.5 * (P(s, 1, 1, U) + P(s - 1, 1, 1, U));
+    const double qiv = 0.5 * (P(s, 1, 1, V) + P(s - 1, 1, 1, V));
+    const double qiw = 0.5 * (P(s, 1, 1, W) + P(s - 1, 1, 1, W));
+    const double dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
+    const double dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
+    const double dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
+    const double dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
+    const double dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
+    const double dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
+    const double dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
+    const double tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+    const double tau_xz = dudz + dwdx;
+    const double tau_yz = dvdz + dwdy;
+    vf[2][1] += sm * tau_xz;
+    vf[2][2] += sm * tau_yz;
+    vf[2][3] += sm * tau_zz;
+    vf[2][4] += sm * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+  }
+}
+
+// Stencil accessor of viscous3d over the ring (column (hy, hx) of layer k).
+struct RingVel {
+  Smem3 S;
+  int k, hy, hx;
+  __device__ __forceinline__ double operator()(int dk, int dj, int di, int var) const {
+    return S.q(slot_of(k + dk - 1), var, hy + dj - 1, hx + di - 1);
+  }
+};
+
+template <int RS, int KIND>
+__global__ void __launch_bounds__(kThreads, 2)
+stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
+             int tz) {
+  extern __shared__ double smem_raw[];
+  __shared__ unsigned long long s_red[kThreads / 32];
+  const Smem3 S{smem_raw};
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+  const int k0 = blockIdx.z * tz;
+  const int k1 = min(k0 + tz, G.nc);
+  const int cx = tid % kTX, cy = tid / kTX;
+  const int x = x0 + cx, y = y0 + cy;
+  const bool own = x < G.na && y < G.nb;
+  const long long col = (long long)y * G.pitch + x;
+  const long long zstride = (long long)G.nb * G.pitch;
+
+  if (!ctrl->active) {
+    if (KIND == STAGE_EULER && own) {
+      for (int k = k0; k < k1; ++k) {
+        const long long o = k * zstride + col;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) uout.f[v][o] = uin.f[v][o];
+      }
+    }
+    return;
+  }
+  const double dt = ctrl->dt_cur;
+  const int parity = ctrl->parity;
+  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+  const int rs = RS;
+  const int recon = G.recon;
+  const bool need_pout = G.wb_flux_z || G.bc_c == DBC_C91;
+
+  // prologue: layers k0-2 .. k0+1, then the z face k0-1/2 of the own column
+  for (int kg = k0 - 2; kg <= k0 + 1; ++kg) load_layer(G, uin, x0, y0, kg, S, tid);
+  __syncthreads();
+  double fzL[5], poutL = 0.0;
+  if (own) {
+    double c[4][5];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k0 - 2 + m), v, cy + 2, cx + 2);
+    face3<2>(c, rs, recon, G, K, fzL, need_pout ? &poutL : nullptr);
+  }
+  __syncthreads();
+
+  unsigned long long red = 0ull;
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    // ---- 1. layer k+2 in, x and y faces of layer k ----
+    load_layer(G, uin, x0, y0, k + 2, S, tid);
+    const int sk = slot_of(k);
+    for (int it = tid; it < kNFA_PAD + kNFB; it += kThreads) {
+      double c[4][5], f[5];
+      if (it < kNFA_PAD) {
+        if (it >= kNFA) continue;
+        const int fy = it / (kTX + 1), fx = it - fy * (kTX + 1);
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+          for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + 2, fx + m);
+        face3<0>(c, rs, recon, G, K, f, nullptr);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) S.fa(v, fy, fx) = f[v];
+      } else {
+        const int j = it - kNFA_PAD;
+        const int fy = j / kTX, fx = j - fy * kTX;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+          for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + m, fx + 2);
+        face3<1>(c, rs, recon, G, K, f, nullptr);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) S.fb(v, fy, fx) = f[v];
+      }
+    }
+    __syncthreads();
+
+    // ---- 2. z face k+1/2 and the update of the own cell ----
+    if (own) {
+      double fzR[5], poutR = 0.0;
+      {
+        double c[4][5];
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+          for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k - 1 + m), v, cy + 2, cx + 2);
+        face3<2>(c, rs, recon, G, K, fzR, need_pout ? &poutR : nullptr);
+      }
+      const long long o = k * zstride + col;
+      double un[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) un[v] = uin.f[v][o];
+      // IX, IY: un += (F(-1/2) - F(+1/2)) * dt / d
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        un[v] = un[v] + div_cell((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx, G.pow2_x);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        un[v] = un[v] + div_cell((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, G.dy, G.inv_dy, G.pow2_y);
+      // IZ with the z-boundary overrides of Update.h:131-143
+      double fL[5], fR[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        fL[v] = fzL[v];
+        fR[v] = fzR[v];
+      }
+      const double rho_c = S.q(sk, 0, cy + 2, cx + 2);
+      if (G.wb_flux_z && (k == 0 || k == G.nc - 1)) {
+        if (k == 0) {
+          fL[0] = 0.0; fL[1] = 0.0; fL[2] = 0.0; fL[4] = 0.0;
+          fL[3] = poutR - rho_c * G.g * G.dz;
+        } else {
+          fR[0] = 0.0; fR[1] = 0.0; fR[2] = 0.0; fR[4] = 0.0;
+          fR[3] = poutL + rho_c * G.g * G.dz;
+        }
+      } else if (G.bc_c == DBC_C91 && (k == 0 || k == G.nc - 1)) {
+        if (k == 0) {
+          fL[0] = 0.0; fL[1] = 0.0; fL[2] = 0.0; fL[4] = 0.0;
+          fL[3] = poutL;
+        } else {
+          fR[0] = 0.0; fR[1] = 0.0; fR[2] = 0.0; fR[4] = 0.0;
+          fR[3] = poutR;
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) un[v] = un[v] + div_cell((fL[v] - fR[v]) * dt, G.dz, G.inv_dz, G.pow2_z);
+      if (G.gravity) {
+        un[3] = un[3] + dt * rho_c * G.g;
+        un[4] = un[4] + dt * 0.5 * (fL[0] + fR[0]) * G.g;
+      }
+      un[0] = fmax(1.0e-6, un[0]);
+
+      if (G.tc) {  // ThermalConduction.h:38-96
+        double kC, kF, kB;
+        if (G.kappa_z) {
+          kC = G.kappa_z[3 * k];
+          kF = G.kappa_z[3 * k + 1];
+          kB = G.kappa_z[3 * k + 2];
+        } else {
+          kC = kF = kB = 0.5 * (G.kappa + G.kappa);
+        }
+        const int hy = cy + 2, hx = cx + 2;
+        const double TC = S.temp(sk, hy, hx);
+        const double FL = div_cell(kC * (TC - S.temp(sk, hy, hx - 1)), G.dx, G.inv_dx, G.pow2_x);
+        const double FR = div_cell(kC * (S.temp(sk, hy, hx + 1) - TC), G.dx, G.inv_dx, G.pow2_x);
+        const double FU = div_cell(kC * (TC - S.temp(sk, hy - 1, hx)), G.dy, G.inv_dy, G.pow2_y);
+        const double FD = div_cell(kC * (S.temp(sk, hy + 1, hx) - TC), G.dy, G.inv_dy, G.pow2_y);
+        double FF = div_cell(kF * (TC - S.temp(slot_of(k - 1), hy, hx)), G.dz, G.inv_dz, G.pow2_z);
+        double FB = div_cell(kB * (S.temp(slot_of(k + 1), hy, hx) - TC), G.dz, G.inv_dz, G.pow2_z);
+        if (k == 0 && G.bctc_zmin != 0) {
+          if (G.bctc_zmin == 1) FF = div_cell(kF * 2.0 * (TC - G.bctc_zmin_value), G.dz, G.inv_dz, G.pow2_z);
+          else FF = kF * G.bctc_zmin_value;
+        }
+        if (k == G.nc - 1 && G.bctc_zmax != 0) {
+          if (G.bctc_zmax == 1) FB = div_cell(kB * 2.0 * (G.bctc_zmax_value - TC), G.dz, G.inv_dz, G.pow2_z);
+          else FB = kB * G.bctc_zmax_value;
+        }
+        const double dtdx = div_cell(dt, G.dx, G.inv_dx, G.pow2_x);
+        const double dtdy = div_cell(dt, G.dy, G.inv_dy, G.pow2_y);
+        const double dtdz = div_cell(dt, G.dz, G.inv_dz, G.pow2_z);
+        un[4] = un[4] + (dtdx * (FR - FL) + dtdy * (FD - FU) + dtdz * (FB - FF));
+      }
+      if (G.visc) {  // Viscosity.h:145-151
+        const RingVel P{S, k, cy + 2, cx + 2};
+        double vf[3][5];
+        viscous3d(P, G.dx, G.dy, G.dz, G.mu, vf);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
+      }
+      if (KIND == STAGE_RK_2) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) un[v] = 0.5 * (u0.f[v][o] + un[v]);
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) uout.f[v][o] = un[v];
+      if (KIND != STAGE_RK_1) {
+        const double inv = inv_dt_hyp64<PLANE_XY, true>(un, G);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
+        red = b > red ? b : red;
+        if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v) fzL[v] = fzR[v];
+      poutL = poutR;
+    }
+    __syncthreads();
+  }
+  if (KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+template <int RS, int KIND>
+cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, cudaStream_t st) {
+  auto kern = stage3d_fp64<RS, KIND>;
+  static bool attr_set = false;  // per instantiation, once per process
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem3::bytes(true));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int tx = (G.na + kTX - 1) / kTX, ty = (G.nb + kTY - 1) / kTY;
+  const int tz = stage3d_layers_per_cta(G);
+  dim3 grid(tx, ty, (G.nc + tz - 1) / tz);
+  kern<<<grid, kThreads, Smem3::bytes(G.tc != 0), st>>>(G, uin, u0, uout, ctrl, tz);
+  return cudaGetLastError();
+}
+
+template <int RS>
+cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
+                        cudaStream_t st) {
+  switch (kind) {
+    case STAGE_EULER: return launch_one<RS, STAGE_EULER>(G, uin, u0, uout, ctrl, st);
+    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1>(G, uin, u0, uout, ctrl, st);
+    default: return launch_one<RS, STAGE_RK_2>(G, uin, u0, uout, ctrl, st);
+  }
+}
+
+}  // namespace
+
+// z layers per CTA: enough CTAs to fill two waves of 2 CTAs on each of the
+// 152 SMs where the grid allows, at least 4 layers (the prologue loads four
+// layers and solves one extra z face per column).
+int stage3d_layers_per_cta(const Grid& G) {
+  const long long cols = (long long)((G.na + kTX - 1) / kTX) * ((G.nb + kTY - 1) / kTY);
+  const long long target = 2LL * 2 * 152;
+  long long chunks = (target + cols - 1) / cols;
+  if (chunks < 1) chunks = 1;
+  long long tz = (G.nc + chunks - 1) / chunks;
+  if (tz < 4) tz = 4;
+  if (tz > G.nc) tz = G.nc;
+  return (int)tz;
+}
+
+cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
+                           StepCtrl* ctrl, cudaStream_t st) {
+  return riemann_solver == 0 ? launch_kind<0>(G, kind, uin, u0, uout, ctrl, st)
+                             : launch_kind<1>(G, kind, uin, u0, uout, ctrl, st);
+}
+
+}  // namespace fv

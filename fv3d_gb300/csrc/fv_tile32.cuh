@@ -84,7 +84,7 @@ __device__ __forceinline__ void cons_to_prim32(const float u[5], float e_lo, flo
 }
 
 template <int PLANE, bool WACT>
-__device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, const Grid2D& G) {
+__device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, const Grid& G) {
   float q[5];
   cons_to_prim32<PLANE, WACT>(u, e_lo, G.gm1_f, q);
   const float cs = sqrtf(q[4] * G.gamma_f / q[0]);
@@ -213,7 +213,7 @@ __device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool pl
 //   STAGE_RK_2 : read U* (FP32) and U^n (pairs) -> write U^n+1 (pairs, over U^n)
 //   STAGE_EULER: read U^n (pairs in `src`) -> write U^n+1 (pairs in `dst`)
 template <int PLANE, bool WACT, class TL>
-__device__ __forceinline__ void stage_tile32(const Grid2D& G, const MixedFields& M, float2* const src[5],
+__device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M, float2* const src[5],
                                              float2* const dst[5], StepCtrl* ctrl, int rs, int kind, int bx, int by,
                                              float* smem, unsigned long long* s_red) {
   constexpr int NV = WACT ? 5 : 4;

@@ -246,7 +246,7 @@ __device__ __forceinline__ void from_slots(const T f[5], T out[5]) {
 // c[k][v] holds variable v of the four cells around the face (left-left,
 // left, right, right-right).
 template <int PLANE, bool WACT, int DIR>
-__device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool plm, bool wb_z, const Grid2D& G,
+__device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool plm, bool wb_z, const Grid& G,
                                             const Consts64& K, double out[5]) {
   constexpr int ZS = WACT ? 0 : (PLANE == PLANE_XY ? 2 : 1);
   double qL[5], qR[5];
@@ -283,7 +283,7 @@ __device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool p
 // rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
 // smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
 template <int PLANE, bool WACT, class TL>
-__device__ __forceinline__ void stage_tile64(const Grid2D& G, const Fields& uin, const Fields& u0, const Fields& uout,
+__device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                              StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
                                              unsigned long long* s_red) {
   constexpr int NV = WACT ? 5 : 4;

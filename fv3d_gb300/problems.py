@@ -20,6 +20,8 @@ only, Update.h:148):
   shear_layer      4096^2 periodic shear layer, gamma 5/3, kappa = mu = 1e-4, t = 1
   batch_sod_sedov  512 instances, sides in {64..256}, Sod tubes and blasts
   batch_rt         64 Rayleigh-Taylor instances, 256x768 ... 1024x3072
+  blast            the reference's 3-D blast (settings/blast.ini), n^3, PCM
+  random_problem   seeded random states for parity tests
 """
 import math
 from dataclasses import dataclass, field
@@ -218,6 +220,54 @@ def sod(n=128, axis="x", gamma=1.4, nx_other=None, tend=0.2, name="sod"):
     return Problem(name + "_" + axis, ini, [rho, z.copy(), z.copy(), z.copy(), prs], params=p)
 
 
+def blast(n=64, nz=None, tend=0.2, cfl=0.1, riemann="hllc", recon="pcm", name="blast"):
+    """The reference's blast problem (Init.h:72-100) on an n x n x nz grid
+    (settings/blast.ini: 64^3, PCM, HLLC, periodic, CFL 0.1): rho = 1,
+    p = 10 within r < 0.2 of the centre, rho = 1.2, p = 0.1 outside."""
+    nz = n if nz is None else nz
+    sec = {
+        "mesh": _mesh(n, n, nz),
+        "run": {"tend": tend, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                "boundaries_z": "periodic"},
+        "solvers": {"riemann_solver": riemann, "reconstruction": recon, "CFL": cfl},
+        "physics": {"gamma0": 1.4, "problem": "blast"},
+    }
+    ini = ini_text(sec)
+    p = _parse(ini)
+    X, Y, Z = _centres(p)
+    xr = 0.5 * (p.xmin + p.xmax) - X
+    yr = 0.5 * (p.ymin + p.ymax) - Y
+    zr = 0.5 * (p.zmin + p.zmax) - Z
+    r = np.sqrt(xr * xr + yr * yr + zr * zr)
+    inside = r < 0.2
+    rho = np.where(inside, 1.0, 1.2)
+    prs = np.where(inside, 10.0, 0.1)
+    z = np.zeros_like(X)
+    return Problem(name, ini, [rho, z.copy(), z.copy(), z.copy(), prs], params=p)
+
+
+def random_state(shape, seed, wmag=0.0, vmag=1.5):
+    """Seeded random primitive fields: rho, p in [0.5, 2), u, v in
+    (-vmag, vmag), w in (-wmag, wmag)."""
+    n = int(np.prod(shape))
+    u = lambda s: uniform(seed, s, n).reshape(shape)  # noqa: E731
+    rho = 0.5 + 1.5 * u(1)
+    prs = 0.5 + 1.5 * u(2)
+    vx = vmag * (2 * u(3) - 1)
+    vy = vmag * (2 * u(4) - 1)
+    vz = wmag * (2 * u(5) - 1)
+    return [rho, vx, vy, vz, prs]
+
+
+def random_problem(name, mesh, run, solvers, physics, seed, extra=None, wmag=0.0, vmag=1.5):
+    """A random state on the grid of `mesh` with the given .ini sections."""
+    sec = {"mesh": mesh, "run": run, "solvers": solvers, "physics": physics}
+    sec.update(extra or {})
+    ini = ini_text(sec)
+    p = _parse(ini)
+    return Problem(name, ini, random_state((p.Nz, p.Ny, p.Nx), seed, wmag=wmag, vmag=vmag), params=p)
+
+
 def batch_sod_sedov(n_inst=512, nsteps=200, seed=MASTER_SEED, sides=(64, 96, 128, 192, 256)):
     """Independent instances: side from `sides`, gamma ~ U[1.1, 1.67];
     even ids Sod tubes (x or y by a coin flip), odd ids point blasts."""
@@ -260,4 +310,5 @@ BUILDERS = {
     "thermal_pulse": thermal_pulse,
     "shear_layer": shear_layer,
     "sod": sod,
+    "blast": blast,
 }

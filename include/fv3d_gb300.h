@@ -158,7 +158,7 @@ int fvgpu_launch_count(const fv_sim* sim, long* count);
 int fvgpu_profile_enable(fv_sim* sim, int enable);
 int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
 
-/* One update (Euler or RK2 per params, with the given dt) of a 2-D problem
+/* One update (Euler or RK2 per params, with the given dt) of a problem
  * whose conserved state lives in device arrays the caller owns, allocating
  * no memory at all.  No counterpart in the reference: it exists for host
  * codes that cannot call cudaMalloc in their time loop -- applications whose
@@ -169,9 +169,11 @@ int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
  * until the process exits once the call has been used on that device.
  *   fields  device pointers to rho, rho*u, rho*v, rho*w, E of the interior
  *           cells, rows of Nx cells along x with a stride of `pitch`
- *           doubles, rows following y (Nz == 1) or z (Ny == 1); the
- *           momentum along the one-cell axis may be NULL when it is zero and
- *           viscosity is off.  Updated in place.
+ *           doubles, rows following y (Nz == 1), z (Ny == 1) or, for a
+ *           3-D grid, y then z (row k*Ny + j); in 2-D the momentum along the
+ *           one-cell axis may be NULL when it is zero and viscosity is off.
+ *           Updated in place.  B02 conductivity and reflecting one-cell
+ *           axes of 3-D grids need fvgpu_create (FV_ERR_UNSUPPORTED).
  *   pitch   row stride in doubles (>= Nx).  5 x pitch x rows x 8 bytes
  *           + 256 must fit in 32 MiB (e.g. 512 x 1536 at pitch 512); larger
  *           problems get FV_ERR_PARAM and a message -- use fvgpu_create.

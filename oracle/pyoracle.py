@@ -66,6 +66,8 @@ def load_ref():
         lib.fvref_read_ini.argtypes = [C.c_char_p, C.POINTER(FvParams)]
         lib.fvref_create.restype = C.c_void_p
         lib.fvref_create.argtypes = [C.c_char_p]
+        lib.fvref_create_b02.restype = C.c_void_p
+        lib.fvref_create_b02.argtypes = [C.c_char_p] + [C.c_double] * 4
         lib.fvref_destroy.argtypes = [C.c_void_p]
         for n in ("fvref_set_prim", "fvref_get_prim", "fvref_get_cons"):
             getattr(lib, n).argtypes = [C.c_void_p] + [_dp] * 5
@@ -156,10 +158,17 @@ class Oracle(_Base):
 class RefOracle(_Base):
     """The reference's own headers, compiled against the shim."""
 
-    def __init__(self, ini_path):
+    def __init__(self, ini_path, b02=None):
+        """b02 = (zmid, kappa1, kappa2, thickness) sets the B02 profile,
+        which the reference's readInifile leaves unset."""
         self.lib = load_ref()
         self.params = ref_read_ini(ini_path)
-        self._h = self.lib.fvref_create(ini_path.encode())
+        if b02 is None:
+            self._h = self.lib.fvref_create(ini_path.encode())
+        else:
+            self._h = self.lib.fvref_create_b02(ini_path.encode(), *[float(x) for x in b02])
+            (self.params.b02_zmid, self.params.b02_kappa1, self.params.b02_kappa2,
+             self.params.b02_thickness) = [float(x) for x in b02]
 
     def close(self):
         if self._h:

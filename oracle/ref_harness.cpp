@@ -99,6 +99,26 @@ int fvref_read_ini(const char* path, fv_params* out) {
   return FV_OK;
 }
 
+// readInifile never assigns the B02 profile (SimInfo.h:150-154 declare the
+// fields without initialisers and no key sets them), so a B02 run needs them
+// set on the Params before the functors copy it, as a C++ caller of the
+// reference would; fvref_create_b02 does that.
+void* fvref_create_b02(const char* ini_path, double zmid, double kappa1, double kappa2, double thickness) {
+  RefSim* s = new RefSim();
+  s->params = readInifile(ini_path);
+  s->params.b02_zmid = zmid;
+  s->params.b02_kappa1 = kappa1;
+  s->params.b02_kappa2 = kappa2;
+  s->params.b02_thickness = thickness;
+  const Params& p = s->params;
+  s->U = Array("U", p.Ntz, p.Nty, p.Ntx, Nfields);
+  s->Unew = Array("Unew", p.Ntz, p.Nty, p.Ntx, Nfields);
+  s->Q = Array("Q", p.Ntz, p.Nty, p.Ntx, Nfields);
+  s->update = new UpdateFunctor(s->params);
+  s->cdt = new ComputeDtFunctor(s->params);
+  return s;
+}
+
 void* fvref_create(const char* ini_path) {
   RefSim* s = new RefSim();
   s->params = readInifile(ini_path);

@@ -14,7 +14,7 @@ and Riemann-solver known answers (hll / hllc) on seeded state pairs that
 cover every wave-speed branch.
 
 Needs the reference sources (only present where the fixtures are made):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]
 """
 import json
 import os
@@ -31,23 +31,7 @@ from fv3d_gb300 import problems  # noqa: E402
 from oracle import pyoracle  # noqa: E402
 
 
-def random_state(shape, seed, wmag=0.0, vmag=1.5):
-    n = int(np.prod(shape))
-    u = lambda s: problems.uniform(seed, s, n).reshape(shape)  # noqa: E731
-    rho = 0.5 + 1.5 * u(1)
-    prs = 0.5 + 1.5 * u(2)
-    vx = vmag * (2 * u(3) - 1)
-    vy = vmag * (2 * u(4) - 1)
-    vz = wmag * (2 * u(5) - 1)
-    return [rho, vx, vy, vz, prs]
-
-
-def random_problem(name, mesh, run, solvers, physics, seed, extra=None, wmag=0.0):
-    sec = {"mesh": mesh, "run": run, "solvers": solvers, "physics": physics}
-    sec.update(extra or {})
-    ini = problems.ini_text(sec)
-    p = problems._parse(ini)
-    return problems.Problem(name, ini, random_state((p.Nz, p.Ny, p.Nx), seed, wmag=wmag), params=p)
+random_problem = problems.random_problem
 
 
 def cases():
@@ -111,6 +95,66 @@ def cases():
                                 "CFL": 0.5}, {"gamma0": 1.4}, seed=107, wmag=1.0,
                                extra={"thermal_conduction": {"active": True, "kappa": 0.01},
                                       "viscosity": {"active": True, "mu": 0.01}}), 2))
+    out += cases_z_physics()
+    return out
+
+
+def cases_z_physics():
+    """3-D grids and the z-boundary physics (C91 ghosts, well-balanced z
+    fluxes, fixed-temperature / gradient conduction boundaries, B02
+    conductivity), plus 2-D grids that need the 3-D kernel."""
+    out = []
+    b = problems.blast(16)
+    b.name = "blast_3d_pcm"
+    out.append((b, 3))
+    out.append((random_problem("c91_3d_tc_visc", problems._mesh(12, 10, 14),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "reflecting",
+                                "boundaries_z": "C91"},
+                               {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.3}, {"gamma0": 1.6666667, "gravity": True, "g": -1.5}, seed=201,
+                               wmag=0.5, vmag=0.5,
+                               extra={"polytrope": {"theta1": 2.0},
+                                      "thermal_conduction": {"active": True, "kappa": 0.02,
+                                                             "bc_zmin": "fixed_temperature",
+                                                             "bc_zmax": "fixed_gradient",
+                                                             "bc_zmin_value": 1.0, "bc_zmax_value": 2.0},
+                                      "viscosity": {"active": True, "mu": 0.01}}), 3))
+    wb = random_problem("wb_b02_3d", problems._mesh(10, 12, 16),
+                        {"tend": 1.0, "boundaries_x": "absorbing", "boundaries_y": "periodic",
+                         "boundaries_z": "reflecting"},
+                        {"riemann_solver": "hll", "reconstruction": "plm", "time_stepping": "RK2", "CFL": 0.4},
+                        {"gamma0": 1.4, "gravity": True, "g": -0.8, "well_balanced_flux_at_z_bc": True},
+                        seed=202, wmag=0.6,
+                        extra={"thermal_conduction": {"active": True, "kappa": 0.05,
+                                                      "conductivity_mode": "B02"}})
+    wb.b02 = (0.5, 1.0, 3.0, 0.1)
+    out.append((wb, 3))
+    out.append((random_problem("euler_3d_pcm_wb", problems._mesh(11, 9, 13),
+                               {"tend": 1.0, "boundaries_x": "reflecting", "boundaries_y": "absorbing",
+                                "boundaries_z": "absorbing"},
+                               {"riemann_solver": "hllc", "reconstruction": "pcm_wb", "time_stepping": "euler",
+                                "CFL": 0.5}, {"gamma0": 1.4, "gravity": True, "g": -0.5}, seed=203, wmag=0.8), 3))
+    out.append((random_problem("xy_gravity_rk2", problems._mesh(20, 16, 1),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "absorbing",
+                                "boundaries_z": "periodic"},
+                               {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4, "gravity": True, "g": -0.4}, seed=204), 3))
+    out.append((random_problem("xz_c91_bctc", problems._mesh(18, 1, 20),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                                "boundaries_z": "C91"},
+                               {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.4}, {"gamma0": 1.4, "gravity": True, "g": -1.0}, seed=205,
+                               vmag=0.5,
+                               extra={"polytrope": {"theta1": 1.5},
+                                      "thermal_conduction": {"active": True, "kappa": 0.02,
+                                                             "bc_zmin": "fixed_gradient",
+                                                             "bc_zmax": "fixed_temperature",
+                                                             "bc_zmin_value": 0.5, "bc_zmax_value": 1.2}}), 3))
+    out.append((random_problem("yz_plane_hll", problems._mesh(1, 20, 18),
+                               {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "reflecting",
+                                "boundaries_z": "absorbing"},
+                               {"riemann_solver": "hll", "reconstruction": "plm", "time_stepping": "RK2",
+                                "CFL": 0.5}, {"gamma0": 1.4}, seed=206, wmag=0.7), 3))
     return out
 
 
@@ -130,15 +174,20 @@ def riemann_kats(seed=2024, n=600):
     return out
 
 
-def main():
+def main(only=None):
+    """Writes every fixture, or with `only` (names) just those, keeping the
+    index complete."""
     pyoracle.load_ref()
     tmp = tempfile.mkdtemp()
     index = []
     for pr, nsteps in cases():
+        if only and pr.name not in only:
+            index.append({"name": pr.name, "steps": nsteps, "shape": list(pr.shape)})
+            continue
         path = os.path.join(tmp, pr.name + ".ini")
         with open(path, "w") as f:
             f.write(pr.ini)
-        ref = pyoracle.RefOracle(path)
+        ref = pyoracle.RefOracle(path, b02=getattr(pr, "b02", None))
         ref.set_prim(*pr.prim)
         q0 = np.stack(ref.get_prim())
         dts, q1 = [], None
@@ -155,10 +204,11 @@ def main():
                             ini=np.array(pr.ini), params=np.array(json.dumps(params)))
         index.append({"name": pr.name, "steps": nsteps, "shape": list(q0.shape[1:])})
         print(pr.name, q0.shape, dts[:2])
-    np.savez_compressed(os.path.join(HERE, "riemann_kats.npz"), **riemann_kats())
+    if not only:
+        np.savez_compressed(os.path.join(HERE, "riemann_kats.npz"), **riemann_kats())
     with open(os.path.join(HERE, "index.json"), "w") as f:
         json.dump(index, f, indent=1)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -46,12 +46,15 @@ def _to_host(arrs, shape):
     return [np.zeros(shape) if t is None else t[:, :nx].cpu().numpy().reshape(shape) for t in arrs]
 
 
-@pytest.mark.parametrize("case", ["rt_xz_null_v", "thermal_xy_visc"])
+@pytest.mark.parametrize("case", ["rt_xz_null_v", "thermal_xy_visc", "blast_3d_euler"])
 def test_noalloc_matches_handle_two_calls(case):
     torch = pytest.importorskip("torch")
     if case == "rt_xz_null_v":
         pr = problems.rayleigh_taylor(64, 192)
         skip = 2          # rho*v: zero in the x-z plane without viscosity
+    elif case == "blast_3d_euler":
+        pr = problems.blast(24, nz=20)  # 3-D kernel, Euler stepping (copies U* back)
+        skip = -1
     else:
         pr = problems.thermal_pulse(96)
         skip = -1         # viscosity drives rho*w: pass it
