@@ -352,6 +352,30 @@ def time_batch(torch, params_list, prims, nsteps, warmup, flush_each=None):
                "gpu_launches": b.launch_count() - l0}
 
 
+def time_sim(torch, pr, nsteps, warmup):
+    """Mcell-updates/s of one problem through fvgpu_* (CUDA events on its
+    stream, the state larger than L2 or the steps long enough to amortise)."""
+    import fv3d_gb300 as fv
+    sim = fv.Simulation(pr.params)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.set_prim(*pr.prim)
+    sim.enqueue_steps(warmup)
+    sim.synchronize()
+    l0 = sim.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.enqueue_steps(nsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    sim.get_prim()  # surfaces any error
+    out = {"mcell_updates_per_s": pr.cells * nsteps / (ms / 1e3) / 1e6, "ms_per_step": ms / nsteps,
+           "cells": pr.cells, "gpu_launches": sim.launch_count() - l0}
+    sim.close()
+    return out
+
+
 def l1_vs_fp64(torch, probs, nsteps, params_mixed):
     """Per-field relative L1 (worst instance) of the mixed batch against the
     bit-exact FP64 batch after nsteps steps."""
@@ -387,6 +411,9 @@ def _mass_energy(prim, gamma):
     rho, u, v, w, p = (np.asarray(a, dtype=np.float64) for a in prim)
     E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v + w * w)
     return float(math.fsum(rho.ravel())), float(math.fsum(E.ravel()))
+
+
+MASTER_SEED_3D = 12345
 
 
 def run_variants(torch, args, flush):
@@ -437,6 +464,19 @@ def run_variants(torch, args, flush):
     add("thermal_pulse_1024_fp64", r, 200)
     _, r = time_batch(torch, [_mixed(tp.params)], [tp.prim], 64, 8)
     add("thermal_pulse_1024_fp32_mixed", r, 160, l1_vs_fp64(torch, [tp], 200, [_mixed(tp.params)]))
+
+    # the reference's 3-D blast (settings/blast.ini: PCM, HLLC, Euler) at 256^3,
+    # and a 3-D PLM / RK2 / conduction + viscosity run at 192^3 (3-D kernel)
+    bl = problems.blast(256)
+    add("blast_3d_256_fp64", time_sim(torch, bl, 4, 2), 80)  # Euler: read + write 5 fields
+    tv = problems.random_problem("tc_visc_3d", problems._mesh(192, 192, 192),
+                                 {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                                  "boundaries_z": "periodic"},
+                                 {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                  "CFL": 0.4}, {"gamma0": 1.4}, seed=MASTER_SEED_3D, wmag=0.5,
+                                 extra={"thermal_conduction": {"active": True, "kappa": 1e-4},
+                                        "viscosity": {"active": True, "mu": 1e-4}})
+    add("random_3d_192_plm_rk2_tc_visc_fp64", time_sim(torch, tv, 2, 1), 200)
 
     # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
     sh = problems.shear_layer(4096)

@@ -125,22 +125,31 @@ def test_advance_matches_oracle_loop_3d():
     np.testing.assert_array_equal(np.stack(sim.get_prim()), np.stack(ora.get_prim()))
 
 
-def test_blast_3d_symmetry_and_conservation():
-    """The reference's blast problem (periodic, 48^3, PCM): mass and energy
-    are conserved to round-off and the x, y, z axes stay interchangeable."""
+def test_blast_3d_conservation_symmetry_trajectory():
+    """The reference's blast problem (periodic, 48^3, PCM, Euler): mass and
+    energy are conserved to round-off; after one step the x, y and z axes are
+    exactly interchangeable (later steps break the symmetry at round-off level
+    and HLLC's star-region switch amplifies it -- the reference does the
+    same); 20 free-running steps equal the oracle's bit for bit."""
     pr = problems.blast(48)
     sim = fv.Simulation(pr.params)
     sim.set_prim(*pr.prim)
+    ora = pyoracle.Oracle(pr.params)
+    ora.set_prim(*pr.prim)
     tot0 = sim.conserved_totals()
-    sim.enqueue_steps(20)
+    sim.enqueue_steps(1)
+    r, u, v, w, p = sim.get_prim()
+    np.testing.assert_array_equal(r, np.transpose(r, (0, 2, 1)))
+    np.testing.assert_array_equal(r, np.transpose(r, (2, 1, 0)))
+    np.testing.assert_array_equal(u, np.transpose(v, (0, 2, 1)))
+    np.testing.assert_array_equal(u, np.transpose(w, (2, 1, 0)))
+    sim.enqueue_steps(19)
     tot1 = sim.conserved_totals()
     assert abs(tot1[0] - tot0[0]) <= 1e-12 * abs(tot0[0])
     assert abs(tot1[4] - tot0[4]) <= 1e-12 * abs(tot0[4])
-    r, u, v, w, p = sim.get_prim()
-    np.testing.assert_allclose(r, np.transpose(r, (0, 2, 1)), rtol=1e-12, atol=1e-14)
-    np.testing.assert_allclose(u, np.transpose(v, (0, 2, 1)), rtol=1e-10, atol=1e-13)
-    np.testing.assert_allclose(r, np.transpose(r, (2, 1, 0)), rtol=1e-12, atol=1e-14)
-    np.testing.assert_allclose(u, np.transpose(w, (2, 1, 0)), rtol=1e-10, atol=1e-13)
+    for _ in range(20):
+        ora.step(ora.compute_dt())
+    np.testing.assert_array_equal(np.stack(sim.get_prim()), np.stack(ora.get_prim()))
 
 
 def test_nonzero_velocity_on_reflecting_one_cell_axis_rejected():
