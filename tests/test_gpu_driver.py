@@ -4,7 +4,10 @@ Runs fv3d_gb300/_lib/fv3d on a Sod tube settings file (the reference's own
 `sod_x` generator, Init.h:19-31) and checks the final snapshot against the
 oracle's loop over the same settings: same number of saves, bit-identical
 final primitive state.  Both the host loop (one compute_dt/step round trip
-per step, like main.cpp) and --device-loop are run.
+per step, like main.cpp) and --device-loop are run.  Two 3-D settings files
+shaped like the reference's settings/sod_x.ini (64 x 16 x 16, reflecting,
+PCM, Euler) and settings/blast.ini (periodic cube, PCM, HLLC, CFL 0.1),
+with shorter end times, run the same check on the 3-D kernel.
 """
 import os
 import re
@@ -65,6 +68,76 @@ def test_driver_matches_oracle(tmp_path, mode):
     t_o, n_o = ora.advance(p.tend)
     assert (steps, t_end) == (n_o, t_o)
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, 1, 8, 64)
+    np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
+
+
+SOD_3D = """[mesh]
+Nx=64
+Ny=16
+Nz=16
+[run]
+tend=0.02
+save_freq=0.01
+boundaries_x=reflecting
+boundaries_y=reflecting
+boundaries_z=reflecting
+[solvers]
+riemann_solver=hllc
+reconstruction=pcm
+CFL=0.1
+[physics]
+gamma0=1.666666667
+problem=sod_x
+"""
+
+BLAST_3D = """[mesh]
+Nx=32
+Ny=32
+Nz=32
+[run]
+tend=0.01
+save_freq=0.004
+boundaries_x=periodic
+boundaries_y=periodic
+boundaries_z=periodic
+[solvers]
+riemann_solver=hllc
+reconstruction=pcm
+CFL=0.1
+[physics]
+gamma0=1.4
+problem=blast
+"""
+
+
+def _ic_3d(p, problem):
+    if problem == "blast":
+        return problems.blast(p.Nx, nz=p.Nz).prim
+    X = p.xmin + (np.arange(p.Nx) + 0.5) * p.dx
+    left = np.broadcast_to(X <= 0.5, (p.Nz, p.Ny, p.Nx))
+    z = np.zeros((p.Nz, p.Ny, p.Nx))
+    return [np.where(left, 1.0, 0.125), z, z, z, np.where(left, 1.0, 0.1)]
+
+
+@pytest.mark.parametrize("problem", ["sod_x", "blast"])
+def test_driver_3d_matches_oracle(tmp_path, problem):
+    text = SOD_3D if problem == "sod_x" else BLAST_3D
+    exe = os.path.join(build.lib_dir(), "fv3d")
+    ini = tmp_path / "run.ini"
+    ini.write_text(text)
+    prefix = str(tmp_path / "snap")
+    r = subprocess.run([exe, str(ini), "--out", prefix, "--device-loop"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
+    steps, t_end = int(m.group(1)), float(m.group(2))
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_"))
+    p = fv.parse_ini(text)
+    ora = pyoracle.Oracle(p)
+    ora.set_prim(*_ic_3d(p, problem))
+    t_o, n_o = ora.advance(p.tend)
+    assert (steps, t_end) == (n_o, t_o)
+    got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, p.Nz, p.Ny, p.Nx)
     np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
 
 
