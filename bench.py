@@ -46,6 +46,11 @@ ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2
 # RK2 step of this workload, from one ncu --set full capture
 # (profiles/stage2d_fp64_rt512x1536.md: 25.29+0.09 MB and 50.40+0.12 MB).
 NCU_TRAFFIC_BYTES_PER_STEP = 75.90e6
+# FP64-pipe lane operations per cell-update of this workload (stage 1: 450,
+# stage 2: 507; (fused + non-fused FP64 warp instructions) x 32 / cells from
+# the same capture).  The FP64 kernel is bound by the FP64 pipe: its roofline
+# against the FP64 rate measured live by fvgpu_probe_fp64_rate.
+FP64_OPS_PER_CELL_UPDATE = 957
 
 
 def peaks():
@@ -246,6 +251,11 @@ def run_gpu(args):
                 "algo_bytes": ALGO_BYTES_PER_CELL_UPDATE * pr.cells,
                 "algo_bytes_per_cell_update": ALGO_BYTES_PER_CELL_UPDATE,
                 "stage_ms_per_launch": stage_ms / stage_n, "dt_kernel_ms_per_launch": kt["dt"][1] / max(kt["dt"][0], 1)}
+    fp64_peak = fv.probe_fp64_rate()
+    fp64_achieved = FP64_OPS_PER_CELL_UPDATE * pr.cells / (ms_per_step_stages / 1e3)
+    roofline["fp64_pipe"] = {"achieved": fp64_achieved, "peak": fp64_peak, "frac": fp64_achieved / fp64_peak,
+                             "unit": "FP64 lane-ops/s", "peak_kind": "measured live (fvgpu_probe_fp64_rate)",
+                             "ops_per_cell_update": FP64_OPS_PER_CELL_UPDATE}
 
     # e2e through the C ABI with pinned host buffers
     host_in = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in pr.prim]
@@ -413,7 +423,16 @@ def _mass_energy(prim, gamma):
     return float(math.fsum(rho.ravel())), float(math.fsum(E.ravel()))
 
 
-MASTER_SEED_3D = 12345
+def random_3d(n):
+    """n^3 periodic random state, HLLC, PLM, RK2, conduction + viscosity."""
+    from fv3d_gb300 import problems
+    return problems.random_problem("tc_visc_3d", problems._mesh(n, n, n),
+                                   {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
+                                    "boundaries_z": "periodic"},
+                                   {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
+                                    "CFL": 0.4}, {"gamma0": 1.4}, seed=12345, wmag=0.5,
+                                   extra={"thermal_conduction": {"active": True, "kappa": 1e-4},
+                                          "viscosity": {"active": True, "mu": 1e-4}})
 
 
 def run_variants(torch, args, flush):
@@ -469,14 +488,7 @@ def run_variants(torch, args, flush):
     # and a 3-D PLM / RK2 / conduction + viscosity run at 192^3 (3-D kernel)
     bl = problems.blast(256)
     add("blast_3d_256_fp64", time_sim(torch, bl, 4, 2), 80)  # Euler: read + write 5 fields
-    tv = problems.random_problem("tc_visc_3d", problems._mesh(192, 192, 192),
-                                 {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic",
-                                  "boundaries_z": "periodic"},
-                                 {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2",
-                                  "CFL": 0.4}, {"gamma0": 1.4}, seed=MASTER_SEED_3D, wmag=0.5,
-                                 extra={"thermal_conduction": {"active": True, "kappa": 1e-4},
-                                        "viscosity": {"active": True, "mu": 1e-4}})
-    add("random_3d_192_plm_rk2_tc_visc_fp64", time_sim(torch, tv, 2, 1), 200)
+    add("random_3d_192_plm_rk2_tc_visc_fp64", time_sim(torch, random_3d(192), 2, 1), 200)
 
     # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
     sh = problems.shear_layer(4096)
@@ -493,13 +505,14 @@ def run_profile_case(args):
     workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
     batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
     512-instance set, to keep captures small), shear_mixed / shear_fp64 (the
-    4096^2 shear layer, a state larger than L2)."""
+    4096^2 shear layer, a state larger than L2), fp64_3d (a 160^3 random
+    state, HLLC, PLM, RK2, conduction + viscosity: the 3-D kernel)."""
     import fv3d_gb300 as fv
     from fv3d_gb300 import problems
     case = args.profile_case
     n = args.warmup + args.steps
-    if case == "fp64_rt":
-        pr = problem()
+    if case in ("fp64_rt", "fp64_3d"):
+        pr = problem() if case == "fp64_rt" else random_3d(160)
         sim = fv.Simulation(pr.params)
         sim.set_prim(*pr.prim)
         sim.enqueue_steps(n)
@@ -529,8 +542,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-case", nargs="?", const="fp64_rt", default=None,
-                    choices=["fp64_rt", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64", "shear_mixed",
-                             "shear_fp64"],
+                    choices=["fp64_rt", "fp64_3d", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64",
+                             "shear_mixed", "shear_fp64"],
                     help="run only a workload's steps (for ncu); prints no JSON")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other configurations (mixed, batched, shear layer)")

@@ -98,12 +98,22 @@ def _declare(lib):
         "fvgpu_batch_set_stream": (C.c_int, [vp, vp]),
         "fvgpu_batch_synchronize": (C.c_int, [vp]),
         "fvgpu_batch_launch_count": (C.c_int, [vp, C.POINTER(C.c_long)]),
+        "fvgpu_probe_fp64_rate": (C.c_int, [_dp]),
         "fvgpu_batch_tiling": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+
+
+def probe_fp64_rate():
+    """Measured FP64 FMA lane operations per second of the current GPU."""
+    r = C.c_double(0.0)
+    rc = load_library().fvgpu_probe_fp64_rate(C.byref(r))
+    if rc:
+        raise FvError(rc, "fvgpu_probe_fp64_rate")
+    return r.value
 
 
 def parse_ini(text):

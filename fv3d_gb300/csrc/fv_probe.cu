@@ -1,0 +1,64 @@
+// fv_probe.cu -- measures the FP64 FMA throughput of the current GPU.
+//
+// The bit-exact FP64 stage kernels are bound by the FP64 pipe, not by HBM,
+// so their roofline is the FP64 instruction rate.  fvgpu_probe_fp64_rate
+// measures it with a throughput loop: every thread of a full-occupancy grid
+// runs eight independent fma chains (enough independent work to cover the
+// pipe latency), timed with CUDA events after one warm-up launch.
+#include <cuda_runtime.h>
+
+#include "fv3d_gb300.h"
+
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kThreads = 256;
+
+__global__ void __launch_bounds__(kThreads) dfma_loop(double a, double b, int iters, double* sink) {
+  double x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) x[c] = (double)(threadIdx.x + c) * 1.0e-3;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = fma(x[c], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) s += x[c];
+  if (s == -1.0) sink[0] = s;  // keeps the chains live; never true for these inputs
+}
+
+}  // namespace
+
+extern "C" int fvgpu_probe_fp64_rate(double* lane_ops_per_s) {
+  if (!lane_ops_per_s) return FV_ERR_PARAM;
+  *lane_ops_per_s = 0.0;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dfma_loop, kThreads, 0) != cudaSuccess)
+    return FV_ERR_CUDA;
+  double* sink = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess) return FV_ERR_NOMEM;
+  int rc = FV_OK;
+  const int blocks = sms * (per_sm > 0 ? per_sm : 1);
+  const int iters = 4096;
+  float ms = 0.f;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = FV_ERR_CUDA;
+  } else {
+    dfma_loop<<<blocks, kThreads>>>(0.999999, 1.0e-7, iters, sink);  // warm-up
+    cudaEventRecord(e0);
+    dfma_loop<<<blocks, kThreads>>>(0.999999, 1.0e-7, iters, sink);
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f)
+      rc = FV_ERR_CUDA;
+  }
+  if (rc == FV_OK)
+    *lane_ops_per_s = (double)blocks * kThreads * (double)iters * kChains / (ms * 1.0e-3);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(sink);
+  return rc;
+}

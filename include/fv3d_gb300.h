@@ -188,6 +188,12 @@ int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
 int fvgpu_step_noalloc(const fv_params* params, double* const fields[5], long pitch, double dt,
                        double* next_dt, void* stream, char* errbuf, size_t errlen);
 
+/* FP64 FMA throughput of the current device in lane operations per second
+ * (a full-occupancy throughput loop of independent fma chains, timed after a
+ * warm-up launch).  The bit-exact FP64 kernels are bound by this rate; the
+ * bench reports their FP64 roofline against it.  No reference counterpart. */
+int fvgpu_probe_fp64_rate(double* lane_ops_per_s);
+
 /* ---- many independent problems (no reference counterpart) --------------- */
 typedef struct fv_batch fv_batch;
 
