@@ -99,6 +99,7 @@ def _declare(lib):
         "fvgpu_batch_synchronize": (C.c_int, [vp]),
         "fvgpu_batch_launch_count": (C.c_int, [vp, C.POINTER(C.c_long)]),
         "fvgpu_probe_fp64_rate": (C.c_int, [_dp]),
+        "fvgpu_step_host": (C.c_int, [vp, C.POINTER(_dp), C.c_double, C.POINTER(_dp), _dp]),
         "fvgpu_batch_tiling": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
     }
     for name, (res, args) in sig.items():
@@ -136,6 +137,15 @@ def read_ini(path):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _checked(a, shape):
+    """An array passed by address: must already be float64, C-contiguous and
+    of the grid's shape (no copy is made, so results land in the caller's
+    memory)."""
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.shape == shape):
+        raise ValueError("expected a C-contiguous float64 array of shape %s" % (shape,))
+    return a
 
 
 def _as_field(a, shape):
@@ -223,6 +233,19 @@ class Simulation:
         self._check(self.lib.fvgpu_advance(self._h, float(tend), int(max_steps), C.byref(tt), C.byref(n)),
                     "advance")
         return tt.value, n.value
+
+    def step_host(self, prim_in, dt=0.0, out=None):
+        """One step from and to primitive arrays the GPU reads and writes
+        directly (fvgpu_step_host); dt <= 0 takes the CFL dt.  Arrays must be
+        C-contiguous float64 of the grid's shape (pinned host memory for full
+        speed).  Returns (out, dt_used)."""
+        ins = (_dp * 5)(*[None if a is None else _ptr(_checked(a, self.shape)) for a in prim_in])
+        if out is None:
+            out = [np.empty(self.shape, np.float64) for _ in range(5)]
+        outs = (_dp * 5)(*[None if a is None else _ptr(_checked(a, self.shape)) for a in out])
+        used = C.c_double(0.0)
+        self._check(self.lib.fvgpu_step_host(self._h, ins, float(dt), outs, C.byref(used)), "step_host")
+        return out, used.value
 
     def enqueue_steps(self, nsteps):
         """Queue nsteps CFL steps on the GPU and return without waiting."""

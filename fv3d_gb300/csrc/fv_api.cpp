@@ -298,7 +298,7 @@ enum StepMode { STEP_LOOP = -1, STEP_GIVEN_DT = 0, STEP_FIXED = 2 };
 // Launches the kernels of one time step (control + stages) on the stream.
 // STEP_GIVEN_DT uses the host-supplied dt; STEP_LOOP derives dt from the CFL
 // reduction and stops at the loop bound; STEP_FIXED derives dt with no bound.
-int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
+int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fields* hout = nullptr) {
   {
     Timed t(s, KC_DT);
     cudaError_t e = fv::launch_control(s->d_ctrl, 1, mode, dt, s->stream);
@@ -315,7 +315,8 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
     }
     {
       Timed t(s, KC_STAGE);
-      cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream);
+      cudaError_t e =
+          fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream, hout);
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 2 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
@@ -323,7 +324,7 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true) {
     Timed t(s, KC_STAGE);
     const Fields& in = Current(s);
     const Fields& out = s->cur == 0 ? s->B : s->A;
-    cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream);
+    cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream, hout);
     if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "euler stage launch: %s", cudaGetErrorString(e));
     if (counting) t.done();
     s->cur ^= 1;
@@ -394,6 +395,26 @@ bool AnyNonzero(const double* a, long long n) {
   for (long long i = 0; i < n; ++i)
     if (a[i] != 0.0) return true;
   return false;
+}
+
+// A pointer the GPU can dereference for p (device, managed or pinned host
+// memory, or ordinary host memory where the device reads pageable memory),
+// or null.  *host tells whether the CPU may read it.
+const double* DeviceView(const double* p, bool* host) {
+  *host = false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    a.type = cudaMemoryTypeUnregistered;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return (const double*)a.devicePointer;
+  *host = true;
+  if (a.type == cudaMemoryTypeHost) return (const double*)a.devicePointer;
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
+    return nullptr;
+  return pageable ? p : nullptr;
 }
 
 int SetState(fv_sim* s, const double* const ref_fields[5], bool prim) {
@@ -577,6 +598,64 @@ int fvgpu_get_cons(fv_sim* s, double* rho, double* mx, double* my, double* mz, d
     dst[3] = nullptr;
   }
   return CopyOut(s, Current(s), dst);
+}
+
+int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double* const prim_out[5],
+                    double* dt_used) {
+  if (!s || !s->buf || !prim_in) return s ? Fail(s, FV_ERR_PARAM, "null argument or unconfigured handle")
+                                          : FV_ERR_PARAM;
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  Fields src{}, hout{};
+  bool host_in[5] = {false, false, false, false, false};
+  for (int k = 0; k < 5; ++k) {
+    const int v = slot_of[k];
+    if (prim_in[k]) {
+      src.f[v] = (double*)DeviceView(prim_in[k], &host_in[v]);
+      if (!src.f[v]) return Fail(s, FV_ERR_PARAM, "input array %d is not addressable by the GPU", k);
+    }
+    if (prim_out && prim_out[k]) {
+      bool h;
+      hout.f[v] = (double*)DeviceView(prim_out[k], &h);
+      if (!hout.f[v]) return Fail(s, FV_ERR_PARAM, "output array %d is not addressable by the GPU", k);
+    }
+  }
+  if (!src.f[0] || !src.f[4]) return Fail(s, FV_ERR_PARAM, "density and pressure arrays are required");
+  const long long ncell = (long long)s->G.na * s->G.rows;
+  // the same checks as set_prim; arrays only the GPU can read are not scanned
+  if (s->G.ndim == 3) {
+    s->wact = true;
+    for (int a = 0; a < 3; ++a)
+      if ((s->refl_deg >> a & 1) && src.f[1 + a] &&
+          (!host_in[1 + a] || AnyNonzero(prim_in[1 + a], ncell)))
+        return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting one-cell axis is not built");
+  } else {
+    const double* c = prim_in[slot_of[3]];
+    s->wact = s->p.viscosity_active || (c && (!host_in[3] || AnyNonzero(c, ncell)));
+    if (s->wact && s->deg_bc == FV_BC_REFLECTING)
+      return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  }
+  s->cur = 0;
+  const bool cfl = !(dt > 0.0);
+  const int slot = (int)(s->step & 1);
+  if (cfl) CUDA_TRY(s, cudaMemsetAsync(&s->d_ctrl->slot[slot], 0, sizeof(unsigned long long), s->stream));
+  {
+    Timed t(s, KC_CONV);
+    cudaError_t e = fv::launch_prim_to_cons_from(s->G, s->wact, src, s->A, cfl ? s->d_ctrl : nullptr, slot,
+                                                 s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "primToCons launch: %s", cudaGetErrorString(e));
+    t.done();
+  }
+  s->state_set = true;
+  int rc = EnqueueStep(s, cfl ? STEP_FIXED : STEP_GIVEN_DT, dt, true, prim_out ? &hout : nullptr);
+  if (rc) return rc;
+  s->step += 1;
+  s->slot_valid = true;
+  rc = ReadCtrl(s);
+  if (rc) return rc;
+  if (dt_used) *dt_used = s->h_ctrl->dt_cur;
+  if (s->h_ctrl->err) return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt");
+  return FV_OK;
 }
 
 int fvgpu_compute_dt(fv_sim* s, double* dt, double inv[3]) {

@@ -102,6 +102,42 @@ __global__ void prim_to_cons2d(const Grid G, const Fields u) {
   }
 }
 
+// primToCons from unpadded primitive arrays the GPU can address (a caller's
+// host arrays), optionally with the CFL maximum of the result.  Same
+// arithmetic as prim_to_cons2d.
+template <int PLANE, bool WACT, bool REDUCE>
+__global__ void __launch_bounds__(256) prim_to_cons_from(const Grid G, const Fields src, const Fields dst,
+                                                         StepCtrl* ctrl, int slot) {
+  __shared__ unsigned long long s_red[8];
+  unsigned long long red = 0ull;
+  const long long n = (long long)G.na * G.rows;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
+    const long long o = (long long)y * G.pitch + x;
+    const double r = src.f[0][c];
+    const double va = src.f[1] ? src.f[1][c] : 0.0, vb = src.f[2] ? src.f[2][c] : 0.0;
+    const double vc = (WACT && src.f[3]) ? src.f[3][c] : 0.0;
+    const double ma = __dmul_rn(r, va), mb = __dmul_rn(r, vb), mc = __dmul_rn(r, vc);
+    const double mx = ma, my = PLANE == PLANE_XY ? mb : mc, mz = PLANE == PLANE_XY ? mc : mb;
+    const double sq = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
+    const double Ek = __ddiv_rn(__dmul_rn(0.5, sq), r);
+    const double E = __dadd_rn(Ek, __ddiv_rn(src.f[4][c], G.gm1));
+    dst.f[0][o] = r;
+    dst.f[1][o] = ma;
+    dst.f[2][o] = mb;
+    if (WACT) dst.f[3][o] = mc;
+    dst.f[4][o] = E;
+    if (REDUCE) {
+      const double u[5] = {r, ma, mb, mc, E};
+      const double inv = inv_dt_hyp64<PLANE, WACT>(u, G);
+      const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
+      red = b > red ? b : red;
+      if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+    }
+  }
+  if (REDUCE) block_max_atomic(red, &ctrl->slot[slot], s_red);
+}
+
 // consToPrim (States.h:34-45); src and dst may alias.
 template <int PLANE>
 __global__ void cons_to_prim2d(const Grid G, const Fields src, const Fields dst) {
@@ -190,6 +226,25 @@ cudaError_t launch_prim_to_cons2d(const Grid& G, Fields u, cudaStream_t st) {
   if (G.plane == PLANE_XY) prim_to_cons2d<PLANE_XY><<<grid, 256, 0, st>>>(G, u);
   else prim_to_cons2d<PLANE_XZ><<<grid, 256, 0, st>>>(G, u);
   return cudaGetLastError();
+}
+
+template <int PLANE, bool WACT>
+cudaError_t launch_p2c_from(const Grid& G, Fields src, Fields dst, StepCtrl* ctrl, int slot, cudaStream_t st) {
+  const int grid = grid_for((long long)G.na * G.rows, 256);
+  if (ctrl)
+    prim_to_cons_from<PLANE, WACT, true><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot);
+  else
+    prim_to_cons_from<PLANE, WACT, false><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prim_to_cons_from(const Grid& G, bool wact, Fields src, Fields dst, StepCtrl* ctrl, int slot,
+                                     cudaStream_t st) {
+  if (G.plane == PLANE_XY)
+    return wact ? launch_p2c_from<PLANE_XY, true>(G, src, dst, ctrl, slot, st)
+                : launch_p2c_from<PLANE_XY, false>(G, src, dst, ctrl, slot, st);
+  return wact ? launch_p2c_from<PLANE_XZ, true>(G, src, dst, ctrl, slot, st)
+              : launch_p2c_from<PLANE_XZ, false>(G, src, dst, ctrl, slot, st);
 }
 
 cudaError_t launch_cons_to_prim2d(const Grid& G, Fields src, Fields dst, cudaStream_t st) {

@@ -14,9 +14,22 @@ struct Fields {
   double* f[5];
 };
 
-// Tile of the 2-D FP64 stage kernel.
-constexpr int kTileX = 32;
-constexpr int kTileY = 16;
+// Tile of the 2-D FP64 stage kernel, and the resident CTAs per SM its
+// register allocation targets (without / with the third momentum).
+#ifndef FV_TILE2D_X
+#define FV_TILE2D_X 32
+#endif
+#ifndef FV_TILE2D_Y
+#define FV_TILE2D_Y 16
+#endif
+#ifndef FV_FP64_MIN_CTAS
+#define FV_FP64_MIN_CTAS 3
+#endif
+#ifndef FV_FP64_MIN_CTAS_W
+#define FV_FP64_MIN_CTAS_W 2
+#endif
+constexpr int kTileX = FV_TILE2D_X;
+constexpr int kTileY = FV_TILE2D_Y;
 
 // One fused stage (Euler step, RK2 stage 1 or RK2 stage 2) over a 2-D plane.
 //   uin  : the stage's input state (read with a 2-cell ghost halo)
@@ -24,22 +37,33 @@ constexpr int kTileY = 16;
 //   uout : output state (may alias u0 for STAGE_RK_2; never uin)
 // dt and the active flag come from ctrl (set by launch_control); STAGE_EULER
 // and STAGE_RK_2 also reduce max inv_dt_hyp of their output into
-// ctrl->slot[parity ^ 1].
+// ctrl->slot[parity ^ 1].  hout (optional, STAGE_EULER / STAGE_RK_2 only):
+// the stage also writes the primitives of its result, storage order, to
+// unpadded arrays of na x rows values that the GPU can address (device or
+// host memory).
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                           Fields uout, StepCtrl* ctrl, cudaStream_t stream);
+                           Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
 
 // The same stage over a 3-D grid (G.ndim == 3): one CTA per 16 x 16 block of
 // columns and stage3d_layers_per_cta(G) z layers; always carries w.
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
-                           StepCtrl* ctrl, cudaStream_t stream);
+                           StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
 int stage3d_layers_per_cta(const Grid& G);
 
 // The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
 inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                                Fields uout, StepCtrl* ctrl, cudaStream_t stream) {
-  if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream);
-  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream);
+                                Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr) {
+  if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream, hout);
+  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout);
 }
+
+// primToCons (States.h:20-31) from primitive arrays the GPU can address
+// (unpadded rows of na values, storage order, a null field reads as 0) into
+// the padded conserved state dst; with ctrl, also the CFL maximum of
+// consToPrim of the result into ctrl->slot[slot] (ComputeDt.h:28-54, the
+// reference's dt after its set-up).
+cudaError_t launch_prim_to_cons_from(const Grid& G, bool wact, Fields src, Fields dst, StepCtrl* ctrl, int slot,
+                                     cudaStream_t stream);
 
 // Reduce max inv_dt_hyp of state u into ctrl->slot[slot] (caller zeroes it).
 cudaError_t launch_reduce2d(const Grid& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t stream);

@@ -49,10 +49,15 @@ __device__ __forceinline__ void cons_to_prim64(const double u[5], double gm1, do
 
 // Hyperbolic inverse time step of one cell, ComputeDt.h:49-52:
 // (cs + |u|)/dx + (cs + |v|)/dy + (cs + |w|)/dz with cs = sqrt(p*gamma/rho).
+// qout, when given, receives the primitives consToPrim computes on the way.
 template <int PLANE, bool WACT>
-__device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid& G) {
+__device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid& G, double* qout = nullptr) {
   double q[5], y;
   cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+  if (qout) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qout[v] = q[v];
+  }
   const double cs = sqrt(div_by_rcp(__dmul_rn(q[4], G.gamma), q[0], y));
   const double vx = q[1], vy = PLANE == PLANE_XY ? q[2] : q[3], vz = PLANE == PLANE_XY ? q[3] : q[2];
   const double tx = div_cell(__dadd_rn(cs, fabs(vx)), G.dx, G.inv_dx, G.pow2_x);

@@ -302,7 +302,7 @@ struct RingVel {
 template <int RS, int KIND>
 __global__ void __launch_bounds__(kThreads, 2)
 stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             int tz) {
+             int tz, const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
   const Smem3 S{smem_raw};
@@ -478,10 +478,17 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
 #pragma unroll
       for (int v = 0; v < 5; ++v) uout.f[v][o] = un[v];
       if (KIND != STAGE_RK_1) {
-        const double inv = inv_dt_hyp64<PLANE_XY, true>(un, G);
+        double q[5];
+        const double inv = inv_dt_hyp64<PLANE_XY, true>(un, G, q);
         const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
         red = b > red ? b : red;
         if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+        if (hout.f[0]) {  // primitives to the caller's unpadded arrays
+          const long long h = ((long long)k * G.nb + y) * G.na + x;
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            if (hout.f[v]) hout.f[v][h] = q[v];
+        }
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) fzL[v] = fzR[v];
@@ -493,7 +500,8 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
 }
 
 template <int RS, int KIND>
-cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, cudaStream_t st) {
+cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, const Fields* hout,
+                       cudaStream_t st) {
   auto kern = stage3d_fp64<RS, KIND>;
   static bool attr_set = false;  // per instantiation, once per process
   if (!attr_set) {
@@ -504,17 +512,18 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   const int tx = (G.na + kTX - 1) / kTX, ty = (G.nb + kTY - 1) / kTY;
   const int tz = stage3d_layers_per_cta(G);
   dim3 grid(tx, ty, (G.nc + tz - 1) / tz);
-  kern<<<grid, kThreads, Smem3::bytes(G.tc != 0), st>>>(G, uin, u0, uout, ctrl, tz);
+  const Fields none{};
+  kern<<<grid, kThreads, Smem3::bytes(G.tc != 0), st>>>(G, uin, u0, uout, ctrl, tz, hout ? *hout : none);
   return cudaGetLastError();
 }
 
 template <int RS>
 cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                        cudaStream_t st) {
+                        const Fields* hout, cudaStream_t st) {
   switch (kind) {
-    case STAGE_EULER: return launch_one<RS, STAGE_EULER>(G, uin, u0, uout, ctrl, st);
-    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1>(G, uin, u0, uout, ctrl, st);
-    default: return launch_one<RS, STAGE_RK_2>(G, uin, u0, uout, ctrl, st);
+    case STAGE_EULER: return launch_one<RS, STAGE_EULER>(G, uin, u0, uout, ctrl, hout, st);
+    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1>(G, uin, u0, uout, ctrl, nullptr, st);
+    default: return launch_one<RS, STAGE_RK_2>(G, uin, u0, uout, ctrl, hout, st);
   }
 }
 
@@ -535,9 +544,9 @@ int stage3d_layers_per_cta(const Grid& G) {
 }
 
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
-                           StepCtrl* ctrl, cudaStream_t st) {
-  return riemann_solver == 0 ? launch_kind<0>(G, kind, uin, u0, uout, ctrl, st)
-                             : launch_kind<1>(G, kind, uin, u0, uout, ctrl, st);
+                           StepCtrl* ctrl, cudaStream_t st, const Fields* hout) {
+  return riemann_solver == 0 ? launch_kind<0>(G, kind, uin, u0, uout, ctrl, hout, st)
+                             : launch_kind<1>(G, kind, uin, u0, uout, ctrl, hout, st);
 }
 
 }  // namespace fv

@@ -282,10 +282,15 @@ __device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool p
 // One stage of one tile (bx, by) of problem G; see the file comment.
 // rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
 // smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
+//
+// hout (optional, last stage of a step only): primitive output arrays in
+// storage order with rows of G.na values and no padding (a caller's host
+// arrays the GPU can address); the stage writes consToPrim of its result
+// there, the values the CFL term computes anyway.
 template <int PLANE, bool WACT, class TL>
 __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                              StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
-                                             unsigned long long* s_red) {
+                                             unsigned long long* s_red, const Fields* hout = nullptr) {
   constexpr int NV = WACT ? 5 : 4;
   constexpr int TX = TL::TX, TY = TL::TY, HX = TL::HX, HY = TL::HY;
   const TileSmem<double, NV, TL> S{smem};
@@ -430,10 +435,17 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
     for (int v = 0; v < 5; ++v)
       if (WACT || v != 3) uout.f[v][o] = un[v];
     if (kind != STAGE_RK_1) {
-      const double inv = inv_dt_hyp64<PLANE, WACT>(un, G);
+      double q[5];
+      const double inv = inv_dt_hyp64<PLANE, WACT>(un, G, q);
       const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
       red = b > red ? b : red;
       if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+      if (hout) {
+        const long long h = (long long)y * G.na + x;
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          if (hout->f[v]) hout->f[v][h] = q[v];
+      }
     }
   }
   if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);

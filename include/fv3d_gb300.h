@@ -132,6 +132,19 @@ int fvgpu_get_cons(fv_sim* sim, double* rho, double* mx, double* my, double* mz,
 int fvgpu_compute_dt(fv_sim* sim, double* dt, double inv[3]);
 /* One UpdateFunctor::update with the given dt (Euler or RK2 per params). */
 int fvgpu_step(fv_sim* sim, double dt);
+/* One update from and to caller arrays of primitives (rho, u, v, w, p;
+ * [Nz][Ny][Nx], no padding) that the GPU addresses directly: pinned host
+ * memory, device memory, or ordinary host memory where the device reads
+ * pageable memory.  Does primToCons of prim_in (the reference's set-up of U,
+ * main.cpp:43-44), takes the CFL dt of that state when dt <= 0
+ * (ComputeDtFunctor::computeDt) or dt otherwise, runs one update and writes
+ * consToPrim of the result to prim_out (NULL entries are skipped); the
+ * kernels read and write the caller's arrays themselves, with no staging
+ * copies.  Returns when prim_out is written; *dt_used (may be NULL)
+ * receives the dt taken.  The result also stays in the handle.  Arrays the
+ * GPU cannot address give FV_ERR_PARAM. */
+int fvgpu_step_host(fv_sim* sim, const double* const prim_in[5], double dt, double* const prim_out[5],
+                    double* dt_used);
 /* The main.cpp:51-74 loop: while (t + epsilon < tend && steps < max_steps)
  * { dt = computeDt(); update(dt); t += dt; }.  *t is read and written; *nsteps
  * (may be NULL) receives the number of steps taken.  max_steps <= 0 means no
