@@ -55,6 +55,26 @@ __device__ __forceinline__ double minmod_exact(double dL, double dR) {
   return fabs(dL) < fabs(dR) ? dL : dR;
 }
 
+// RN(0.5 * x) with integer instructions only.  For |x| >= 2^-1021 the
+// product is exact: x with its exponent decremented (only the high word
+// changes).  Below that the halved value is subnormal: the magnitude in units
+// of 2^-1074 is halved with round-to-nearest-even.  Infinities and NaN are
+// returned unchanged.
+__device__ __forceinline__ double half64(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
+  if (e - 2u < 0x7fdu) return __hiloint2double(hi - 0x100000, __double2loint(x));
+  if (e == 0x7ffu) return x;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long m = b & 0x7fffffffffffffffull;
+  const unsigned long long r = (m >> 1) + (m & (m >> 1) & 1ull);
+  return __longlong_as_double((long long)((b & 0x8000000000000000ull) | r));
+}
+
+// 0.5 * x for either precision (FP32 keeps its multiply: that pipe is fast).
+__device__ __forceinline__ double half_of(double x) { return half64(x); }
+__device__ __forceinline__ float half_of(float x) { return 0.5f * x; }
+
 // Face-state reconstruction q + (slope*sign)*0.5 (Update.h:21): the product
 // with +-0.5 is exact, so a single fused operation rounds identically.
 __device__ __forceinline__ double recon_plus(double q, double slope) { return fma(slope, 0.5, q); }

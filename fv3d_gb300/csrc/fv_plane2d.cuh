@@ -39,7 +39,7 @@ __device__ __forceinline__ void cons_to_prim64(const double u[5], double gm1, do
   } else {
     ke = __dadd_rn(__dmul_rn(va, va), __dmul_rn(vb, vb));
   }
-  const double Ek = __dmul_rn(__dmul_rn(0.5, r), ke);
+  const double Ek = __dmul_rn(half64(r), ke);
   q[0] = r;
   q[1] = va;
   q[2] = vb;

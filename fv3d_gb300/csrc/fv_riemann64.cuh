@@ -7,9 +7,11 @@
 // 2: t2, 0: none); its terms are exact zeros in the reference arithmetic and
 // are dropped.  Cheaper-but-identical steps, each returning the same bits:
 //   - p/(gamma-1) via the corrected quotient with RN(1/(gamma-1));
-//   - the five HLL flux components share one reciprocal of SR-SL;
+//   - the five HLL flux components share one reciprocal of SR-SL, and each
+//     state's sound speed and kinetic energy share one reciprocal of rho;
 //   - HLLC's max(cL, cR) as sqrt(max(cL^2, cR^2)) (sqrt is monotone and
-//     correctly rounded), and u*, p* / the star state share reciprocals.
+//     correctly rounded), and u*, p* / the star state share reciprocals;
+//   - products with 0.5 by exponent arithmetic (half64, exact).
 #pragma once
 
 #include "fv_device.cuh"
@@ -28,7 +30,7 @@ __device__ __forceinline__ double ke_sum3(double un, double t1, double t2) {
 // computeFlux (States.h:114-127) given e = p/(gamma-1).
 template <int ZS>
 __device__ __forceinline__ void euler_flux64(const Slots<double>& q, double e, double F[5]) {
-  const double Ek = 0.5 * q.r * ke_sum3<ZS>(q.un, q.t1, q.t2);
+  const double Ek = half64(q.r) * ke_sum3<ZS>(q.un, q.t1, q.t2);
   const double E = e + Ek;
   F[0] = q.r * q.un;
   F[1] = F[0] * q.un + q.p;
@@ -37,14 +39,14 @@ __device__ __forceinline__ void euler_flux64(const Slots<double>& q, double e, d
   F[4] = (q.p + E) * q.un;
 }
 
-// primToCons (States.h:20-31) given e = p/(gamma-1).
+// primToCons (States.h:20-31) given e = p/(gamma-1) and y = RN(1/rho).
 template <int ZS>
-__device__ __forceinline__ void prim_to_cons64(const Slots<double>& q, double e, double u[5]) {
+__device__ __forceinline__ void prim_to_cons64(const Slots<double>& q, double e, double y, double u[5]) {
   u[0] = q.r;
   u[1] = q.r * q.un;
   u[2] = ZS == 1 ? 0.0 : q.r * q.t1;
   u[3] = ZS == 2 ? 0.0 : q.r * q.t2;
-  const double Ek = 0.5 * ke_sum3<ZS>(u[1], u[2], u[3]) / q.r;
+  const double Ek = div_by_rcp(half64(ke_sum3<ZS>(u[1], u[2], u[3])), q.r, y);
   u[4] = Ek + e;
 }
 
@@ -54,8 +56,11 @@ __device__ __forceinline__ void prim_to_cons64(const Slots<double>& q, double e,
 template <int ZS>
 __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double>& R, const Consts64& K,
                                       double flux[5], double* pout = nullptr) {
-  const double aL = sqrt(L.p * K.gamma / L.r);
-  const double aR = sqrt(R.p * K.gamma / R.r);
+  // one correctly rounded reciprocal of each density serves both quotients by
+  // it (the sound speed's p*gamma/rho and, in the star region, Ek/rho)
+  const double yL = 1.0 / L.r, yR = 1.0 / R.r;
+  const double aL = sqrt(div_by_rcp(L.p * K.gamma, L.r, yL));
+  const double aR = sqrt(div_by_rcp(R.p * K.gamma, R.r, yR));
   const double SL = fmin(L.un - aL, R.un - aR);
   const double SR = fmax(L.un + aL, R.un + aR);
   const double eL = div_by_rcp(L.p, K.gm1, K.inv_gm1);
@@ -72,10 +77,10 @@ __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double
     for (int v = 0; v < 5; ++v) flux[v] = FR[v];
     if (pout) *pout = R.p;
   } else {
-    if (pout) *pout = 0.5 * (L.p + R.p);
+    if (pout) *pout = half64(L.p + R.p);
     double uL[5], uR[5];
-    prim_to_cons64<ZS>(L, eL, uL);
-    prim_to_cons64<ZS>(R, eR, uR);
+    prim_to_cons64<ZS>(L, eL, yL, uL);
+    prim_to_cons64<ZS>(R, eR, yR, uR);
     const double slsr = SL * SR;
     const double den = SR - SL;
     const double y = 1.0 / den;
@@ -100,8 +105,8 @@ __device__ __forceinline__ void hllc64(const Slots<double>& L, const Slots<doubl
   const double rR = R.r, uR = R.un, pR = R.p;
   const double kL = ZS == 1 ? uL * uL : uL * uL + L.t1 * L.t1;
   const double kR = ZS == 1 ? uR * uR : uR * uR + R.t1 * R.t1;
-  const double EL = 0.5 * rL * kL + pL * K.inv_gm1;
-  const double ER = 0.5 * rR * kR + pR * K.inv_gm1;
+  const double EL = half64(rL) * kL + pL * K.inv_gm1;
+  const double ER = half64(rR) * kR + pR * K.inv_gm1;
   const double c2L = pL * K.gamma / rL;
   const double c2R = pR * K.gamma / rR;
   const double cmax = sqrt(fmax(c2L, c2R));

@@ -198,8 +198,8 @@ __device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, c
     }
   }
   if (DIR == 2 && recon == R_PCM_WB) {  // Update.h:27
-    qL[4] = qL[4] + 1.0 * qL[0] * G.g * G.dz * 0.5;
-    qR[4] = qR[4] + -1.0 * qR[0] * G.g * G.dz * 0.5;
+    qL[4] = qL[4] + half64(1.0 * qL[0] * G.g * G.dz);
+    qR[4] = qR[4] + half64(-1.0 * qR[0] * G.g * G.dz);
   }
   const Slots<double> L = slots3<DIR>(qL), R = slots3<DIR>(qR);
   double f[5];
@@ -215,11 +215,11 @@ __device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, c
 // velocity var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x),
 // i.e. stencil[dk][dj][di][var].
 template <class PA>
-__device__ __forceinline__ void viscous3d(const PA& P, double dx, double dy, double dz, double mu, double vf[3][5]) {
+__device__ __forceinline__ void viscous3d(const PA& P, double odx, double ody, double odz, double mu,
+                                          double vf[3][5]) {
   const double four_thirds = 4.0 / 3.0;
   const double two_thirds = 2.0 / 3.0;
-  const double odx = 1.0 / dx, ody = 1.0 / dy, odz = 1.0 / dz;
-  const double c4x = 0.25 * odx, c4y = 0.25 * ody, c4z = 0.25 * odz;
+  const double c4x = half64(half64(odx)), c4y = half64(half64(ody)), c4z = half64(half64(odz));
   const int U = 1, V = 2, W = 3;
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -228,9 +228,9 @@ __device__ __forceinline__ void viscous3d(const PA& P, double dx, double dy, dou
 #pragma unroll
   for (int s = 1; s < 3; ++s) {  // IX
     const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = 0.5 * (P(1, 1, s, U) + P(1, 1, s - 1, U));
-    const double qiv = 0.5 * (P(1, 1, s, V) + P(1, 1, s - 1, V));
-    const double qiw = 0.5 * (P(1, 1, s, W) + P(1, 1, s - 1, W));
+    const double qiu = half64(P(1, 1, s, U) + P(1, 1, s - 1, U));
+    const double qiv = half64(P(1, 1, s, V) + P(1, 1, s - 1, V));
+    const double qiw = half64(P(1, 1, s, W) + P(1, 1, s - 1, W));
     const double dudx = odx * (P(1, 1, s, U) - P(1, 1, s - 1, U));
     const double dvdx = odx * (P(1, 1, s, V) - P(1, 1, s - 1, V));
     const double dwdx = odx * (P(1, 1, s, W) - P(1, 1, s - 1, W));
@@ -249,9 +249,9 @@ __device__ __forceinline__ void viscous3d(const PA& P, double dx, double dy, dou
 #pragma unroll
   for (int s = 1; s < 3; ++s) {  // IY
     const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = 0.5 * (P(1, s, 1, U) + P(1, s - 1, 1, U));
-    const double qiv = 0.5 * (P(1, s, 1, V) + P(1, s - 1, 1, V));
-    const double qiw = 0.5 * (P(1, s, 1, W) + P(1, s - 1, 1, W));
+    const double qiu = half64(P(1, s, 1, U) + P(1, s - 1, 1, U));
+    const double qiv = half64(P(1, s, 1, V) + P(1, s - 1, 1, V));
+    const double qiw = half64(P(1, s, 1, W) + P(1, s - 1, 1, W));
     const double dudy = ody * (P(1, s, 1, U) - P(1, s - 1, 1, U));
     const double dvdy = ody * (P(1, s, 1, V) - P(1, s - 1, 1, V));
     const double dwdy = ody * (P(1, s, 1, W) - P(1, s - 1, 1, W));
@@ -270,9 +270,9 @@ __device__ __forceinline__ void viscous3d(const PA& P, double dx, double dy, dou
 #pragma unroll
   for (int s = 1; s < 3; ++s) {  // IZ, with the reference's mix-ups
     const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = 0.5 * (P(s, 1, 1, U) + P(s - 1, 1, 1, U));
-    const double qiv = 0.5 * (P(s, 1, 1, V) + P(s - 1, 1, 1, V));
-    const double qiw = 0.5 * (P(s, 1, 1, W) + P(s - 1, 1, 1, W));
+    const double qiu = half64(P(s, 1, 1, U) + P(s - 1, 1, 1, U));
+    const double qiv = half64(P(s, 1, 1, V) + P(s - 1, 1, 1, V));
+    const double qiw = half64(P(s, 1, 1, W) + P(s - 1, 1, 1, W));
     const double dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
     const double dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
     const double dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
@@ -430,7 +430,7 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
       for (int v = 0; v < 5; ++v) un[v] = un[v] + div_cell((fL[v] - fR[v]) * dt, G.dz, G.inv_dz, G.pow2_z);
       if (G.gravity) {
         un[3] = un[3] + dt * rho_c * G.g;
-        un[4] = un[4] + dt * 0.5 * (fL[0] + fR[0]) * G.g;
+        un[4] = un[4] + half64(dt) * (fL[0] + fR[0]) * G.g;
       }
       un[0] = fmax(1.0e-6, un[0]);
 
@@ -441,7 +441,7 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
           kF = G.kappa_z[3 * k + 1];
           kB = G.kappa_z[3 * k + 2];
         } else {
-          kC = kF = kB = 0.5 * (G.kappa + G.kappa);
+          kC = kF = kB = half64(G.kappa + G.kappa);
         }
         const int hy = cy + 2, hx = cx + 2;
         const double TC = S.temp(sk, hy, hx);
@@ -467,13 +467,13 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
       if (G.visc) {  // Viscosity.h:145-151
         const RingVel P{S, k, cy + 2, cx + 2};
         double vf[3][5];
-        viscous3d(P, G.dx, G.dy, G.dz, G.mu, vf);
+        viscous3d(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
 #pragma unroll
         for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
       }
       if (KIND == STAGE_RK_2) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) un[v] = 0.5 * (u0.f[v][o] + un[v]);
+        for (int v = 0; v < 5; ++v) un[v] = half64(u0.f[v][o] + un[v]);
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) uout.f[v][o] = un[v];

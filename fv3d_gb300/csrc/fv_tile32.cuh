@@ -363,7 +363,7 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     if (WACT && G.visc) {
       PlaneVel<PLANE, TileSmem<float, NV, TL>> P{S, cy + 2, cx + 2};
       float vf[3][5];
-      viscous_plane<PLANE, float>(P, G.dx_f, G.dy_f, G.dz_f, G.mu_f, vf);
+      viscous_plane<PLANE, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);

@@ -83,12 +83,13 @@ struct TileSmem {
 // same values (at most the sign of an exact zero differs).  P(r, c, var) reads
 // velocity var (1 u, 2 v, 3 w) of the cell at offset (r-1, c-1) along (b, a).
 // vf receives the per-direction fluxes of components u, v, w, E (index 1..4).
+// odx, ody, odz are the reference's one_over_d = RN(1/d) (Viscosity.h:44-46),
+// computed once on the host.
 template <int PLANE, class T, class PA>
-__device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T mu, T vf[3][5]) {
+__device__ __forceinline__ void viscous_plane(const PA& P, T odx, T ody, T odz, T mu, T vf[3][5]) {
   const T four_thirds = T(4.0 / 3.0);
   const T two_thirds = T(2.0 / 3.0);
-  const T odx = T(1) / dx, ody = T(1) / dy, odz = T(1) / dz;
-  const T c4x = T(0.25) * odx, c4y = T(0.25) * ody, c4z = T(0.25) * odz;
+  const T c4x = half_of(half_of(odx)), c4y = half_of(half_of(ody)), c4z = half_of(half_of(odz));
   const int U = 1, V = 2, W = 3;
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -98,9 +99,9 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T m
 #pragma unroll
     for (int s = 1; s < 3; ++s) {  // IX (Viscosity.h:163-186), z-derivatives vanish
       const T sign = s == 1 ? T(-1) : T(1);
-      const T qiu = (P(1, s, U) + P(1, s - 1, U)) * T(0.5);
-      const T qiv = (P(1, s, V) + P(1, s - 1, V)) * T(0.5);
-      const T qiw = (P(1, s, W) + P(1, s - 1, W)) * T(0.5);
+      const T qiu = half_of(P(1, s, U) + P(1, s - 1, U));
+      const T qiv = half_of(P(1, s, V) + P(1, s - 1, V));
+      const T qiw = half_of(P(1, s, W) + P(1, s - 1, W));
       const T dudx = odx * (P(1, s, U) - P(1, s - 1, U));
       const T dvdx = odx * (P(1, s, V) - P(1, s - 1, V));
       const T dwdx = odx * (P(1, s, W) - P(1, s - 1, W));
@@ -117,9 +118,9 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T m
 #pragma unroll
     for (int s = 1; s < 3; ++s) {  // IY (Viscosity.h:188-213), z-derivatives vanish
       const T sign = s == 1 ? T(-1) : T(1);
-      const T qiu = (P(s, 1, U) + P(s - 1, 1, U)) * T(0.5);
-      const T qiv = (P(s, 1, V) + P(s - 1, 1, V)) * T(0.5);
-      const T qiw = (P(s, 1, W) + P(s - 1, 1, W)) * T(0.5);
+      const T qiu = half_of(P(s, 1, U) + P(s - 1, 1, U));
+      const T qiv = half_of(P(s, 1, V) + P(s - 1, 1, V));
+      const T qiw = half_of(P(s, 1, W) + P(s - 1, 1, W));
       const T dudy = ody * (P(s, 1, U) - P(s - 1, 1, U));
       const T dvdy = ody * (P(s, 1, V) - P(s - 1, 1, V));
       const T dwdy = ody * (P(s, 1, W) - P(s - 1, 1, W));
@@ -155,9 +156,9 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T m
 #pragma unroll
     for (int s = 1; s < 3; ++s) {  // IX, y-derivatives vanish
       const T sign = s == 1 ? T(-1) : T(1);
-      const T qiu = (P(1, s, U) + P(1, s - 1, U)) * T(0.5);
-      const T qiv = (P(1, s, V) + P(1, s - 1, V)) * T(0.5);
-      const T qiw = (P(1, s, W) + P(1, s - 1, W)) * T(0.5);
+      const T qiu = half_of(P(1, s, U) + P(1, s - 1, U));
+      const T qiv = half_of(P(1, s, V) + P(1, s - 1, V));
+      const T qiw = half_of(P(1, s, W) + P(1, s - 1, W));
       const T dudx = odx * (P(1, s, U) - P(1, s - 1, U));
       const T dvdx = odx * (P(1, s, V) - P(1, s - 1, V));
       const T dwdx = odx * (P(1, s, W) - P(1, s - 1, W));
@@ -175,9 +176,9 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T dx, T dy, T dz, T m
 #pragma unroll
     for (int s = 1; s < 3; ++s) {  // IZ, with the reference's index/field mix-ups
       const T sign = s == 1 ? T(-1) : T(1);
-      const T qiu = (P(s, 1, U) + P(s - 1, 1, U)) * T(0.5);
-      const T qiv = (P(s, 1, V) + P(s - 1, 1, V)) * T(0.5);
-      const T qiw = (P(s, 1, W) + P(s - 1, 1, W)) * T(0.5);
+      const T qiu = half_of(P(s, 1, U) + P(s - 1, 1, U));
+      const T qiv = half_of(P(s, 1, V) + P(s - 1, 1, V));
+      const T qiw = half_of(P(s, 1, W) + P(s - 1, 1, W));
       const T dudz = odz * (P(s, 1, U) - P(s - 1, 1, U));
       const T dvdz = odz * (P(s, 1, V) - P(s - 1, 1, V));
       const T dwdz = odz * (P(s, 1, W) - P(s - 1, 1, W));
@@ -267,8 +268,8 @@ __device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool p
     }
   }
   if (DIR == 1 && wb_z) {  // PCM_WB hydrostatic pressure in z (Update.h:27)
-    qL[4] = qL[4] + 1.0 * qL[0] * G.g * G.dz * 0.5;
-    qR[4] = qR[4] + -1.0 * qR[0] * G.g * G.dz * 0.5;
+    qL[4] = qL[4] + half64(1.0 * qL[0] * G.g * G.dz);
+    qR[4] = qR[4] + half64(-1.0 * qR[0] * G.g * G.dz);
   }
   const Slots<double> L = to_slots<PLANE, DIR>(qL), R = to_slots<PLANE, DIR>(qR);
   double f[5];
@@ -400,12 +401,12 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
         un[v] = un[v] + div_cell((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, db, inv_db, pow2_b);
     if (PLANE == PLANE_XZ && G.gravity) {
       un[2] = un[2] + dt * S.q(0, cy + 2, cx + 2) * G.g;
-      un[4] = un[4] + dt * 0.5 * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g;
+      un[4] = un[4] + half64(dt) * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g;
     }
     un[0] = fmax(1.0e-6, un[0]);
 
     if (G.tc) {  // ThermalConduction.h:47-95, constant kappa, 2-D
-      const double kf = 0.5 * (G.kappa + G.kappa);
+      const double kf = half64(G.kappa + G.kappa);
       const int hy = cy + 2, hx = cx + 2;
       const double TC = S.temp(hy, hx);
       const double FL = div_cell(kf * (TC - S.temp(hy, hx - 1)), G.dx, G.inv_dx, G.pow2_x);
@@ -419,7 +420,7 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
     if (WACT && G.visc) {  // Viscosity.h:245-251
       PlaneVel<PLANE, TileSmem<double, NV, TL>> P{S, cy + 2, cx + 2};
       double vf[3][5];
-      viscous_plane<PLANE, double>(P, G.dx, G.dy, G.dz, G.mu, vf);
+      viscous_plane<PLANE, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
@@ -429,7 +430,7 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
     if (kind == STAGE_RK_2) {
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) un[v] = 0.5 * (u0.f[v][o] + un[v]);
+        if (WACT || v != 3) un[v] = half64(u0.f[v][o] + un[v]);
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v)
