@@ -44,13 +44,13 @@ WORKLOAD = "rayleigh_taylor_512x1536_fp64"
 ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2-D)
 # dram__bytes_read.sum + dram__bytes_write.sum of the two stage launches of one
 # RK2 step of this workload, from one ncu --set full capture
-# (profiles/stage2d_fp64_rt512x1536.md: 25.29+0.09 MB and 50.40+0.12 MB).
-NCU_TRAFFIC_BYTES_PER_STEP = 75.90e6
-# FP64-pipe lane operations per cell-update of this workload (stage 1: 450,
-# stage 2: 507; (fused + non-fused FP64 warp instructions) x 32 / cells from
-# the same capture).  The FP64 kernel is bound by the FP64 pipe: its roofline
-# against the FP64 rate measured live by fvgpu_probe_fp64_rate.
-FP64_OPS_PER_CELL_UPDATE = 957
+# (profiles/stage2d_fp64_rt512x1536.md: 25.23+0.07 MB and 50.40+0.10 MB).
+NCU_TRAFFIC_BYTES_PER_STEP = 75.80e6
+# FP64 arithmetic lane operations (DADD + DMUL + DFMA thread instructions)
+# per cell-update of this workload from the same capture (stage 1: 395.9,
+# stage 2: 436.4).  The FP64 kernel is bound by the FP64 pipe: its roofline
+# against the FP64 FMA rate measured live by fvgpu_probe_fp64_rate.
+FP64_OPS_PER_CELL_UPDATE = 832
 
 
 def peaks():

@@ -146,6 +146,7 @@ void SetExactConstants(Grid& G) {
   G.pow2_x = PowerOfTwo(G.dx);
   G.pow2_y = PowerOfTwo(G.dy);
   G.pow2_z = PowerOfTwo(G.dz);
+  G.pow2_all = G.pow2_x && G.pow2_y && G.pow2_z;
   G.gm1 = G.gamma - 1.0;
   G.inv_gm1 = 1.0 / G.gm1;
   G.gamma_f = (float)G.gamma;

@@ -58,7 +58,10 @@ batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
     } else {
       uin = flip ? I.B : I.A; u0 = uin; uout = flip ? I.A : I.B;
     }
-    stage_tile64<PLANE, WACT, TL>(I.G, uin, u0, uout, I.ctrl, I.rs, kind, bx, by, smem_raw, s_red);
+    if (I.G.pow2_all)
+      stage_tile64<PLANE, WACT, TL, true>(I.G, uin, u0, uout, I.ctrl, I.rs, kind, bx, by, smem_raw, s_red);
+    else
+      stage_tile64<PLANE, WACT, TL, false>(I.G, uin, u0, uout, I.ctrl, I.rs, kind, bx, by, smem_raw, s_red);
   }
 }
 

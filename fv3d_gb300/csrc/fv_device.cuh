@@ -59,6 +59,7 @@ struct Grid {
   // Exact-arithmetic helpers (host-computed with IEEE double):
   double inv_dx, inv_dy, inv_dz;   // RN(1/d)
   int pow2_x, pow2_y, pow2_z;      // d is a power of two (1/d exact)
+  int pow2_all;                    // all three are
   double gm1, inv_gm1;             // gamma - 1, RN(1/(gamma - 1))
   // FP32 copies for the mixed form (a double->float conversion runs on the
   // slow FP64 pipe, so kernels never convert per cell).

@@ -30,9 +30,20 @@ __device__ __forceinline__ double div_by_rcp(double a, double b, double y) {
 
 // (x) / d for a cell size d: an exact multiplication by 1/d when d is a power
 // of two (then 1/d is exact and scaling by it rounds nowhere), else the
-// corrected quotient above.
-__device__ __forceinline__ double div_cell(double x, double d, double inv_d, bool pow2) {
-  return pow2 ? __dmul_rn(x, inv_d) : div_by_rcp(x, d, inv_d);
+// corrected quotient above (exact for any d).  P2 is a compile-time choice:
+// the kernels branch once, uniformly, on "every cell size is a power of two",
+// because a per-call select would issue both forms.
+template <bool P2>
+__device__ __forceinline__ double div_cell(double x, double d, double inv_d) {
+  return P2 ? __dmul_rn(x, inv_d) : div_by_rcp(x, d, inv_d);
+}
+
+// The reference formula of minmod, out of line: the rare operands that reach
+// it (NaN, infinities, a product that may underflow) take a real branch, so
+// its FP64 instructions are not issued on the common path.
+static __device__ __noinline__ double minmod_rare(double dL, double dR) {
+  if (dL * dR < 0.0) return 0.0;
+  return fabs(dL) < fabs(dR) ? dL : dR;
 }
 
 // minmod of Update.h:73-80 -- 0 if dL*dR < 0, else the argument of smaller
@@ -51,8 +62,7 @@ __device__ __forceinline__ double minmod_exact(double dL, double dR) {
     const unsigned ea = (unsigned)(ma >> 52), eb = (unsigned)(mb >> 52);
     if (ea != 0u && eb != 0u && ea + eb >= 972u) return 0.0;  // |dL*dR| >= 2^-1074
   }
-  if (dL * dR < 0.0) return 0.0;
-  return fabs(dL) < fabs(dR) ? dL : dR;
+  return minmod_rare(dL, dR);
 }
 
 // RN(0.5 * x) with integer instructions only.  For |x| >= 2^-1021 the

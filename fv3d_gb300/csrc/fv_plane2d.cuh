@@ -50,7 +50,7 @@ __device__ __forceinline__ void cons_to_prim64(const double u[5], double gm1, do
 // Hyperbolic inverse time step of one cell, ComputeDt.h:49-52:
 // (cs + |u|)/dx + (cs + |v|)/dy + (cs + |w|)/dz with cs = sqrt(p*gamma/rho).
 // qout, when given, receives the primitives consToPrim computes on the way.
-template <int PLANE, bool WACT>
+template <int PLANE, bool WACT, bool P2 = false>
 __device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid& G, double* qout = nullptr) {
   double q[5], y;
   cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
@@ -60,9 +60,9 @@ __device__ __forceinline__ double inv_dt_hyp64(const double u[5], const Grid& G,
   }
   const double cs = sqrt(div_by_rcp(__dmul_rn(q[4], G.gamma), q[0], y));
   const double vx = q[1], vy = PLANE == PLANE_XY ? q[2] : q[3], vz = PLANE == PLANE_XY ? q[3] : q[2];
-  const double tx = div_cell(__dadd_rn(cs, fabs(vx)), G.dx, G.inv_dx, G.pow2_x);
-  const double ty = div_cell(__dadd_rn(cs, fabs(vy)), G.dy, G.inv_dy, G.pow2_y);
-  const double tz = div_cell(__dadd_rn(cs, fabs(vz)), G.dz, G.inv_dz, G.pow2_z);
+  const double tx = div_cell<P2>(__dadd_rn(cs, fabs(vx)), G.dx, G.inv_dx);
+  const double ty = div_cell<P2>(__dadd_rn(cs, fabs(vy)), G.dy, G.inv_dy);
+  const double tz = div_cell<P2>(__dadd_rn(cs, fabs(vz)), G.dz, G.inv_dz);
   return __dadd_rn(__dadd_rn(tx, ty), tz);
 }
 

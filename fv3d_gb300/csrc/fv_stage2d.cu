@@ -15,8 +15,13 @@ stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
              const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
-  stage_tile64<PLANE, WACT, SingleTile>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw, s_red,
-                                        hout.f[0] ? &hout : nullptr);
+  const Fields* ho = hout.f[0] ? &hout : nullptr;
+  if (G.pow2_all)
+    stage_tile64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw,
+                                                s_red, ho);
+  else
+    stage_tile64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw,
+                                                 s_red, ho);
 }
 
 template <int PLANE, int RS, int KIND, bool WACT>

@@ -299,12 +299,12 @@ struct RingVel {
   }
 };
 
-template <int RS, int KIND>
-__global__ void __launch_bounds__(kThreads, 2)
-stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             int tz, const Fields hout) {
-  extern __shared__ double smem_raw[];
-  __shared__ unsigned long long s_red[kThreads / 32];
+// One stage for the CTA's columns and z chunk; P2: every cell size is a
+// power of two (the kernel branches on it once, uniformly).
+template <int RS, int KIND, bool P2>
+__device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                             StepCtrl* __restrict__ ctrl, int tz, const Fields& hout,
+                                             double* smem_raw, unsigned long long* s_red) {
   const Smem3 S{smem_raw};
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
@@ -397,10 +397,10 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
       // IX, IY: un += (F(-1/2) - F(+1/2)) * dt / d
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        un[v] = un[v] + div_cell((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx, G.pow2_x);
+        un[v] = un[v] + div_cell<P2>((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        un[v] = un[v] + div_cell((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, G.dy, G.inv_dy, G.pow2_y);
+        un[v] = un[v] + div_cell<P2>((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, G.dy, G.inv_dy);
       // IZ with the z-boundary overrides of Update.h:131-143
       double fL[5], fR[5];
 #pragma unroll
@@ -427,7 +427,7 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
         }
       }
 #pragma unroll
-      for (int v = 0; v < 5; ++v) un[v] = un[v] + div_cell((fL[v] - fR[v]) * dt, G.dz, G.inv_dz, G.pow2_z);
+      for (int v = 0; v < 5; ++v) un[v] = un[v] + div_cell<P2>((fL[v] - fR[v]) * dt, G.dz, G.inv_dz);
       if (G.gravity) {
         un[3] = un[3] + dt * rho_c * G.g;
         un[4] = un[4] + half64(dt) * (fL[0] + fR[0]) * G.g;
@@ -445,23 +445,23 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
         }
         const int hy = cy + 2, hx = cx + 2;
         const double TC = S.temp(sk, hy, hx);
-        const double FL = div_cell(kC * (TC - S.temp(sk, hy, hx - 1)), G.dx, G.inv_dx, G.pow2_x);
-        const double FR = div_cell(kC * (S.temp(sk, hy, hx + 1) - TC), G.dx, G.inv_dx, G.pow2_x);
-        const double FU = div_cell(kC * (TC - S.temp(sk, hy - 1, hx)), G.dy, G.inv_dy, G.pow2_y);
-        const double FD = div_cell(kC * (S.temp(sk, hy + 1, hx) - TC), G.dy, G.inv_dy, G.pow2_y);
-        double FF = div_cell(kF * (TC - S.temp(slot_of(k - 1), hy, hx)), G.dz, G.inv_dz, G.pow2_z);
-        double FB = div_cell(kB * (S.temp(slot_of(k + 1), hy, hx) - TC), G.dz, G.inv_dz, G.pow2_z);
+        const double FL = div_cell<P2>(kC * (TC - S.temp(sk, hy, hx - 1)), G.dx, G.inv_dx);
+        const double FR = div_cell<P2>(kC * (S.temp(sk, hy, hx + 1) - TC), G.dx, G.inv_dx);
+        const double FU = div_cell<P2>(kC * (TC - S.temp(sk, hy - 1, hx)), G.dy, G.inv_dy);
+        const double FD = div_cell<P2>(kC * (S.temp(sk, hy + 1, hx) - TC), G.dy, G.inv_dy);
+        double FF = div_cell<P2>(kF * (TC - S.temp(slot_of(k - 1), hy, hx)), G.dz, G.inv_dz);
+        double FB = div_cell<P2>(kB * (S.temp(slot_of(k + 1), hy, hx) - TC), G.dz, G.inv_dz);
         if (k == 0 && G.bctc_zmin != 0) {
-          if (G.bctc_zmin == 1) FF = div_cell(kF * 2.0 * (TC - G.bctc_zmin_value), G.dz, G.inv_dz, G.pow2_z);
+          if (G.bctc_zmin == 1) FF = div_cell<P2>(kF * 2.0 * (TC - G.bctc_zmin_value), G.dz, G.inv_dz);
           else FF = kF * G.bctc_zmin_value;
         }
         if (k == G.nc - 1 && G.bctc_zmax != 0) {
-          if (G.bctc_zmax == 1) FB = div_cell(kB * 2.0 * (G.bctc_zmax_value - TC), G.dz, G.inv_dz, G.pow2_z);
+          if (G.bctc_zmax == 1) FB = div_cell<P2>(kB * 2.0 * (G.bctc_zmax_value - TC), G.dz, G.inv_dz);
           else FB = kB * G.bctc_zmax_value;
         }
-        const double dtdx = div_cell(dt, G.dx, G.inv_dx, G.pow2_x);
-        const double dtdy = div_cell(dt, G.dy, G.inv_dy, G.pow2_y);
-        const double dtdz = div_cell(dt, G.dz, G.inv_dz, G.pow2_z);
+        const double dtdx = div_cell<P2>(dt, G.dx, G.inv_dx);
+        const double dtdy = div_cell<P2>(dt, G.dy, G.inv_dy);
+        const double dtdz = div_cell<P2>(dt, G.dz, G.inv_dz);
         un[4] = un[4] + (dtdx * (FR - FL) + dtdy * (FD - FU) + dtdz * (FB - FF));
       }
       if (G.visc) {  // Viscosity.h:145-151
@@ -479,7 +479,7 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
       for (int v = 0; v < 5; ++v) uout.f[v][o] = un[v];
       if (KIND != STAGE_RK_1) {
         double q[5];
-        const double inv = inv_dt_hyp64<PLANE_XY, true>(un, G, q);
+        const double inv = inv_dt_hyp64<PLANE_XY, true, P2>(un, G, q);
         const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
         red = b > red ? b : red;
         if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
@@ -497,6 +497,18 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
     __syncthreads();
   }
   if (KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+template <int RS, int KIND>
+__global__ void __launch_bounds__(kThreads, 2)
+stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
+             int tz, const Fields hout) {
+  extern __shared__ double smem_raw[];
+  __shared__ unsigned long long s_red[kThreads / 32];
+  if (G.pow2_all)
+    stage3d_body<RS, KIND, true>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
+  else
+    stage3d_body<RS, KIND, false>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
 }
 
 template <int RS, int KIND>

@@ -288,7 +288,9 @@ __device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool p
 // storage order with rows of G.na values and no padding (a caller's host
 // arrays the GPU can address); the stage writes consToPrim of its result
 // there, the values the CFL term computes anyway.
-template <int PLANE, bool WACT, class TL>
+// P2: every cell size is a power of two (G.pow2_all); callers branch on it
+// once, uniformly, and instantiate both forms.
+template <int PLANE, bool WACT, class TL, bool P2>
 __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                              StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
                                              unsigned long long* s_red, const Fields* hout = nullptr) {
@@ -377,7 +379,6 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
   // ---- 3-5. conservative update, sources, RK2 combination, CFL term ----
   const double db = PLANE == PLANE_XY ? G.dy : G.dz;
   const double inv_db = PLANE == PLANE_XY ? G.inv_dy : G.inv_dz;
-  const bool pow2_b = PLANE == PLANE_XY ? G.pow2_y : G.pow2_z;
   unsigned long long red = 0ull;
 #pragma unroll 1
   for (int cidx = tid; cidx < TL::CELLS; cidx += kTileThreads) {
@@ -393,12 +394,12 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
 #pragma unroll
     for (int v = 0; v < 5; ++v)
       if (WACT || v != 3)
-        un[v] = un[v] + div_cell((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx, G.pow2_x);
+        un[v] = un[v] + div_cell<P2>((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx);
     // IY sweep (x-y plane) or IZ sweep (x-z plane), gravity on IZ
 #pragma unroll
     for (int v = 0; v < 5; ++v)
       if (WACT || v != 3)
-        un[v] = un[v] + div_cell((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, db, inv_db, pow2_b);
+        un[v] = un[v] + div_cell<P2>((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, db, inv_db);
     if (PLANE == PLANE_XZ && G.gravity) {
       un[2] = un[2] + dt * S.q(0, cy + 2, cx + 2) * G.g;
       un[4] = un[4] + half64(dt) * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g;
@@ -409,12 +410,12 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
       const double kf = half64(G.kappa + G.kappa);
       const int hy = cy + 2, hx = cx + 2;
       const double TC = S.temp(hy, hx);
-      const double FL = div_cell(kf * (TC - S.temp(hy, hx - 1)), G.dx, G.inv_dx, G.pow2_x);
-      const double FR = div_cell(kf * (S.temp(hy, hx + 1) - TC), G.dx, G.inv_dx, G.pow2_x);
-      const double FU = div_cell(kf * (TC - S.temp(hy - 1, hx)), db, inv_db, pow2_b);
-      const double FD = div_cell(kf * (S.temp(hy + 1, hx) - TC), db, inv_db, pow2_b);
-      const double dtdx = div_cell(dt, G.dx, G.inv_dx, G.pow2_x);
-      const double dtdb = div_cell(dt, db, inv_db, pow2_b);
+      const double FL = div_cell<P2>(kf * (TC - S.temp(hy, hx - 1)), G.dx, G.inv_dx);
+      const double FR = div_cell<P2>(kf * (S.temp(hy, hx + 1) - TC), G.dx, G.inv_dx);
+      const double FU = div_cell<P2>(kf * (TC - S.temp(hy - 1, hx)), db, inv_db);
+      const double FD = div_cell<P2>(kf * (S.temp(hy + 1, hx) - TC), db, inv_db);
+      const double dtdx = div_cell<P2>(dt, G.dx, G.inv_dx);
+      const double dtdb = div_cell<P2>(dt, db, inv_db);
       un[4] = un[4] + (dtdx * (FR - FL) + dtdb * (FD - FU));
     }
     if (WACT && G.visc) {  // Viscosity.h:245-251
@@ -437,7 +438,7 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
       if (WACT || v != 3) uout.f[v][o] = un[v];
     if (kind != STAGE_RK_1) {
       double q[5];
-      const double inv = inv_dt_hyp64<PLANE, WACT>(un, G, q);
+      const double inv = inv_dt_hyp64<PLANE, WACT, P2>(un, G, q);
       const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
       red = b > red ? b : red;
       if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
