@@ -2,19 +2,26 @@
 // main.cpp (main.cpp:12-89) on the GB300 path.
 //
 //   fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]
+//                     [--write-ic state.bin]
 //
 // Reads the same .ini file (readInifile semantics), sets the initial state,
 // and runs the reference's time loop: while (t + epsilon < tend) { dt =
 // computeDt; log every log_frequency steps; save when due; update; t += dt }.
-// The problem generators of Init.h that need no random numbers are provided
-// (sod_x, sod_y, sod_z, blast, diffusion, rayleigh-taylor); any other initial
-// state is read with --ic from a raw file of 5 float64 arrays (rho, u, v, w,
-// p), each Nz*Ny*Nx in C order.  Snapshots are written as the same raw
-// format (<prefix>_<ite>.bin) instead of HDF5.
+// Every problem generator of Init.h is provided (sod_x, sod_y, sod_z, blast,
+// diffusion, rayleigh-taylor, H84, C91).  H84 and C91 draw their
+// perturbations from Kokkos' XorShift64 pool in the reference, whose
+// sequence depends on the thread schedule; here each cell draws from a
+// counter-based splitmix64 stream of [misc] seed instead (the same stream as
+// fv3d_gb300.problems.uniform), so the runs are reproducible but not
+// bit-identical to a reference run.  Any other initial state is read with --ic
+// from a raw file of 5 float64 arrays (rho, u, v, w, p), each Nz*Ny*Nx in C
+// order; --write-ic writes the generated state in that format.  Snapshots
+// are written as the same raw format (<prefix>_<ite>.bin) instead of HDF5.
 //
 // --device-loop runs the steps between two saves with fvgpu_advance (dt stays
 // on the GPU) instead of one compute_dt/step round trip per step.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -33,7 +40,23 @@ double PosX(const fv_params& p, int i) { return p.xmin + (i + 0.5) * p.dx; }
 double PosY(const fv_params& p, int j) { return p.ymin + (j + 0.5) * p.dy; }
 double PosZ(const fv_params& p, int k) { return p.zmin + (k + 0.5) * p.dz; }
 
-// Init.h:18-99, 150-209 on the interior cells.
+uint64_t Mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Uniform [0, 1) number `c` of stream `stream` of `seed` (counter-based
+// splitmix64, top 53 bits).
+double Uniform(uint64_t seed, uint64_t stream, uint64_t c) {
+  const uint64_t golden = 0x9E3779B97F4A7C15ull;
+  const uint64_t key = Mix64(seed + golden * (stream + 1));
+  return (double)(Mix64(key + golden * (c + 1)) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+constexpr uint64_t kStreamH84 = 31, kStreamC91 = 32;
+
+// Init.h:18-209 on the interior cells.
 bool Generate(const fv_params& p, Fields& q) {
   const std::string prob = p.problem;
   const size_t n = (size_t)p.Nx * p.Ny * p.Nz;
@@ -68,6 +91,16 @@ bool Generate(const fv_params& p, Fields& q) {
           if (z > -1.0 / 3.0 && z < 1.0 / 3.0)
             w = 0.01 * (1.0 + std::cos(4 * M_PI * x)) * (1.0 + std::cos(4.0 * M_PI * y)) *
                 (1 + std::cos(3.0 * M_PI * z)) / 4.0;
+        } else if (prob == "H84") {  // Init.h:104-121
+          r = std::pow(z, p.m1);
+          pr = std::pow(z, p.m1 + 1.0);
+          w = p.h84_pert * (Uniform((uint64_t)p.seed, kStreamH84, c) - 0.5);
+        } else if (prob == "C91") {  // Init.h:127-148
+          const double T = 1.0 + p.theta1 * z;
+          r = std::pow(T, p.m1);
+          pr = std::pow(T, p.m1 + 1.0);
+          const double pert = p.c91_pert * (Uniform((uint64_t)p.seed, kStreamC91, c) - 0.5);
+          pr = pr * (1.0 + pert);
         } else {
           return false;
         }
@@ -110,15 +143,17 @@ int Check(fv_sim* s, int rc, const char* what) {
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    std::fprintf(stderr, "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]\n");
+    std::fprintf(stderr,
+                 "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop] [--write-ic state.bin]\n");
     return 2;
   }
-  std::string ini = argv[1], ic, out;
+  std::string ini = argv[1], ic, out, write_ic;
   bool device_loop = false;
   for (int a = 2; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--ic") && a + 1 < argc) ic = argv[++a];
     else if (!std::strcmp(argv[a], "--out") && a + 1 < argc) out = argv[++a];
     else if (!std::strcmp(argv[a], "--device-loop")) device_loop = true;
+    else if (!std::strcmp(argv[a], "--write-ic") && a + 1 < argc) write_ic = argv[++a];
     else {
       std::fprintf(stderr, "unknown argument %s\n", argv[a]);
       return 2;
@@ -136,6 +171,10 @@ int main(int argc, char** argv) {
     }
   } else if (!Generate(p, q)) {
     std::fprintf(stderr, "Error unknown problem %s (give --ic)\n", p.problem);
+    return 1;
+  }
+  if (!write_ic.empty() && !WriteRaw(write_ic, q)) {
+    std::fprintf(stderr, "cannot write %s\n", write_ic.c_str());
     return 1;
   }
   fv_sim* s = nullptr;

@@ -21,6 +21,7 @@ only, Update.h:148):
   batch_sod_sedov  512 instances, sides in {64..256}, Sod tubes and blasts
   batch_rt         64 Rayleigh-Taylor instances, 256x768 ... 1024x3072
   blast            the reference's 3-D blast (settings/blast.ini), n^3, PCM
+  stratified       the reference's H84 / C91 polytropes from an .ini
   random_problem   seeded random states for parity tests
 """
 import math
@@ -244,6 +245,32 @@ def blast(n=64, nz=None, tend=0.2, cfl=0.1, riemann="hllc", recon="pcm", name="b
     prs = np.where(inside, 10.0, 0.1)
     z = np.zeros_like(X)
     return Problem(name, ini, [rho, z.copy(), z.copy(), z.copy(), prs], params=p)
+
+
+def stratified(ini, seed=None):
+    """The reference's H84 / C91 generators (Init.h:104-148) for the .ini
+    text `ini` (problem = H84 or C91): polytropic rho, p from cell centres,
+    the perturbation drawn per cell from stream 31 (H84) / 32 (C91) of
+    [misc] seed -- the same numbers as the fv3d driver draws (the reference
+    draws them from Kokkos' XorShift64 pool instead)."""
+    p = _parse(ini)
+    name = p.problem.decode()
+    X, Y, Z = _centres(p)
+    n = X.size
+    s = p.seed if seed is None else seed
+    z = np.zeros_like(X)
+    if name == "H84":
+        rho = np.power(Z, p.m1)
+        prs = np.power(Z, p.m1 + 1.0)
+        w = p.h84_pert * (uniform(s, 31, n).reshape(X.shape) - 0.5)
+        return Problem(name, ini, [rho, z.copy(), z.copy(), w, prs], params=p)
+    if name == "C91":
+        T = 1.0 + p.theta1 * Z
+        rho = np.power(T, p.m1)
+        prs = np.power(T, p.m1 + 1.0)
+        prs = prs * (1.0 + p.c91_pert * (uniform(s, 32, n).reshape(X.shape) - 0.5))
+        return Problem(name, ini, [rho, z.copy(), z.copy(), z.copy(), prs], params=p)
+    raise ValueError("not a stratified problem: %s" % name)
 
 
 def random_state(shape, seed, wmag=0.0, vmag=1.5):

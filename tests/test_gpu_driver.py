@@ -141,10 +141,126 @@ def test_driver_3d_matches_oracle(tmp_path, problem):
     np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
 
 
+# settings/C91.ini with a smaller grid and end time: 3-D, C91 z boundary,
+# fixed-temperature / fixed-gradient conduction boundaries, viscosity, gravity.
+# With these settings the reference's own run turns non-finite after a few
+# steps (its C91 ghost fill scales the hydrostatic term by the boolean
+# params.gravity instead of g = 40, BoundaryConditions.h:104); the end time
+# keeps the run to the first two steps, before that.
+C91_3D = """[mesh]
+Nx=16
+Ny=16
+Nz=8
+xmin=0.0
+xmax=4.0
+ymin=0.0
+ymax=4.0
+zmin=0.0
+zmax=1.0
+[run]
+tend=0.002
+save_freq=0.001
+boundaries_x=periodic
+boundaries_y=periodic
+boundaries_z=C91
+[solvers]
+riemann_solver=hllc
+reconstruction=plm
+CFL=0.1
+[physics]
+gamma0=1.66666667
+problem=C91
+gravity=true
+g=40.0
+[C91]
+perturbation=1.0e-3
+[polytrope]
+theta1=20.0
+m1=1.0
+[thermal_conduction]
+active=true
+kappa=0.07
+bc_zmin=fixed_temperature
+bc_zmax=fixed_gradient
+bc_zmin_value=1.0
+bc_zmax_value=20.0
+[viscosity]
+active=true
+mu=0.0028
+"""
+
+# settings/H84_chi1.5.ini with a smaller grid and end time; Nz is left unset,
+# so it takes readInifile's default of 32 (a 3-D run, as in the reference)
+H84_3D = """[mesh]
+Nx=16
+Ny=8
+xmin=0.0
+xmax=4.0
+ymin=2.0
+ymax=3.0
+[run]
+tend=0.01
+save_freq=0.005
+boundaries_x=periodic
+boundaries_y=reflecting
+[solvers]
+time_stepping=euler
+riemann_solver=hllc
+reconstruction=plm
+CFL=0.1
+[physics]
+gamma0=1.66666667
+problem=H84
+gravity=true
+g=2.0
+[H84]
+perturbation=1.0e-4
+[thermal_conduction]
+active=true
+kappa=0.0071
+[viscosity]
+active=true
+mu=0.0028
+"""
+
+
+@pytest.mark.parametrize("problem", ["C91", "H84"])
+def test_driver_random_generators_match_oracle(tmp_path, problem):
+    """The perturbed stratified problems (Init.h:104-148) run end to end
+    from the reference's settings: the driver's generated state (--write-ic)
+    advanced by the oracle equals the driver's final snapshot bit for bit."""
+    text = C91_3D if problem == "C91" else H84_3D
+    exe = os.path.join(build.lib_dir(), "fv3d")
+    ini = tmp_path / "run.ini"
+    ini.write_text(text)
+    prefix = str(tmp_path / "snap")
+    ic = str(tmp_path / "ic.bin")
+    r = subprocess.run([exe, str(ini), "--out", prefix, "--write-ic", ic, "--device-loop"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
+    steps, t_end = int(m.group(1)), float(m.group(2))
+    p = fv.parse_ini(text)
+    if problem == "H84":
+        assert p.Nz == 32
+    shape = (p.Nz, p.Ny, p.Nx)
+    q0 = np.fromfile(ic, dtype=np.float64).reshape(5, *shape)
+    assert np.all(np.isfinite(q0))
+    pert = q0[3] if problem == "H84" else q0[4]
+    assert np.std(pert) > 0  # the perturbation is present
+    ora = pyoracle.Oracle(p)
+    ora.set_prim(*q0)
+    t_o, n_o = ora.advance(p.tend)
+    assert (steps, t_end) == (n_o, t_o)
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_"))
+    got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, *shape)
+    np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
+
+
 def test_driver_rejects_unknown_problem(tmp_path):
     exe = os.path.join(build.lib_dir(), "fv3d")
     ini = tmp_path / "x.ini"
-    ini.write_text(INI.replace("sod_x", "H84"))
+    ini.write_text(INI.replace("sod_x", "kelvin_helmholtz"))
     r = subprocess.run([exe, str(ini)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1
     assert "unknown problem" in r.stderr
