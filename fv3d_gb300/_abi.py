@@ -13,6 +13,7 @@ FV_TCM_CONSTANT, FV_TCM_B02 = 0, 1
 FV_BCTC_NONE, FV_BCTC_FIXED_TEMPERATURE, FV_BCTC_FIXED_GRADIENT = 0, 1, 2
 FV_VSC_CONSTANT = 0
 FV_PREC_FP64, FV_PREC_FP32_MIXED = 0, 1
+FV_PHYS_REFERENCE, FV_PHYS_CORRECTED = 0, 1
 
 STATUS_NAMES = {
     0: "FV_OK",
@@ -56,6 +57,7 @@ class FvParams(C.Structure):
         ("log_frequency", C.c_int), ("precision", C.c_int),
         ("problem", C.c_char * 64),
         ("filename_out", C.c_char * 256),
+        ("physics", C.c_int),
     ]
 
     def as_dict(self):

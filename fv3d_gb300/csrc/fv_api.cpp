@@ -181,7 +181,9 @@ int Configure(fv_sim* s) {
     return Fail(s, FV_ERR_UNSUPPORTED, "unknown thermal conductivity mode");
   const bool tc_z = p.thermal_conductivity_active && (B02(p) || p.bctc_zmin != FV_BCTC_NONE ||
                                                       p.bctc_zmax != FV_BCTC_NONE);
-  const bool z_physics = p.well_balanced_flux_at_z_bc || p.boundary_z == FV_BC_C91 || tc_z;
+  // corrected physics runs on the 3-D kernel only (its viscous and HLLC forms)
+  const bool z_physics = p.well_balanced_flux_at_z_bc || p.boundary_z == FV_BC_C91 || tc_z ||
+                         p.physics == FV_PHYS_CORRECTED;
   Grid& G = s->G;
   G = Grid{};
   int plane = -1;
@@ -245,6 +247,7 @@ int Configure(fv_sim* s) {
   G.kappa = p.kappa;
   G.mu = p.mu;
   G.wb_flux_z = p.well_balanced_flux_at_z_bc ? 1 : 0;
+  G.corrected = p.physics == FV_PHYS_CORRECTED ? 1 : 0;
   G.gravity_flag = p.gravity ? 1 : 0;
   G.bctc_zmin = p.thermal_conductivity_active ? p.bctc_zmin : FV_BCTC_NONE;
   G.bctc_zmax = p.thermal_conductivity_active ? p.bctc_zmax : FV_BCTC_NONE;

@@ -439,7 +439,8 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
     if (rc) return Fail(b, rc, "problem %d: %s", i, err.c_str());
     if (b->G[i].ndim != 2)
       return Fail(b, FV_ERR_UNSUPPORTED,
-                  "problem %d: batches run 2-D problems without z-boundary physics; use fvgpu_create", i);
+                  "problem %d: batches run 2-D problems without z-boundary physics or corrected physics; "
+                  "use fvgpu_create", i);
     b->wact[i] = params[i].viscosity_active ? 1 : 0;
     off[i] = total;
     total += (size_t)10 * b->G[i].fstride;

@@ -67,6 +67,7 @@ struct Grid {
   float dx_f, dy_f, dz_f, inv_dx_f, inv_dy_f, inv_dz_f;
   // z-boundary physics of the 3-D kernel (Update.h:131-143,
   // BoundaryConditions.h:87-134, ThermalConduction.h:78-92):
+  int corrected;                   // fv_physics corrected (3-D kernel only)
   int wb_flux_z;                   // well_balanced_flux_at_z_bc
   int gravity_flag;                // params.gravity as the C91 ghost uses it (0/1)
   int bctc_zmin, bctc_zmax;        // fv_bctc_mode

@@ -208,6 +208,8 @@ void FromValues(const IniValues& r, fv_params* o) {
   // Driver-only key (no reference counterpart): storage/arithmetic of the GPU path.
   const std::map<std::string, int> prec{{"fp64", FV_PREC_FP64}, {"fp32_mixed", FV_PREC_FP32_MIXED}};
   o->precision = Lookup(prec, r.Get("gpu", "precision", "fp64"));
+  const std::map<std::string, int> phys{{"reference", FV_PHYS_REFERENCE}, {"corrected", FV_PHYS_CORRECTED}};
+  o->physics = Lookup(phys, r.Get("gpu", "physics", "reference"));
 }
 
 }  // namespace

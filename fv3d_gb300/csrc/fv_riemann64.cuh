@@ -98,13 +98,14 @@ __device__ __forceinline__ void hll64(const Slots<double>& L, const Slots<double
 // HLLC, RiemannSolvers.h:39-112; the kinetic energy uses un and t1 only, as
 // the reference does.
 // pout as for hll64 (RiemannSolvers.h:81-104: pL, p*, p*, pR by region).
-template <int ZS>
+// KE3 (corrected physics): the kinetic energy of all three velocities.
+template <int ZS, bool KE3 = false>
 __device__ __forceinline__ void hllc64(const Slots<double>& L, const Slots<double>& R, const Consts64& K,
                                        double flux[5], double* pout = nullptr) {
   const double rL = L.r, uL = L.un, pL = L.p;
   const double rR = R.r, uR = R.un, pR = R.p;
-  const double kL = ZS == 1 ? uL * uL : uL * uL + L.t1 * L.t1;
-  const double kR = ZS == 1 ? uR * uR : uR * uR + R.t1 * R.t1;
+  const double kL = KE3 ? ke_sum3<ZS>(uL, L.t1, L.t2) : (ZS == 1 ? uL * uL : uL * uL + L.t1 * L.t1);
+  const double kR = KE3 ? ke_sum3<ZS>(uR, R.t1, R.t2) : (ZS == 1 ? uR * uR : uR * uR + R.t1 * R.t1);
   const double EL = half64(rL) * kL + pL * K.inv_gm1;
   const double ER = half64(rR) * kR + pR * K.inv_gm1;
   const double c2L = pL * K.gamma / rL;

@@ -180,7 +180,9 @@ __device__ __forceinline__ void unslot3(const double f[5], double out[5]) {
 // The z slopes take minmod(forward, backward) (Update.h:84), x and y
 // minmod(backward, forward); the two orders differ only in the sign of a
 // zero slope.
-template <int DIR>
+// CORR: corrected physics (HLLC with the kinetic energy of all three
+// velocities).
+template <int DIR, bool CORR>
 __device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, const Grid& G, const Consts64& K,
                                       double out[5], double* pout) {
   double qL[5], qR[5];
@@ -206,15 +208,16 @@ __device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, c
   if (rs == 0)
     hll64<0>(L, R, K, f, pout);
   else
-    hllc64<0>(L, R, K, f, pout);
+    hllc64<0, CORR>(L, R, K, f, pout);
   unslot3<DIR>(f, out);
 }
 
 // Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
-// including its z-branch index and field mix-ups.  P(dk, dj, di, var) reads
-// velocity var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x),
-// i.e. stencil[dk][dj][di][var].
-template <class PA>
+// including its z-branch index and field mix-ups (CORR: the z branch as the
+// mirror of the x / y branches instead).  P(dk, dj, di, var) reads velocity
+// var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x), i.e.
+// stencil[dk][dj][di][var].
+template <bool CORR, class PA>
 __device__ __forceinline__ void viscous3d(const PA& P, double odx, double ody, double odz, double mu,
                                           double vf[3][5]) {
   const double four_thirds = 4.0 / 3.0;
@@ -276,10 +279,18 @@ __device__ __forceinline__ void viscous3d(const PA& P, double odx, double ody, d
     const double dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
     const double dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
     const double dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
-    const double dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
-    const double dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
-    const double dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
-    const double dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
+    double dudx, dwdx, dvdy, dwdy;
+    if (CORR) {
+      dudx = c4x * (P(s, 1, 2, U) - P(s, 1, 0, U) + P(s - 1, 1, 2, U) - P(s - 1, 1, 0, U));
+      dwdx = c4x * (P(s, 1, 2, W) - P(s, 1, 0, W) + P(s - 1, 1, 2, W) - P(s - 1, 1, 0, W));
+      dvdy = c4y * (P(s, 2, 1, V) - P(s, 0, 1, V) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, V));
+      dwdy = c4y * (P(s, 2, 1, W) - P(s, 0, 1, W) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, W));
+    } else {
+      dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
+      dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
+      dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
+      dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
+    }
     const double tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
     const double tau_xz = dudz + dwdx;
     const double tau_yz = dvdz + dwdy;
@@ -301,7 +312,7 @@ struct RingVel {
 
 // One stage for the CTA's columns and z chunk; P2: every cell size is a
 // power of two (the kernel branches on it once, uniformly).
-template <int RS, int KIND, bool P2>
+template <int RS, int KIND, bool P2, bool CORR>
 __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                              StepCtrl* __restrict__ ctrl, int tz, const Fields& hout,
                                              double* smem_raw, unsigned long long* s_red) {
@@ -343,7 +354,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
     for (int m = 0; m < 4; ++m)
 #pragma unroll
       for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k0 - 2 + m), v, cy + 2, cx + 2);
-    face3<2>(c, rs, recon, G, K, fzL, need_pout ? &poutL : nullptr);
+    face3<2, CORR>(c, rs, recon, G, K, fzL, need_pout ? &poutL : nullptr);
   }
   __syncthreads();
 
@@ -362,7 +373,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + 2, fx + m);
-        face3<0>(c, rs, recon, G, K, f, nullptr);
+        face3<0, CORR>(c, rs, recon, G, K, f, nullptr);
 #pragma unroll
         for (int v = 0; v < 5; ++v) S.fa(v, fy, fx) = f[v];
       } else {
@@ -372,7 +383,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + m, fx + 2);
-        face3<1>(c, rs, recon, G, K, f, nullptr);
+        face3<1, CORR>(c, rs, recon, G, K, f, nullptr);
 #pragma unroll
         for (int v = 0; v < 5; ++v) S.fb(v, fy, fx) = f[v];
       }
@@ -388,7 +399,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k - 1 + m), v, cy + 2, cx + 2);
-        face3<2>(c, rs, recon, G, K, fzR, need_pout ? &poutR : nullptr);
+        face3<2, CORR>(c, rs, recon, G, K, fzR, need_pout ? &poutR : nullptr);
       }
       const long long o = k * zstride + col;
       double un[5];
@@ -467,9 +478,16 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
       if (G.visc) {  // Viscosity.h:145-151
         const RingVel P{S, k, cy + 2, cx + 2};
         double vf[3][5];
-        viscous3d(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
+        viscous3d<CORR>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
+        if (CORR) {  // the flux differences divided by the cell sizes
 #pragma unroll
-        for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
+          for (int v = 1; v < 5; ++v)
+            un[v] = un[v] + dt * (div_cell<P2>(vf[0][v], G.dx, G.inv_dx) + div_cell<P2>(vf[1][v], G.dy, G.inv_dy) +
+                                  div_cell<P2>(vf[2][v], G.dz, G.inv_dz));
+        } else {
+#pragma unroll
+          for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
+        }
       }
       if (KIND == STAGE_RK_2) {
 #pragma unroll
@@ -499,22 +517,22 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
   if (KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
-template <int RS, int KIND>
+template <int RS, int KIND, bool CORR>
 __global__ void __launch_bounds__(kThreads, 2)
 stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
              int tz, const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
   if (G.pow2_all)
-    stage3d_body<RS, KIND, true>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
+    stage3d_body<RS, KIND, true, CORR>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
   else
-    stage3d_body<RS, KIND, false>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
+    stage3d_body<RS, KIND, false, CORR>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
 }
 
-template <int RS, int KIND>
+template <int RS, int KIND, bool CORR>
 cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, const Fields* hout,
                        cudaStream_t st) {
-  auto kern = stage3d_fp64<RS, KIND>;
+  auto kern = stage3d_fp64<RS, KIND, CORR>;
   static bool attr_set = false;  // per instantiation, once per process
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem3::bytes(true));
@@ -529,14 +547,21 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   return cudaGetLastError();
 }
 
-template <int RS>
+template <int RS, bool CORR>
 cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
                         const Fields* hout, cudaStream_t st) {
   switch (kind) {
-    case STAGE_EULER: return launch_one<RS, STAGE_EULER>(G, uin, u0, uout, ctrl, hout, st);
-    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1>(G, uin, u0, uout, ctrl, nullptr, st);
-    default: return launch_one<RS, STAGE_RK_2>(G, uin, u0, uout, ctrl, hout, st);
+    case STAGE_EULER: return launch_one<RS, STAGE_EULER, CORR>(G, uin, u0, uout, ctrl, hout, st);
+    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1, CORR>(G, uin, u0, uout, ctrl, nullptr, st);
+    default: return launch_one<RS, STAGE_RK_2, CORR>(G, uin, u0, uout, ctrl, hout, st);
   }
+}
+
+template <int RS>
+cudaError_t launch_phys(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
+                        const Fields* hout, cudaStream_t st) {
+  return G.corrected ? launch_kind<RS, true>(G, kind, uin, u0, uout, ctrl, hout, st)
+                     : launch_kind<RS, false>(G, kind, uin, u0, uout, ctrl, hout, st);
 }
 
 }  // namespace
@@ -557,8 +582,8 @@ int stage3d_layers_per_cta(const Grid& G) {
 
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
                            StepCtrl* ctrl, cudaStream_t st, const Fields* hout) {
-  return riemann_solver == 0 ? launch_kind<0>(G, kind, uin, u0, uout, ctrl, hout, st)
-                             : launch_kind<1>(G, kind, uin, u0, uout, ctrl, hout, st);
+  return riemann_solver == 0 ? launch_phys<0>(G, kind, uin, u0, uout, ctrl, hout, st)
+                             : launch_phys<1>(G, kind, uin, u0, uout, ctrl, hout, st);
 }
 
 }  // namespace fv

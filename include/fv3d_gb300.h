@@ -45,6 +45,13 @@ enum fv_bctc_mode  { FV_BCTC_NONE = 0, FV_BCTC_FIXED_TEMPERATURE = 1, FV_BCTC_FI
 enum fv_visc_mode  { FV_VSC_CONSTANT = 0 };
 /* Storage/arithmetic of the GPU path (driver-only setting, no reference counterpart). */
 enum fv_precision  { FV_PREC_FP64 = 0, FV_PREC_FP32_MIXED = 1 };
+/* FV_PHYS_REFERENCE reproduces the reference's arithmetic, including its
+ * viscous flux divergence without 1/d (Viscosity.h:151), its z-branch index
+ * and field mix-ups (Viscosity.h:122-129) and HLLC's kinetic energy from two
+ * velocities (RiemannSolvers.h:52-55).  FV_PHYS_CORRECTED divides the
+ * viscous fluxes by the cell size, uses the mirror of the x / y branches
+ * for z, and gives HLLC all three velocities (no reference counterpart). */
+enum fv_physics    { FV_PHYS_REFERENCE = 0, FV_PHYS_CORRECTED = 1 };
 
 /* Status codes. */
 enum fv_status {
@@ -61,7 +68,8 @@ enum fv_status {
 
 /*
  * Run parameters.  Mirrors fv3d::Params (SimInfo.h:72-159) minus the Kokkos
- * ranges, plus two driver-only fields (precision, problem/filename strings).
+ * ranges, plus driver-only fields (precision, physics, problem/filename
+ * strings).
  * Fill it with fv_read_ini / fv_parse_ini (reference readInifile semantics,
  * including single-precision parsing of every GetFloat key) or by hand; dx,
  * dy, dz must then equal (max-min)/N as readInifile computes them.
@@ -96,6 +104,7 @@ typedef struct fv_params {
   int log_frequency, precision;
   char problem[64];
   char filename_out[256];
+  int physics;          /* fv_physics ([gpu] physics = reference | corrected) */
 } fv_params;
 
 /* Human-readable name of a status code (static storage). */

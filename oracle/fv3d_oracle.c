@@ -124,13 +124,15 @@ static void hll(const double* qL, const double* qR, double* flux, double* pout, 
 }
 
 /* RiemannSolvers.h:39-112 (HLLC) */
-static void hllc(const double* qL, const double* qR, double* flux, double* pout, double gamma0) {
+/* ke3 (corrected physics only): the kinetic energy of all three velocities
+ * instead of the reference's IU, IV slots. */
+static void hllc(const double* qL, const double* qR, double* flux, double* pout, double gamma0, int ke3) {
   const double rL = qL[IR], uL = qL[IU], vL = qL[IV], pL = qL[IP];
   const double rR = qR[IR], uR = qR[IU], vR = qR[IV], pR = qR[IP];
   const double entho = 1.0 / (gamma0 - 1.0);
-  const double ekL = 0.5 * rL * (uL * uL + vL * vL);
+  const double ekL = ke3 ? 0.5 * rL * (uL * uL + vL * vL + qL[IW] * qL[IW]) : 0.5 * rL * (uL * uL + vL * vL);
   const double EL = ekL + pL * entho;
-  const double ekR = 0.5 * rR * (uR * uR + vR * vR);
+  const double ekR = ke3 ? 0.5 * rR * (uR * uR + vR * vR + qR[IW] * qR[IW]) : 0.5 * rR * (uR * uR + vR * vR);
   const double ER = ekR + pR * entho;
   const double cfastL = sound_speed(qL, gamma0);
   const double cfastR = sound_speed(qR, gamma0);
@@ -173,7 +175,7 @@ static void riemann(const fvora_sim* s, const double* qL, const double* qR, doub
   if (s->p.riemann_solver == FV_HLL)
     hll(qL, qR, flux, pout, s->p.gamma0);
   else
-    hllc(qL, qR, flux, pout, s->p.gamma0);
+    hllc(qL, qR, flux, pout, s->p.gamma0, s->p.physics == FV_PHYS_CORRECTED);
 }
 
 /* ---------------- SimInfo.h array kernels ---------------- */
@@ -506,6 +508,7 @@ static void apply_viscosity(fvora_sim* s, const double* Q, double* Unew, double 
   const double dx = P->dx, dy = P->dy, dz = P->dz;
   const double four_thirds = 4.0 / 3.0;
   const double two_thirds = 2.0 / 3.0;
+  const int corrected = P->physics == FV_PHYS_CORRECTED;
 #pragma omp parallel for collapse(2) schedule(static)
   for (int k = r.b[2]; k < r.e[2]; ++k)
     for (int j = r.b[1]; j < r.e[1]; ++j)
@@ -565,6 +568,27 @@ static void apply_viscosity(fvora_sim* s, const double* Q, double* Unew, double 
               flux[IV] += sign * mu * tau_yy;
               flux[IW] += sign * mu * tau_yz;
               flux[IE] += sign * mu * (tau_xy * qi[IU] + tau_yy * qi[IV] + tau_yz * qi[IW]);
+            } else if (corrected) {
+              /* the mirror of the x / y branches (no counterpart in the reference) */
+              for (int v = 0; v < 5; ++v) qi[v] = (st[side][1][1][v] + st[side - 1][1][1][v]) * 0.5;
+              double dudz = one_over_dz * (st[side][1][1][IU] - st[side - 1][1][1][IU]);
+              double dvdz = one_over_dz * (st[side][1][1][IV] - st[side - 1][1][1][IV]);
+              double dwdz = one_over_dz * (st[side][1][1][IW] - st[side - 1][1][1][IW]);
+              double dudx = 0.25 * one_over_dx * (st[side][1][2][IU] - st[side][1][0][IU]
+                                                + st[side - 1][1][2][IU] - st[side - 1][1][0][IU]);
+              double dwdx = 0.25 * one_over_dx * (st[side][1][2][IW] - st[side][1][0][IW]
+                                                + st[side - 1][1][2][IW] - st[side - 1][1][0][IW]);
+              double dvdy = 0.25 * one_over_dy * (st[side][2][1][IV] - st[side][0][1][IV]
+                                                + st[side - 1][2][1][IV] - st[side - 1][0][1][IV]);
+              double dwdy = 0.25 * one_over_dy * (st[side][2][1][IW] - st[side][0][1][IW]
+                                                + st[side - 1][2][1][IW] - st[side - 1][0][1][IW]);
+              const double tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+              const double tau_xz = dudz + dwdx;
+              const double tau_yz = dvdz + dwdy;
+              flux[IU] += sign * mu * tau_xz;
+              flux[IV] += sign * mu * tau_yz;
+              flux[IW] += sign * mu * tau_zz;
+              flux[IE] += sign * mu * (tau_xz * qi[IU] + tau_yz * qi[IV] + tau_zz * qi[IW]);
             } else {
               for (int v = 0; v < 5; ++v) qi[v] = (st[side][1][1][v] + st[side - 1][1][1][v]) * 0.5;
               double dudz = one_over_dz * (st[side][1][1][IU] - st[side - 1][1][1][IU]);
@@ -590,7 +614,10 @@ static void apply_viscosity(fvora_sim* s, const double* Q, double* Unew, double 
           memcpy(vf[dir], flux, sizeof(flux));
         }
         double* un = AT(s, Unew, i, j, k);
-        for (int v = 0; v < 5; ++v) un[v] += (vf[0][v] + vf[1][v] + vf[2][v]) * dt;
+        if (corrected)
+          for (int v = 0; v < 5; ++v) un[v] += (vf[0][v] / dx + vf[1][v] / dy + vf[2][v] / dz) * dt;
+        else
+          for (int v = 0; v < 5; ++v) un[v] += (vf[0][v] + vf[1][v] + vf[2][v]) * dt;
       }
 }
 
@@ -793,7 +820,7 @@ int fvora_riemann(int solver, double gamma0, long n, const double* qL, const dou
                   double* pout) {
   for (long c = 0; c < n; ++c) {
     if (solver == FV_HLL) hll(qL + 5 * c, qR + 5 * c, flux + 5 * c, pout + c, gamma0);
-    else hllc(qL + 5 * c, qR + 5 * c, flux + 5 * c, pout + c, gamma0);
+    else hllc(qL + 5 * c, qR + 5 * c, flux + 5 * c, pout + c, gamma0, 0);
   }
   return FV_OK;
 }

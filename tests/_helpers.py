@@ -35,7 +35,7 @@ def load_case(name):
 def params_from_dict(dct):
     p = FvParams()
     for name, _ in FvParams._fields_:
-        v = dct[name]
+        v = dct.get(name, 0)  # fields added after a fixture was made default to 0
         setattr(p, name, v.encode() if isinstance(v, str) else v)
     return p
 
