@@ -16,7 +16,10 @@
 // bit-identical to a reference run.  Any other initial state is read with --ic
 // from a raw file of 5 float64 arrays (rho, u, v, w, p), each Nz*Ny*Nx in C
 // order; --write-ic writes the generated state in that format.  Snapshots
-// are written as the same raw format (<prefix>_<ite>.bin) instead of HDF5.
+// are written as the same raw format (<prefix>_<ite>.bin) instead of HDF5,
+// with the vertex coordinates in <prefix>_grid.bin and an XDMF index
+// (<prefix>.xdmf) shaped like the reference's, so XDMF readers (ParaView,
+// VisIt) open the series.
 //
 // --device-loop runs the steps between two saves with fvgpu_advance (dt stays
 // on the GPU) instead of one compute_dt/step round trip per step.
@@ -26,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "fv3d_gb300.h"
@@ -134,6 +138,89 @@ bool WriteRaw(const std::string& path, const Fields& q) {
   return ok;
 }
 
+std::string BaseName(const std::string& path) {
+  const size_t k = path.find_last_of('/');
+  return k == std::string::npos ? path : path.substr(k + 1);
+}
+
+// Vertex coordinates as IOManager.h:115-124 writes them ((i - ibeg) * dx,
+// ...; no xmin offset), three arrays of (Nz+1)(Ny+1)(Nx+1) doubles.
+bool WriteGrid(const std::string& path, const fv_params& p) {
+  Fields g;
+  const size_t nv = (size_t)(p.Nx + 1) * (p.Ny + 1) * (p.Nz + 1);
+  for (int a = 0; a < 3; ++a) g.f[a].reserve(nv);
+  for (int k = 0; k <= p.Nz; ++k)
+    for (int j = 0; j <= p.Ny; ++j)
+      for (int i = 0; i <= p.Nx; ++i) {
+        g.f[0].push_back(i * p.dx);
+        g.f[1].push_back(j * p.dy);
+        g.f[2].push_back(k * p.dz);
+      }
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return false;
+  bool ok = true;
+  for (int a = 0; a < 3; ++a) ok = ok && std::fwrite(g.f[a].data(), sizeof(double), nv, f) == nv;
+  std::fclose(f);
+  return ok;
+}
+
+// The XDMF index of the snapshots, laid out like the reference's
+// (IOManager.h:16-77: a temporal collection over one 3DSMesh / X_Y_Z
+// geometry; per save rho, a velocity vector joined from u, v, w, and prs),
+// with its data items pointing into the raw files (Format="Binary", Seek =
+// byte offset of the field) instead of HDF5 datasets.
+bool WriteXdmf(const std::string& path, const fv_params& p, const std::string& grid,
+               const std::vector<std::pair<std::string, double>>& snaps) {
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  const int nx = p.Nx, ny = p.Ny, nz = p.Nz;
+  const size_t nv = (size_t)(nx + 1) * (ny + 1) * (nz + 1), nc = (size_t)nx * ny * nz;
+  auto item = [&](const std::string& file, size_t seek, int a, int b, int c) {
+    std::fprintf(f,
+                 "<DataItem Dimensions=\"%d %d %d\" NumberType=\"Float\" Precision=\"8\" Format=\"Binary\" "
+                 "Endian=\"Little\" Seek=\"%zu\">%s</DataItem>",
+                 a, b, c, seek, file.c_str());
+  };
+  std::fprintf(f, "<?xml version=\"1.0\" ?>\n<!DOCTYPE Xdmf SYSTEM \"Xdmf.dtd\" []>\n<Xdmf Version=\"2.0\">\n"
+                  "<Domain CollectionType=\"Temporal\">\n"
+                  "  <Grid Name=\"MainTimeSeries\" GridType=\"Collection\" CollectionType=\"Temporal\">\n"
+                  "    <Topology Name=\"Main Topology\" TopologyType=\"3DSMesh\" NumberOfElements=\"%d %d %d\"/>\n"
+                  "    <Geometry Name=\"Main Geometry\" GeometryType=\"X_Y_Z\">\n",
+               nz + 1, ny + 1, nx + 1);
+  for (int a = 0; a < 3; ++a) {
+    std::fprintf(f, "      ");
+    item(grid, a * nv * sizeof(double), nz + 1, ny + 1, nx + 1);
+    std::fprintf(f, "\n");
+  }
+  std::fprintf(f, "    </Geometry>\n");
+  for (const auto& sn : snaps) {
+    std::fprintf(f,
+                 "    <Grid Name=\"Cells\" GridType=\"Uniform\">\n      <Time TimeType=\"Single\" Value=\"%.17g\" />\n"
+                 "      <Topology Reference=\"//Topology[@Name='Main Topology']\" />\n"
+                 "      <Geometry Reference=\"//Geometry[@Name='Main Geometry']\" />\n",
+                 sn.second);
+    std::fprintf(f, "      <Attribute Name=\"rho\" AttributeType=\"Scalar\" Center=\"Cell\">\n        ");
+    item(sn.first, 0, nz, ny, nx);
+    std::fprintf(f, "\n      </Attribute>\n");
+    std::fprintf(f, "      <Attribute Name=\"velocity\" AttributeType=\"Vector\" Center=\"Cell\">\n"
+                    "        <DataItem Dimensions=\"%d %d %d 3\" ItemType=\"Function\" Function=\"JOIN($0, $1, $2)\">\n",
+                 nz, ny, nx);
+    for (int v = 1; v <= 3; ++v) {
+      std::fprintf(f, "          ");
+      item(sn.first, v * nc * sizeof(double), nz, ny, nx);
+      std::fprintf(f, "\n");
+    }
+    std::fprintf(f, "        </DataItem>\n      </Attribute>\n");
+    std::fprintf(f, "      <Attribute Name=\"prs\" AttributeType=\"Scalar\" Center=\"Cell\">\n        ");
+    item(sn.first, 4 * nc * sizeof(double), nz, ny, nx);
+    std::fprintf(f, "\n      </Attribute>\n    </Grid>\n");
+  }
+  std::fprintf(f, "  </Grid>\n</Domain>\n</Xdmf>\n");
+  const bool ok = std::ferror(f) == 0;
+  std::fclose(f);
+  return ok;
+}
+
 int Check(fv_sim* s, int rc, const char* what) {
   if (rc != FV_OK) std::fprintf(stderr, "%s: %s (%s)\n", what, fv_status_string(rc), fvgpu_last_error(s));
   return rc;
@@ -187,12 +274,17 @@ int main(int argc, char** argv) {
   int ite = 0, next_log = 0;
   long steps = 0;
   // the loop announces its saves (main.cpp:64); the final one is silent (main.cpp:76)
+  std::vector<std::pair<std::string, double>> snaps;
+  const std::string grid = out + "_grid.bin";
   auto save = [&](double tt, bool announce) {
     fvgpu_get_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data());
     char name[512];
     std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite++);
     if (announce) std::printf(" - Saving at time %g\n", tt);
+    if (snaps.empty()) WriteGrid(grid, p);
     WriteRaw(name, q);
+    snaps.emplace_back(BaseName(name), tt);
+    WriteXdmf(out + ".xdmf", p, BaseName(grid), snaps);
   };
   while (t + p.epsilon < p.tend) {
     const bool save_needed = (t + p.epsilon > next_save);

@@ -45,6 +45,36 @@ log_frequency=5
 """
 
 
+def _check_xdmf(tmp_path, shape, nsnaps):
+    """The XDMF index lists every snapshot in order, and each data item
+    (file, byte offset, dimensions) reads back the snapshot's field."""
+    import xml.etree.ElementTree as ET
+    root = ET.parse(str(tmp_path / "snap.xdmf")).getroot()
+    coll = root.find("Domain/Grid")
+    assert coll.get("CollectionType") == "Temporal"
+    nz, ny, nx = shape
+    geo = coll.findall("Geometry/DataItem")
+    assert len(geo) == 3
+    xs = np.fromfile(str(tmp_path / geo[0].text), dtype=np.float64, count=(nz + 1) * (ny + 1) * (nx + 1),
+                     offset=int(geo[0].get("Seek")))
+    assert xs[1] > xs[0] == 0.0
+    grids = coll.findall("Grid")
+    assert len(grids) == nsnaps
+    times = [float(g.find("Time").get("Value")) for g in grids]
+    assert times == sorted(times) and times[0] == 0.0
+    for g in grids:
+        items = g.findall(".//Attribute/DataItem") + g.findall(".//Attribute/DataItem/DataItem")
+        items = [d for d in items if d.get("Format") == "Binary"]
+        assert len(items) == 5
+        for d in items:
+            dims = tuple(int(v) for v in d.get("Dimensions").split())
+            assert dims == shape
+            a = np.fromfile(str(tmp_path / d.text), dtype=np.float64, count=nz * ny * nx, offset=int(d.get("Seek")))
+            raw = np.fromfile(str(tmp_path / d.text), dtype=np.float64).reshape(5, nz * ny * nx)
+            k = int(d.get("Seek")) // (8 * nz * ny * nx)
+            np.testing.assert_array_equal(a, raw[k])
+
+
 @pytest.mark.parametrize("mode", ["host", "device"])
 def test_driver_matches_oracle(tmp_path, mode):
     exe = os.path.join(build.lib_dir(), "fv3d")
@@ -58,7 +88,7 @@ def test_driver_matches_oracle(tmp_path, mode):
     assert "Computing dts at (t=0)" in r.stdout
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_"))
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
     assert len(snaps) == r.stdout.count("Saving at time") + 1
 
     p = fv.parse_ini(INI)
@@ -69,6 +99,7 @@ def test_driver_matches_oracle(tmp_path, mode):
     assert (steps, t_end) == (n_o, t_o)
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, 1, 8, 64)
     np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
+    _check_xdmf(tmp_path, (1, 8, 64), len(snaps))
 
 
 SOD_3D = """[mesh]
@@ -131,7 +162,7 @@ def test_driver_3d_matches_oracle(tmp_path, problem):
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_"))
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
     p = fv.parse_ini(text)
     ora = pyoracle.Oracle(p)
     ora.set_prim(*_ic_3d(p, problem))
@@ -252,7 +283,7 @@ def test_driver_random_generators_match_oracle(tmp_path, problem):
     ora.set_prim(*q0)
     t_o, n_o = ora.advance(p.tend)
     assert (steps, t_end) == (n_o, t_o)
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_"))
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, *shape)
     np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
 
