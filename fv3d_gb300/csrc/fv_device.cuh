@@ -1,8 +1,6 @@
-// fv_device.cuh -- device-side building blocks of the GB300 hydro step.
-//
-// Everything here is templated on the arithmetic type T (double for the plain
-// FP64 path, float for the mixed path) and follows the reference's
-// floating-point operation order unless a comment says otherwise.
+// fv_device.cuh -- device-side types shared by every kernel of the GB300
+// hydro step: the control block, the grid description, the ghost-cell index
+// map, the slot order of a sweep and the CFL atomic.
 #pragma once
 
 #include <cstdint>
@@ -105,117 +103,6 @@ template <class T>
 struct Slots {
   T r, un, t1, t2, p;
 };
-
-// sqrt(p*gamma/rho), States.h:48-50
-template <class T>
-__device__ __forceinline__ T sound_speed(T r, T p, T gamma) {
-  return sqrt(p * gamma / r);
-}
-
-// computeFlux, States.h:114-127 (slot order in, slot order out).
-template <class T>
-__device__ __forceinline__ void euler_flux(const Slots<T>& q, T gamma, T f[5]) {
-  const T Ek = T(0.5) * q.r * (q.un * q.un + q.t1 * q.t1 + q.t2 * q.t2);
-  const T E = (q.p / (gamma - T(1)) + Ek);
-  f[0] = q.r * q.un;
-  f[1] = q.r * q.un * q.un + q.p;
-  f[2] = q.r * q.un * q.t1;
-  f[3] = q.r * q.un * q.t2;
-  f[4] = (q.p + E) * q.un;
-}
-
-// primToCons, States.h:20-31 (slot order).
-template <class T>
-__device__ __forceinline__ void prim_to_cons_slots(const Slots<T>& q, T gamma, T u[5]) {
-  u[0] = q.r;
-  u[1] = q.r * q.un;
-  u[2] = q.r * q.t1;
-  u[3] = q.r * q.t2;
-  const T Ek = T(0.5) * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / q.r;
-  u[4] = (Ek + q.p / (gamma - T(1)));
-}
-
-// HLL with Davis wave-speed estimates, RiemannSolvers.h:6-36.
-template <class T>
-__device__ __forceinline__ void riemann_hll(const Slots<T>& L, const Slots<T>& R, T gamma, T flux[5]) {
-  const T aL = sound_speed(L.r, L.p, gamma);
-  const T aR = sound_speed(R.r, R.p, gamma);
-  const T SL = fmin(L.un - aL, R.un - aR);
-  const T SR = fmax(L.un + aL, R.un + aR);
-  T FL[5], FR[5];
-  euler_flux(L, gamma, FL);
-  euler_flux(R, gamma, FR);
-  if (SL >= T(0)) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) flux[v] = FL[v];
-  } else if (SR <= T(0)) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) flux[v] = FR[v];
-  } else {
-    T uL[5], uR[5];
-    prim_to_cons_slots(L, gamma, uL);
-    prim_to_cons_slots(R, gamma, uR);
-    const T slsr = SL * SR;
-    const T den = SR - SL;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) flux[v] = ((FL[v] * SR - FR[v] * SL) + (uR[v] - uL[v]) * slsr) / den;
-  }
-}
-
-// HLLC, RiemannSolvers.h:39-112.  The kinetic energy uses only the normal
-// and first transverse slots, as the reference does (RiemannSolvers.h:52,54).
-template <class T>
-__device__ __forceinline__ void riemann_hllc(const Slots<T>& L, const Slots<T>& R, T gamma, T flux[5]) {
-  const T rL = L.r, uL = L.un, vL = L.t1, pL = L.p;
-  const T rR = R.r, uR = R.un, vR = R.t1, pR = R.p;
-  const T entho = T(1) / (gamma - T(1));
-  const T EL = T(0.5) * rL * (uL * uL + vL * vL) + pL * entho;
-  const T ER = T(0.5) * rR * (uR * uR + vR * vR) + pR * entho;
-  const T cL = sound_speed(rL, pL, gamma);
-  const T cR = sound_speed(rR, pR, gamma);
-  const T cmax = fmax(cL, cR);
-  const T SL = fmin(uL, uR) - cmax;
-  const T SR = fmax(uL, uR) + cmax;
-  const T rcL = rL * (uL - SL);
-  const T rcR = rR * (SR - uR);
-  const T uS = (rcR * uR + rcL * uL + (pL - pR)) / (rcR + rcL);
-  const T pS = (rcR * pL + rcL * pR + rcL * rcR * (uL - uR)) / (rcR + rcL);
-  T sr, su, st1, st2, sp, E;
-  if (SL > T(0)) {
-    sr = rL; su = uL; st1 = L.t1; st2 = L.t2; sp = pL; E = EL;
-  } else if (uS > T(0)) {
-    sr = rL * (SL - uL) / (SL - uS);
-    E = ((SL - uL) * EL - pL * uL + pS * uS) / (SL - uS);
-    su = uS; st1 = L.t1; st2 = L.t2; sp = pS;
-  } else if (SR > T(0)) {
-    sr = rR * (SR - uR) / (SR - uS);
-    E = ((SR - uR) * ER - pR * uR + pS * uS) / (SR - uS);
-    su = uS; st1 = R.t1; st2 = R.t2; sp = pS;
-  } else {
-    sr = rR; su = uR; st1 = R.t1; st2 = R.t2; sp = pR; E = ER;
-  }
-  flux[0] = sr * su;
-  flux[1] = sr * su * su + sp;
-  flux[2] = flux[0] * st1;
-  flux[3] = flux[0] * st2;
-  flux[4] = (E + sp) * su;
-}
-
-template <class T, int RS>
-__device__ __forceinline__ void riemann(const Slots<T>& L, const Slots<T>& R, T gamma, T flux[5]) {
-  if (RS == 0)
-    riemann_hll(L, R, gamma, flux);
-  else
-    riemann_hllc(L, R, gamma, flux);
-}
-
-// minmod of Update.h:73-80: 0 if dL*dR < 0, else the argument of smaller
-// magnitude, ties going to the second.
-template <class T>
-__device__ __forceinline__ T minmod(T dL, T dR) {
-  if (dL * dR < T(0)) return T(0);
-  return fabs(dL) < fabs(dR) ? dL : dR;
-}
 
 // Atomic max of a non-negative double stored as its bit pattern (IEEE order
 // of non-negative doubles equals unsigned integer order; NaN sorts above +inf).

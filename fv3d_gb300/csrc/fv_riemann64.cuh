@@ -147,13 +147,4 @@ __device__ __forceinline__ void hllc64(const Slots<double>& L, const Slots<doubl
   flux[4] = (E + sp) * su;
 }
 
-template <int RS, int ZS>
-__device__ __forceinline__ void riemann64(const Slots<double>& L, const Slots<double>& R, const Consts64& K,
-                                          double flux[5]) {
-  if (RS == 0)
-    hll64<ZS>(L, R, K, flux);
-  else
-    hllc64<ZS>(L, R, K, flux);
-}
-
 }  // namespace fv
