@@ -44,8 +44,11 @@ using fv::StepCtrl;
 namespace {
 
 constexpr int kGraphSteps = 8;
+constexpr int kMaxGroups = 8;  // two work-queue counters each
 
 struct Group {
+  int ndim = 2;     // 3: 3-D problems (one kernel shape, grouped by solver)
+  int rs = -1;      // 3-D groups: the shared Riemann solver
   int plane = 0;
   bool wact = false;
   bool tc = false;
@@ -176,12 +179,20 @@ int NumShapes(int precision, const fv::TileShape** shapes) {
 }
 
 int Occupancy(const fv_batch* b, const Group& g, int shape) {
+  if (g.ndim == 3)
+    return b->precision == FV_PREC_FP64 ? fv::batch_stage3d_occupancy64(g.tc) : fv::batch_stage3d_occupancy32(g.tc);
   return b->precision == FV_PREC_FP64 ? fv::batch_stage_occupancy64(g.plane, g.wact, shape, g.tc)
                                       : fv::batch_stage_occupancy32(g.plane, g.wact, shape, g.tc);
 }
 
 cudaError_t LaunchStage(const fv_batch* b, const Group& g, const BatchInst* insts, int ntiles, int grid,
                         unsigned* queue, int kind, int flip) {
+  if (g.ndim == 3)
+    return b->precision == FV_PREC_FP64
+               ? fv::launch_batch_stage3d64(insts, (int)g.members.size(), ntiles, queue, kind, flip, g.rs, grid, g.tc,
+                                            b->stream)
+               : fv::launch_batch_stage3d32(insts, (int)g.members.size(), ntiles, queue, kind, flip, g.rs, grid, g.tc,
+                                            b->stream);
   return b->precision == FV_PREC_FP64
              ? fv::launch_batch_stage64(g.plane, g.wact, g.shape, insts, (int)g.members.size(), ntiles, queue, kind,
                                         flip, grid, g.tc, b->stream)
@@ -190,10 +201,12 @@ cudaError_t LaunchStage(const fv_batch* b, const Group& g, const BatchInst* inst
 }
 
 // Descriptors of group g for tile shape `shape` (tile numbering per group).
+// 3-D groups: 16 x 16 column blocks and chunks of up to 16 z layers.
 std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, StepCtrl* ctrl_base, int* ntiles) {
   const fv::TileShape* shapes;
   NumShapes(b->precision, &shapes);
-  const int tx = shapes[shape].tx, ty = shapes[shape].ty;
+  const int tx = g.ndim == 3 ? fv::batch3d_columns() : shapes[shape].tx;
+  const int ty = g.ndim == 3 ? fv::batch3d_columns() : shapes[shape].ty;
   std::vector<BatchInst> out;
   int t0 = 0;
   for (int i : g.members) {
@@ -204,10 +217,12 @@ std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, St
     I.B = b->B[i];
     I.ctrl = ctrl_base + i;
     I.tiles_x = (I.G.na + tx - 1) / tx;
-    const int tiles_y = (I.G.nb + ty - 1) / ty;
+    I.tiles_y = (I.G.nb + ty - 1) / ty;
+    I.tz = g.ndim == 3 ? std::min(I.G.nc, 16) : 1;
+    const int chunks = g.ndim == 3 ? (I.G.nc + I.tz - 1) / I.tz : 1;
     I.tile0 = t0;
     I.rs = b->p[i].riemann_solver == FV_HLL ? 0 : 1;
-    t0 += I.tiles_x * tiles_y;
+    t0 += I.tiles_x * I.tiles_y * chunks;
     out.push_back(I);
   }
   *ntiles = t0;
@@ -226,6 +241,10 @@ int SmCount() {
 // against a scratch copy of the control blocks, so the problems' state and
 // clocks are untouched.
 int Autotune(fv_batch* b, Group& g) {
+  if (g.ndim == 3) {  // one shape: the 16 x 16 column kernel
+    g.shape = 0;
+    return Occupancy(b, g, 0) > 0 ? FV_OK : Fail(b, FV_ERR_CUDA, "the 3-D batch kernel cannot be launched");
+  }
   const fv::TileShape* shapes;
   const int ns = NumShapes(b->precision, &shapes);
   if (const char* force = std::getenv("FV3D_TILE")) {
@@ -326,19 +345,23 @@ int Prepare(fv_batch* b) {
   if (b->prepared) return FV_OK;
   ReleaseGroups(b);
   for (int i = 0; i < b->n; ++i) {
+    const int ndim = b->G[i].ndim;
+    const int rs = ndim == 3 ? (b->p[i].riemann_solver == FV_HLL ? 0 : 1) : -1;
     Group* g = nullptr;
     for (auto& h : b->groups)
-      if (h.plane == b->G[i].plane && h.wact == (bool)b->wact[i]) g = &h;
+      if (h.ndim == ndim && h.rs == rs && h.plane == b->G[i].plane && h.wact == (bool)b->wact[i]) g = &h;
     if (!g) {
       b->groups.push_back(Group());
       g = &b->groups.back();
+      g->ndim = ndim;
+      g->rs = rs;
       g->plane = b->G[i].plane;
       g->wact = b->wact[i];
     }
     g->members.push_back(i);
     g->tc = g->tc || b->G[i].tc;
   }
-  if (b->groups.size() > 4) return Fail(b, FV_ERR_UNSUPPORTED, "more than 4 batch groups");
+  if ((int)b->groups.size() > kMaxGroups) return Fail(b, FV_ERR_UNSUPPORTED, "more than %d batch groups", kMaxGroups);
   for (auto& g : b->groups) {
     int rc = Autotune(b, g);
     if (rc) return rc;
@@ -437,11 +460,16 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
     std::string err;
     int rc = fv::configure_grid(q, &b->G[i], &b->inv_tc[i], &b->inv_visc[i], &b->deg_bc[i], &err);
     if (rc) return Fail(b, rc, "problem %d: %s", i, err.c_str());
-    if (b->G[i].ndim != 2)
-      return Fail(b, FV_ERR_UNSUPPORTED,
-                  "problem %d: batches run 2-D problems without z-boundary physics or corrected physics; "
-                  "use fvgpu_create", i);
-    b->wact[i] = params[i].viscosity_active ? 1 : 0;
+    if (b->G[i].ndim == 3) {
+      if (b->G[i].corrected)
+        return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: corrected physics runs with fvgpu_create", i);
+      const int n_ax[3] = {params[i].Nx, params[i].Ny, params[i].Nz};
+      const int bc_ax[3] = {params[i].boundary_x, params[i].boundary_y, params[i].boundary_z};
+      for (int a = 0; a < 3; ++a)
+        if (n_ax[a] == 1 && bc_ax[a] == FV_BC_REFLECTING)
+          return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: a reflecting one-cell axis runs with fvgpu_create", i);
+    }
+    b->wact[i] = (params[i].viscosity_active || b->G[i].ndim == 3) ? 1 : 0;
     off[i] = total;
     total += (size_t)10 * b->G[i].fstride;
     b->max_fstride = std::max(b->max_fstride, b->G[i].fstride);
@@ -450,10 +478,10 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
       cudaMalloc(&b->scratch, (size_t)5 * b->max_fstride * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&b->d_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
       cudaMallocHost(&b->h_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
-      cudaMalloc(&b->d_queue, sizeof(unsigned) * 8) != cudaSuccess)
+      cudaMalloc(&b->d_queue, sizeof(unsigned) * 2 * kMaxGroups) != cudaSuccess)
     return Fail(b, FV_ERR_NOMEM, "batch allocation of %zu bytes failed", total * sizeof(double));
   cudaMemset(b->buf, 0, total * sizeof(double));
-  cudaMemset(b->d_queue, 0, sizeof(unsigned) * 8);
+  cudaMemset(b->d_queue, 0, sizeof(unsigned) * 2 * kMaxGroups);
   b->A.resize(n);
   b->B.resize(n);
   for (int i = 0; i < n; ++i)
@@ -506,10 +534,10 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
   for (int k = 0; k < 5; ++k) src[slot_of[k]] = ref[k];
   if (!src[0] || !src[4]) return Fail(b, FV_ERR_PARAM, "density and pressure arrays are required");
   bool nonzero = false;
-  if (src[3])
-    for (long long c = 0; c < (long long)G.na * G.nb && !nonzero; ++c) nonzero = src[3][c] != 0.0;
-  const bool wact = b->p[inst].viscosity_active || nonzero;
-  if (wact && b->deg_bc[inst] == FV_BC_REFLECTING)
+  if (src[3] && G.ndim == 2)
+    for (long long c = 0; c < (long long)G.na * G.rows && !nonzero; ++c) nonzero = src[3][c] != 0.0;
+  const bool wact = b->p[inst].viscosity_active || nonzero || G.ndim == 3;
+  if (G.ndim == 2 && wact && b->deg_bc[inst] == FV_BC_REFLECTING)
     return Fail(b, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
   if ((bool)b->wact[inst] != wact) b->prepared = false;
   b->wact[inst] = wact;
@@ -522,7 +550,7 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
   const size_t rowb = (size_t)G.na * sizeof(double);
   for (int k = 0; k < 5; ++k) {
     if (src[k])
-      BCUDA(b, cudaMemcpy2DAsync(stage.f[k], (size_t)G.pitch * sizeof(double), src[k], rowb, rowb, G.nb,
+      BCUDA(b, cudaMemcpy2DAsync(stage.f[k], (size_t)G.pitch * sizeof(double), src[k], rowb, rowb, G.rows,
                                  cudaMemcpyHostToDevice, b->stream));
     else
       BCUDA(b, cudaMemsetAsync(stage.f[k], 0, (size_t)G.fstride * sizeof(double), b->stream));
@@ -562,7 +590,7 @@ int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* 
   const size_t rowb = (size_t)G.na * sizeof(double);
   for (int k = 0; k < 5; ++k)
     if (dst[k])
-      BCUDA(b, cudaMemcpy2DAsync(dst[k], rowb, S.f[k], (size_t)G.pitch * sizeof(double), rowb, G.nb,
+      BCUDA(b, cudaMemcpy2DAsync(dst[k], rowb, S.f[k], (size_t)G.pitch * sizeof(double), rowb, G.rows,
                                  cudaMemcpyDeviceToHost, b->stream));
   BCUDA(b, cudaStreamSynchronize(b->stream));
   return FV_OK;
@@ -661,8 +689,9 @@ int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_grou
   NumShapes(b->precision, &shapes);
   *ngroups = (int)b->groups.size();
   for (int g = 0; g < *ngroups && g < max_groups; ++g) {
-    if (tx) tx[g] = shapes[b->groups[g].shape].tx;
-    if (ty) ty[g] = shapes[b->groups[g].shape].ty;
+    const bool d3 = b->groups[g].ndim == 3;
+    if (tx) tx[g] = d3 ? fv::batch3d_columns() : shapes[b->groups[g].shape].tx;
+    if (ty) ty[g] = d3 ? fv::batch3d_columns() : shapes[b->groups[g].shape].ty;
   }
   return FV_OK;
 }

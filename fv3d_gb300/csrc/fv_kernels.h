@@ -100,6 +100,8 @@ struct BatchInst {
   int tiles_x;  // tiles along a
   int tile0;    // first tile of this problem in its group's tile numbering
   int rs;       // 0 HLL, 1 HLLC
+  int tiles_y;  // tiles along b (3-D: column blocks along y)
+  int tz;       // 3-D: z layers per work item (work item = column block x z chunk)
   int pad;
 };
 
@@ -122,6 +124,19 @@ cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchIns
 // Resident CTAs per SM of one batch stage kernel (0 on error).
 int batch_stage_occupancy64(int plane, bool wact, int shape, bool tc);
 int batch_stage_occupancy32(int plane, bool wact, int shape, bool tc);
+
+// Persistent stage kernels for groups of 3-D problems sharing a Riemann
+// solver (rs): a work item is a 16 x 16 column block and a chunk of tz z
+// layers of one problem (numbered x fastest, then y, then z); same body as
+// launch_stage3d, so a problem in a batch is bit-identical to the same
+// problem alone (FP64).
+int batch3d_columns();  // column-block side (16)
+cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
+                                   int rs, int grid, bool tc, cudaStream_t stream);
+cudaError_t launch_batch_stage3d32(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
+                                   int rs, int grid, bool tc, cudaStream_t stream);
+int batch_stage3d_occupancy64(bool tc);
+int batch_stage3d_occupancy32(bool tc);
 
 // launch_control for n problems plus a reset of nq work-queue counters.
 cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override, double dt_given,

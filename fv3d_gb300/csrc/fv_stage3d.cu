@@ -212,95 +212,6 @@ __device__ __forceinline__ void face3(const double c[4][5], int rs, int recon, c
   unslot3<DIR>(f, out);
 }
 
-// Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
-// including its z-branch index and field mix-ups (CORR: the z branch as the
-// mirror of the x / y branches instead).  P(dk, dj, di, var) reads velocity
-// var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x), i.e.
-// stencil[dk][dj][di][var].
-template <bool CORR, class PA>
-__device__ __forceinline__ void viscous3d(const PA& P, double odx, double ody, double odz, double mu,
-                                          double vf[3][5]) {
-  const double four_thirds = 4.0 / 3.0;
-  const double two_thirds = 2.0 / 3.0;
-  const double c4x = half64(half64(odx)), c4y = half64(half64(ody)), c4z = half64(half64(odz));
-  const int U = 1, V = 2, W = 3;
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-#pragma unroll
-    for (int v = 0; v < 5; ++v) vf[d][v] = 0.0;
-#pragma unroll
-  for (int s = 1; s < 3; ++s) {  // IX
-    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = half64(P(1, 1, s, U) + P(1, 1, s - 1, U));
-    const double qiv = half64(P(1, 1, s, V) + P(1, 1, s - 1, V));
-    const double qiw = half64(P(1, 1, s, W) + P(1, 1, s - 1, W));
-    const double dudx = odx * (P(1, 1, s, U) - P(1, 1, s - 1, U));
-    const double dvdx = odx * (P(1, 1, s, V) - P(1, 1, s - 1, V));
-    const double dwdx = odx * (P(1, 1, s, W) - P(1, 1, s - 1, W));
-    const double dudy = c4y * (P(1, 2, s, U) - P(1, 0, s, U) + P(1, 2, s - 1, U) - P(1, 0, s - 1, U));
-    const double dvdy = c4y * (P(1, 2, s, V) - P(1, 0, s, V) + P(1, 2, s - 1, V) - P(1, 0, s - 1, V));
-    const double dudz = c4z * (P(2, 1, s, U) - P(0, 1, s, U) + P(2, 1, s - 1, U) - P(0, 1, s - 1, U));
-    const double dwdz = c4z * (P(2, 1, s, W) - P(0, 1, s, W) + P(2, 1, s - 1, W) - P(0, 1, s - 1, W));
-    const double tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
-    const double tau_xy = dvdx + dudy;
-    const double tau_xz = dwdx + dudz;
-    vf[0][1] += sm * tau_xx;
-    vf[0][2] += sm * tau_xy;
-    vf[0][3] += sm * tau_xz;
-    vf[0][4] += sm * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
-  }
-#pragma unroll
-  for (int s = 1; s < 3; ++s) {  // IY
-    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = half64(P(1, s, 1, U) + P(1, s - 1, 1, U));
-    const double qiv = half64(P(1, s, 1, V) + P(1, s - 1, 1, V));
-    const double qiw = half64(P(1, s, 1, W) + P(1, s - 1, 1, W));
-    const double dudy = ody * (P(1, s, 1, U) - P(1, s - 1, 1, U));
-    const double dvdy = ody * (P(1, s, 1, V) - P(1, s - 1, 1, V));
-    const double dwdy = ody * (P(1, s, 1, W) - P(1, s - 1, 1, W));
-    const double dudx = c4x * (P(1, s, 2, U) - P(1, s, 0, U) + P(1, s - 1, 2, U) - P(1, s - 1, 0, U));
-    const double dvdx = c4x * (P(1, s, 2, V) - P(1, s, 0, V) + P(1, s - 1, 2, V) - P(1, s - 1, 0, V));
-    const double dwdz = c4z * (P(2, s, 1, W) - P(0, s, 1, W) + P(2, s - 1, 1, W) - P(0, s - 1, 1, W));
-    const double dvdz = c4z * (P(2, s, 1, V) - P(0, s, 1, V) + P(2, s - 1, 1, V) - P(0, s - 1, 1, V));
-    const double tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
-    const double tau_xy = dvdx + dudy;
-    const double tau_yz = dvdz + dwdy;
-    vf[1][1] += sm * tau_xy;
-    vf[1][2] += sm * tau_yy;
-    vf[1][3] += sm * tau_yz;
-    vf[1][4] += sm * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
-  }
-#pragma unroll
-  for (int s = 1; s < 3; ++s) {  // IZ, with the reference's mix-ups
-    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
-    const double qiu = half64(P(s, 1, 1, U) + P(s - 1, 1, 1, U));
-    const double qiv = half64(P(s, 1, 1, V) + P(s - 1, 1, 1, V));
-    const double qiw = half64(P(s, 1, 1, W) + P(s - 1, 1, 1, W));
-    const double dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
-    const double dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
-    const double dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
-    double dudx, dwdx, dvdy, dwdy;
-    if (CORR) {
-      dudx = c4x * (P(s, 1, 2, U) - P(s, 1, 0, U) + P(s - 1, 1, 2, U) - P(s - 1, 1, 0, U));
-      dwdx = c4x * (P(s, 1, 2, W) - P(s, 1, 0, W) + P(s - 1, 1, 2, W) - P(s - 1, 1, 0, W));
-      dvdy = c4y * (P(s, 2, 1, V) - P(s, 0, 1, V) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, V));
-      dwdy = c4y * (P(s, 2, 1, W) - P(s, 0, 1, W) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, W));
-    } else {
-      dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
-      dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
-      dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
-      dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
-    }
-    const double tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
-    const double tau_xz = dudz + dwdx;
-    const double tau_yz = dvdz + dwdy;
-    vf[2][1] += sm * tau_xz;
-    vf[2][2] += sm * tau_yz;
-    vf[2][3] += sm * tau_zz;
-    vf[2][4] += sm * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
-  }
-}
-
 // Stencil accessor of viscous3d over the ring (column (hy, hx) of layer k).
 struct RingVel {
   Smem3 S;
@@ -310,16 +221,19 @@ struct RingVel {
   }
 };
 
-// One stage for the CTA's columns and z chunk; P2: every cell size is a
-// power of two (the kernel branches on it once, uniformly).
-template <int RS, int KIND, bool P2, bool CORR>
+// One stage for the columns (bx, by) and z chunk bz of tz layers; rs 0 HLL /
+// 1 HLLC, kind a StageKind (constants in the one-problem kernel, per work
+// item in the batch kernel); P2: every cell size is a power of two (callers
+// branch on it once, uniformly).  Every thread of the CTA must call it.
+template <bool P2, bool CORR>
 __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
-                                             StepCtrl* __restrict__ ctrl, int tz, const Fields& hout,
-                                             double* smem_raw, unsigned long long* s_red) {
+                                             StepCtrl* __restrict__ ctrl, int rs, int kind, int bx, int by, int bz,
+                                             int tz, const Fields& hout, double* smem_raw,
+                                             unsigned long long* s_red) {
   const Smem3 S{smem_raw};
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
-  const int k0 = blockIdx.z * tz;
+  const int x0 = bx * kTX, y0 = by * kTY;
+  const int k0 = bz * tz;
   const int k1 = min(k0 + tz, G.nc);
   const int cx = tid % kTX, cy = tid / kTX;
   const int x = x0 + cx, y = y0 + cy;
@@ -328,7 +242,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
   const long long zstride = (long long)G.nb * G.pitch;
 
   if (!ctrl->active) {
-    if (KIND == STAGE_EULER && own) {
+    if (kind == STAGE_EULER && own) {
       for (int k = k0; k < k1; ++k) {
         const long long o = k * zstride + col;
 #pragma unroll
@@ -340,7 +254,6 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
   const double dt = ctrl->dt_cur;
   const int parity = ctrl->parity;
   const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
-  const int rs = RS;
   const int recon = G.recon;
   const bool need_pout = G.wb_flux_z || G.bc_c == DBC_C91;
 
@@ -478,7 +391,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
       if (G.visc) {  // Viscosity.h:145-151
         const RingVel P{S, k, cy + 2, cx + 2};
         double vf[3][5];
-        viscous3d<CORR>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
+        viscous3d<CORR, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
         if (CORR) {  // the flux differences divided by the cell sizes
 #pragma unroll
           for (int v = 1; v < 5; ++v)
@@ -489,13 +402,13 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
           for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
         }
       }
-      if (KIND == STAGE_RK_2) {
+      if (kind == STAGE_RK_2) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) un[v] = half64(u0.f[v][o] + un[v]);
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) uout.f[v][o] = un[v];
-      if (KIND != STAGE_RK_1) {
+      if (kind != STAGE_RK_1) {
         double q[5];
         const double inv = inv_dt_hyp64<PLANE_XY, true, P2>(un, G, q);
         const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
@@ -514,7 +427,7 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
     }
     __syncthreads();
   }
-  if (KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+  if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
 template <int RS, int KIND, bool CORR>
@@ -524,9 +437,11 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
   if (G.pow2_all)
-    stage3d_body<RS, KIND, true, CORR>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
+    stage3d_body<true, CORR>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, blockIdx.z, tz, hout,
+                             smem_raw, s_red);
   else
-    stage3d_body<RS, KIND, false, CORR>(G, uin, u0, uout, ctrl, tz, hout, smem_raw, s_red);
+    stage3d_body<false, CORR>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, blockIdx.z, tz, hout,
+                              smem_raw, s_red);
 }
 
 template <int RS, int KIND, bool CORR>
@@ -564,7 +479,103 @@ cudaError_t launch_phys(const Grid& G, int kind, Fields uin, Fields u0, Fields u
                      : launch_kind<RS, false>(G, kind, uin, u0, uout, ctrl, hout, st);
 }
 
+static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
+
+// Persistent FP64 kernel over a group of 3-D problems (see
+// launch_batch_stage3d64): CTAs take work items from the queue counter, find
+// their problem by binary search over the first item numbers, and run the
+// same body as the one-problem kernel.
+template <int KIND, int RS>
+__global__ void __launch_bounds__(kThreads, 2)
+batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int flip) {
+  const int kind = KIND;
+  extern __shared__ double smem_raw[];
+  __shared__ unsigned long long s_red[kThreads / 32];
+  __shared__ BatchInst s_inst;
+  __shared__ int s_tile;
+  const Fields none{};
+  for (;;) {
+    __syncthreads();  // the previous item is finished with s_tile, s_inst and smem
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) break;
+    {
+      int lo = 0, hi = ninst - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (insts[mid].tile0 <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      const unsigned long long* src = reinterpret_cast<const unsigned long long*>(insts + lo);
+      unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s_inst);
+      for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
+    }
+    __syncthreads();
+    const BatchInst& I = s_inst;
+    const int lt = t - I.tile0;
+    const int per_layer = I.tiles_x * I.tiles_y;
+    const int bz = lt / per_layer, rem = lt - bz * per_layer;
+    const int by = rem / I.tiles_x, bx = rem - by * I.tiles_x;
+    Fields uin, u0, uout;
+    if (kind == STAGE_RK_1) {
+      uin = I.A; u0 = I.A; uout = I.B;
+    } else if (kind == STAGE_RK_2) {
+      uin = I.B; u0 = I.A; uout = I.A;
+    } else {
+      uin = flip ? I.B : I.A; u0 = uin; uout = flip ? I.A : I.B;
+    }
+    // the group shares the solver (RS); the cell-size form is a uniform branch
+    if (I.G.pow2_all)
+      stage3d_body<true, false>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
+    else
+      stage3d_body<false, false>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
+  }
+}
+
+typedef void (*Batch3dKernel)(const BatchInst*, int, int, unsigned*, int);
+
+template <int RS>
+Batch3dKernel batch3d_kernel_rs(int kind) {
+  return kind == STAGE_EULER ? batch_stage3d64<STAGE_EULER, RS>
+                             : (kind == STAGE_RK_1 ? batch_stage3d64<STAGE_RK_1, RS> : batch_stage3d64<STAGE_RK_2, RS>);
+}
+
+Batch3dKernel batch3d_kernel(int kind, int rs) {
+  return rs == 0 ? batch3d_kernel_rs<0>(kind) : batch3d_kernel_rs<1>(kind);
+}
+
+bool batch3d_prepare() {
+  static bool done = false;
+  if (done) return true;
+  for (int rs = 0; rs < 2; ++rs)
+    for (int k = 0; k < 3; ++k)
+      if (cudaFuncSetAttribute(batch3d_kernel(k, rs), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)Smem3::bytes(true)) != cudaSuccess)
+        return false;
+  done = true;
+  return true;
+}
+
 }  // namespace
+
+int batch3d_columns() { return kTX; }
+
+int batch_stage3d_occupancy64(bool tc) {
+  if (!batch3d_prepare()) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch3d_kernel(STAGE_RK_2, 1), kThreads, Smem3::bytes(tc)) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+
+cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
+                                   int rs, int grid, bool tc, cudaStream_t st) {
+  if (!batch3d_prepare()) return cudaErrorInvalidConfiguration;
+  batch3d_kernel(kind, rs)<<<grid, kThreads, Smem3::bytes(tc), st>>>(insts, ninst, ntiles, queue, flip);
+  return cudaGetLastError();
+}
 
 // z layers per CTA: enough CTAs to fill two waves of 2 CTAs on each of the
 // 152 SMs where the grid allows, at least 4 layers (the prologue loads four

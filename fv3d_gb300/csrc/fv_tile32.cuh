@@ -121,11 +121,13 @@ __device__ __forceinline__ State32 state32(const Slots<float>& q, float gamma, f
 
 // HLL with Davis wave speeds (RiemannSolvers.h:6-36) in FP32.  The conserved
 // states of the star formula are (r, F0 = r un, r t1, r t2, E).
+// pout (optional): the interface pressure of RiemannSolvers.h:24-33.
 __device__ __forceinline__ void hll32(const Slots<float>& qL, const Slots<float>& qR, float gamma, float inv_gm1,
-                                      float flux[5]) {
+                                      float flux[5], float* pout = nullptr) {
   const State32 L = state32(qL, gamma, inv_gm1), R = state32(qR, gamma, inv_gm1);
   const float SL = fminf(L.un - L.c, R.un - R.c);
   const float SR = fmaxf(L.un + L.c, R.un + R.c);
+  if (pout) *pout = SL >= 0.0f ? L.p : (SR <= 0.0f ? R.p : 0.5f * (L.p + R.p));
   if (SL >= 0.0f) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) flux[v] = L.F[v];
@@ -144,10 +146,15 @@ __device__ __forceinline__ void hll32(const Slots<float>& qL, const Slots<float>
 
 // HLLC (RiemannSolvers.h:39-112) in FP32; the energy uses the normal and
 // first transverse velocity only, as the reference does.
+// pout (optional): the interface pressure of RiemannSolvers.h:81-104.
+// KE3: the kinetic energy of all three velocities (corrected physics).
+template <bool KE3 = false>
 __device__ __forceinline__ void hllc32(const Slots<float>& L, const Slots<float>& R, float gamma, float inv_gm1,
-                                       float flux[5]) {
-  const float EL = 0.5f * L.r * (L.un * L.un + L.t1 * L.t1) + L.p * inv_gm1;
-  const float ER = 0.5f * R.r * (R.un * R.un + R.t1 * R.t1) + R.p * inv_gm1;
+                                       float flux[5], float* pout = nullptr) {
+  const float kL = KE3 ? L.un * L.un + L.t1 * L.t1 + L.t2 * L.t2 : L.un * L.un + L.t1 * L.t1;
+  const float kR = KE3 ? R.un * R.un + R.t1 * R.t1 + R.t2 * R.t2 : R.un * R.un + R.t1 * R.t1;
+  const float EL = 0.5f * L.r * kL + L.p * inv_gm1;
+  const float ER = 0.5f * R.r * kR + R.p * inv_gm1;
   const float cmax = sqrtf(gamma * fmaxf(L.p / L.r, R.p / R.r));
   const float SL = fminf(L.un, R.un) - cmax;
   const float SR = fmaxf(L.un, R.un) + cmax;
@@ -172,6 +179,7 @@ __device__ __forceinline__ void hllc32(const Slots<float>& L, const Slots<float>
   } else {
     sr = R.r; su = R.un; st1 = R.t1; st2 = R.t2; sp = R.p; E = ER;
   }
+  if (pout) *pout = sp;
   flux[0] = sr * su;
   flux[1] = flux[0] * su + sp;
   flux[2] = flux[0] * st1;

@@ -453,4 +453,93 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
   if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
+// Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
+// including its z-branch index and field mix-ups (CORR: the z branch as the
+// mirror of the x / y branches instead).  P(dk, dj, di, var) reads velocity
+// var (1 u, 2 v, 3 w) at offset (dk-1, dj-1, di-1) along (z, y, x), i.e.
+// stencil[dk][dj][di][var].
+template <bool CORR, class T, class PA>
+__device__ __forceinline__ void viscous3d(const PA& P, T odx, T ody, T odz, T mu, T vf[3][5]) {
+  const T four_thirds = T(4.0 / 3.0);
+  const T two_thirds = T(2.0 / 3.0);
+  const T c4x = half_of(half_of(odx)), c4y = half_of(half_of(ody)), c4z = half_of(half_of(odz));
+  const int U = 1, V = 2, W = 3;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) vf[d][v] = T(0);
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IX
+    const T sm = (s == 1 ? T(-1) : T(1)) * mu;
+    const T qiu = half_of(P(1, 1, s, U) + P(1, 1, s - 1, U));
+    const T qiv = half_of(P(1, 1, s, V) + P(1, 1, s - 1, V));
+    const T qiw = half_of(P(1, 1, s, W) + P(1, 1, s - 1, W));
+    const T dudx = odx * (P(1, 1, s, U) - P(1, 1, s - 1, U));
+    const T dvdx = odx * (P(1, 1, s, V) - P(1, 1, s - 1, V));
+    const T dwdx = odx * (P(1, 1, s, W) - P(1, 1, s - 1, W));
+    const T dudy = c4y * (P(1, 2, s, U) - P(1, 0, s, U) + P(1, 2, s - 1, U) - P(1, 0, s - 1, U));
+    const T dvdy = c4y * (P(1, 2, s, V) - P(1, 0, s, V) + P(1, 2, s - 1, V) - P(1, 0, s - 1, V));
+    const T dudz = c4z * (P(2, 1, s, U) - P(0, 1, s, U) + P(2, 1, s - 1, U) - P(0, 1, s - 1, U));
+    const T dwdz = c4z * (P(2, 1, s, W) - P(0, 1, s, W) + P(2, 1, s - 1, W) - P(0, 1, s - 1, W));
+    const T tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
+    const T tau_xy = dvdx + dudy;
+    const T tau_xz = dwdx + dudz;
+    vf[0][1] += sm * tau_xx;
+    vf[0][2] += sm * tau_xy;
+    vf[0][3] += sm * tau_xz;
+    vf[0][4] += sm * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+  }
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IY
+    const T sm = (s == 1 ? T(-1) : T(1)) * mu;
+    const T qiu = half_of(P(1, s, 1, U) + P(1, s - 1, 1, U));
+    const T qiv = half_of(P(1, s, 1, V) + P(1, s - 1, 1, V));
+    const T qiw = half_of(P(1, s, 1, W) + P(1, s - 1, 1, W));
+    const T dudy = ody * (P(1, s, 1, U) - P(1, s - 1, 1, U));
+    const T dvdy = ody * (P(1, s, 1, V) - P(1, s - 1, 1, V));
+    const T dwdy = ody * (P(1, s, 1, W) - P(1, s - 1, 1, W));
+    const T dudx = c4x * (P(1, s, 2, U) - P(1, s, 0, U) + P(1, s - 1, 2, U) - P(1, s - 1, 0, U));
+    const T dvdx = c4x * (P(1, s, 2, V) - P(1, s, 0, V) + P(1, s - 1, 2, V) - P(1, s - 1, 0, V));
+    const T dwdz = c4z * (P(2, s, 1, W) - P(0, s, 1, W) + P(2, s - 1, 1, W) - P(0, s - 1, 1, W));
+    const T dvdz = c4z * (P(2, s, 1, V) - P(0, s, 1, V) + P(2, s - 1, 1, V) - P(0, s - 1, 1, V));
+    const T tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
+    const T tau_xy = dvdx + dudy;
+    const T tau_yz = dvdz + dwdy;
+    vf[1][1] += sm * tau_xy;
+    vf[1][2] += sm * tau_yy;
+    vf[1][3] += sm * tau_yz;
+    vf[1][4] += sm * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+  }
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {  // IZ, with the reference's mix-ups
+    const T sm = (s == 1 ? T(-1) : T(1)) * mu;
+    const T qiu = half_of(P(s, 1, 1, U) + P(s - 1, 1, 1, U));
+    const T qiv = half_of(P(s, 1, 1, V) + P(s - 1, 1, 1, V));
+    const T qiw = half_of(P(s, 1, 1, W) + P(s - 1, 1, 1, W));
+    const T dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
+    const T dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
+    const T dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
+    T dudx, dwdx, dvdy, dwdy;
+    if (CORR) {
+      dudx = c4x * (P(s, 1, 2, U) - P(s, 1, 0, U) + P(s - 1, 1, 2, U) - P(s - 1, 1, 0, U));
+      dwdx = c4x * (P(s, 1, 2, W) - P(s, 1, 0, W) + P(s - 1, 1, 2, W) - P(s - 1, 1, 0, W));
+      dvdy = c4y * (P(s, 2, 1, V) - P(s, 0, 1, V) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, V));
+      dwdy = c4y * (P(s, 2, 1, W) - P(s, 0, 1, W) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, W));
+    } else {
+      dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
+      dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
+      dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
+      dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
+    }
+    const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+    const T tau_xz = dudz + dwdx;
+    const T tau_yz = dvdz + dwdy;
+    vf[2][1] += sm * tau_xz;
+    vf[2][2] += sm * tau_yz;
+    vf[2][3] += sm * tau_zz;
+    vf[2][4] += sm * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+  }
+}
+
+
 }  // namespace fv
