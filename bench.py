@@ -499,7 +499,13 @@ def run_variants(torch, args, flush):
     # and a 3-D PLM / RK2 / conduction + viscosity run at 192^3 (3-D kernel)
     bl = problems.blast(256)
     add("blast_3d_256_fp64", time_sim(torch, bl, 4, 2), 80)  # Euler: read + write 5 fields
-    add("random_3d_192_plm_rk2_tc_visc_fp64", time_sim(torch, random_3d(192), 2, 1), 200)
+    _, r = time_batch(torch, [_mixed(bl.params)], [bl.prim], 16, 4)
+    # Euler in the mixed form: read U^n pairs, write U^n+1 pairs, 5 fields: 80 B
+    add("blast_3d_256_fp32_mixed", r, 80, l1_vs_fp64(torch, [bl], 40, [_mixed(bl.params)]))
+    r3 = random_3d(192)
+    add("random_3d_192_plm_rk2_tc_visc_fp64", time_sim(torch, r3, 2, 1), 200)
+    _, r = time_batch(torch, [_mixed(r3.params)], [r3.prim], 8, 2)
+    add("random_3d_192_plm_rk2_tc_visc_fp32_mixed", r, 160, l1_vs_fp64(torch, [r3], 10, [_mixed(r3.params)]))
 
     # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
     sh = problems.shear_layer(4096)
