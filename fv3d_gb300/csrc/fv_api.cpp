@@ -61,7 +61,16 @@ struct fv_sim {
   cudaGraphExec_t graph = nullptr;
   const void* graph_key = nullptr;
   cudaStream_t graph_stream = nullptr;
+  fv_batch* mixed = nullptr;  // FP32-mixed form: the problem is a batch of one
 };
+
+namespace fv {
+const char* batch_error(const fv_batch* b);
+int batch_compute_dt(fv_batch* b, int i, double* dt, double inv[3]);
+int batch_step_dt(fv_batch* b, double dt);
+int batch_advance(fv_batch* b, double tend, long max_steps, double* t, long* nsteps);
+int batch_totals(fv_batch* b, int i, double out[5]);
+}  // namespace fv
 
 namespace {
 
@@ -175,8 +184,7 @@ int Configure(fv_sim* s) {
   if (p.Ng < 2) return Fail(s, FV_ERR_PARAM, "Nghosts must be >= 2 (slopes read two cells out)");
   if (!(p.dx > 0 && p.dy > 0 && p.dz > 0)) return Fail(s, FV_ERR_PARAM, "cell sizes must be positive");
   if (!(p.gamma0 > 1.0)) return Fail(s, FV_ERR_PARAM, "gamma0 must be > 1");
-  if (p.precision != FV_PREC_FP64)
-    return Fail(s, FV_ERR_UNSUPPORTED, "fvgpu_create runs the FP64 form; the FP32-mixed form is batch-only");
+  if (p.precision != FV_PREC_FP64) return Fail(s, FV_ERR_UNSUPPORTED, "unknown precision");
   if (p.thermal_conductivity_active && p.thermal_conductivity_mode != FV_TCM_CONSTANT && !B02(p))
     return Fail(s, FV_ERR_UNSUPPORTED, "unknown thermal conductivity mode");
   const bool tc_z = p.thermal_conductivity_active && (B02(p) || p.bctc_zmin != FV_BCTC_NONE ||
@@ -259,6 +267,13 @@ int Configure(fv_sim* s) {
   SetExactConstants(G);
   DtConstants(p, &s->inv_tc, &s->inv_visc);
   return FV_OK;
+}
+
+// The FP32-mixed handle forwards to its batch of one; a failure's message is
+// copied to the handle.
+int Mixed(fv_sim* s, int rc) {
+  if (rc != FV_OK) s->err = fv::batch_error(s->mixed);
+  return rc;
 }
 
 Fields StateAt(double* base, long long fstride) {
@@ -484,6 +499,17 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
   *out = nullptr;
   fv_sim* s = new fv_sim();
   s->p = *params;
+  if (params->precision == FV_PREC_FP32_MIXED) {
+    // the FP32-mixed form runs through the batch machinery (2-D or 3-D)
+    *out = s;
+    const int rc = fvgpu_batch_create(params, 1, &s->mixed);
+    if (rc != FV_OK) {
+      s->err = fv::batch_error(s->mixed);
+      fvgpu_batch_destroy(s->mixed);
+      s->mixed = nullptr;
+    }
+    return rc;
+  }
   int rc = Configure(s);
   if (rc != FV_OK) {
     // keep the handle so the caller can read the message, but mark it unusable
@@ -537,6 +563,7 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
 
 int fvgpu_destroy(fv_sim* s) {
   if (!s) return FV_OK;
+  if (s->mixed) fvgpu_batch_destroy(s->mixed);
   if (s->stream) cudaStreamSynchronize(s->stream);
   ResetGraph(s);
   if (s->buf) cudaFree(s->buf);
@@ -556,6 +583,7 @@ const char* fvgpu_last_error(const fv_sim* s) { return s ? s->err.c_str() : "nul
 
 int fvgpu_set_prim(fv_sim* s, const double* rho, const double* u, const double* v, const double* w,
                    const double* p) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_set_prim(s->mixed, 0, rho, u, v, w, p));
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   const double* f[5] = {rho, u, v, w, p};
   return SetState(s, f, true);
@@ -563,12 +591,15 @@ int fvgpu_set_prim(fv_sim* s, const double* rho, const double* u, const double* 
 
 int fvgpu_set_cons(fv_sim* s, const double* rho, const double* mx, const double* my, const double* mz,
                    const double* E) {
+  if (s && s->mixed)
+    return Fail(s, FV_ERR_UNSUPPORTED, "the FP32-mixed handle takes primitive states (fvgpu_set_prim)");
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   const double* f[5] = {rho, mx, my, mz, E};
   return SetState(s, f, false);
 }
 
 int fvgpu_get_prim(fv_sim* s, double* rho, double* u, double* v, double* w, double* p) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_get_prim(s->mixed, 0, rho, u, v, w, p));
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   int slot_of[5];
@@ -589,6 +620,8 @@ int fvgpu_get_prim(fv_sim* s, double* rho, double* u, double* v, double* w, doub
 }
 
 int fvgpu_get_cons(fv_sim* s, double* rho, double* mx, double* my, double* mz, double* E) {
+  if (s && s->mixed)
+    return Fail(s, FV_ERR_UNSUPPORTED, "the FP32-mixed handle returns primitive states (fvgpu_get_prim)");
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   int slot_of[5];
@@ -606,6 +639,22 @@ int fvgpu_get_cons(fv_sim* s, double* rho, double* mx, double* my, double* mz, d
 
 int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double* const prim_out[5],
                     double* dt_used) {
+  if (s && s->mixed) {  // staged copies through the batch calls
+    if (!prim_in) return Fail(s, FV_ERR_PARAM, "null argument");
+    int rc = Mixed(s, fvgpu_batch_set_prim(s->mixed, 0, prim_in[0], prim_in[1], prim_in[2], prim_in[3], prim_in[4]));
+    if (rc) return rc;
+    double d = dt;
+    if (!(dt > 0.0)) {
+      rc = Mixed(s, fv::batch_compute_dt(s->mixed, 0, &d, nullptr));
+      if (rc) return rc;
+    }
+    rc = Mixed(s, fv::batch_step_dt(s->mixed, d));
+    if (rc) return rc;
+    if (dt_used) *dt_used = d;
+    if (!prim_out) return Mixed(s, fvgpu_batch_synchronize(s->mixed));
+    return Mixed(s, fvgpu_batch_get_prim(s->mixed, 0, prim_out[0], prim_out[1], prim_out[2], prim_out[3],
+                                         prim_out[4]));
+  }
   if (!s || !s->buf || !prim_in) return s ? Fail(s, FV_ERR_PARAM, "null argument or unconfigured handle")
                                           : FV_ERR_PARAM;
   int slot_of[5];
@@ -663,6 +712,7 @@ int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double
 }
 
 int fvgpu_compute_dt(fv_sim* s, double* dt, double inv[3]) {
+  if (s && s->mixed) return Mixed(s, fv::batch_compute_dt(s->mixed, 0, dt, inv));
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   int rc = EnsureSlot(s);
@@ -691,6 +741,7 @@ int fvgpu_compute_dt(fv_sim* s, double* dt, double inv[3]) {
 }
 
 int fvgpu_step(fv_sim* s, double dt) {
+  if (s && s->mixed) return Mixed(s, fv::batch_step_dt(s->mixed, dt));
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   // stream-ordered and asynchronous: the control kernel takes dt as an argument
@@ -702,6 +753,7 @@ int fvgpu_step(fv_sim* s, double dt) {
 }
 
 int fvgpu_enqueue_steps(fv_sim* s, long nsteps) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_run(s->mixed, nsteps));
   if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   if (nsteps < 0) return Fail(s, FV_ERR_PARAM, "nsteps must be >= 0");
@@ -717,6 +769,7 @@ int fvgpu_enqueue_steps(fv_sim* s, long nsteps) {
 }
 
 int fvgpu_advance(fv_sim* s, double tend, long max_steps, double* t, long* nsteps) {
+  if (s && s->mixed && t) return Mixed(s, fv::batch_advance(s->mixed, tend, max_steps, t, nsteps));
   if (!s || !s->buf || !t) return s ? Fail(s, FV_ERR_PARAM, "null argument") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   int rc = EnsureSlot(s);
@@ -793,6 +846,7 @@ int fvgpu_advance(fv_sim* s, double tend, long max_steps, double* t, long* nstep
 }
 
 int fvgpu_conserved_totals(fv_sim* s, double out[5]) {
+  if (s && s->mixed && out) return Mixed(s, fv::batch_totals(s->mixed, 0, out));
   if (!s || !s->buf || !out) return s ? Fail(s, FV_ERR_PARAM, "null argument") : FV_ERR_PARAM;
   if (!s->state_set) return Fail(s, FV_ERR_STATE, "no state set");
   int nb = 0;
@@ -824,6 +878,7 @@ int fvgpu_conserved_totals(fv_sim* s, double out[5]) {
 }
 
 int fvgpu_set_stream(fv_sim* s, void* stream) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_set_stream(s->mixed, stream));
   if (!s) return FV_ERR_PARAM;
   if (s->stream) cudaStreamSynchronize(s->stream);
   s->stream = stream ? (cudaStream_t)stream : s->own_stream;
@@ -832,18 +887,22 @@ int fvgpu_set_stream(fv_sim* s, void* stream) {
 }
 
 int fvgpu_synchronize(fv_sim* s) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_synchronize(s->mixed));
   if (!s) return FV_ERR_PARAM;
   CUDA_TRY(s, cudaStreamSynchronize(s->stream));
   return FV_OK;
 }
 
 int fvgpu_launch_count(const fv_sim* s, long* count) {
+  if (s && s->mixed) return fvgpu_batch_launch_count(s->mixed, count);
   if (!s || !count) return FV_ERR_PARAM;
   *count = s->launches;
   return FV_OK;
 }
 
 int fvgpu_profile_enable(fv_sim* s, int enable) {
+  if (s && s->mixed && enable)
+    return Fail(s, FV_ERR_UNSUPPORTED, "per-kernel timing is not built for the FP32-mixed handle");
   if (!s) return FV_ERR_PARAM;
   if (s->stream) cudaStreamSynchronize(s->stream);
   s->profile = enable != 0;

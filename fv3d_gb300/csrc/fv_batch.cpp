@@ -82,6 +82,7 @@ struct fv_batch {
   int flip = 0;  // Euler: current states are in B
   cudaStream_t own_stream = nullptr, stream = nullptr;
   cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph_loop = nullptr;  // steps in each control block's own mode
   long launches = 0;
   std::string err;
 };
@@ -335,7 +336,9 @@ void ReleaseGroups(fv_batch* b) {
     if (g.d_inst) cudaFree(g.d_inst);
   b->groups.clear();
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_loop) cudaGraphExecDestroy(b->graph_loop);
   b->graph = nullptr;
+  b->graph_loop = nullptr;
   b->prepared = false;
 }
 
@@ -409,9 +412,11 @@ int KernelsPerStep(const fv_batch* b) {
 }
 
 // Control + stages of one step for every group.
-int EnqueueStep(fv_batch* b) {
+// mode_override: 2 = CFL dt, no time bound (fvgpu_batch_run); 0 = the given
+// dt; -1 = each control block's own mode (the main.cpp loop of batch_advance).
+int EnqueueStep(fv_batch* b, int mode_override = 2, double dt = 0.0) {
   const int nq = 2 * (int)b->groups.size();
-  cudaError_t e = fv::launch_batch_control(b->d_ctrl, b->n, b->d_queue, nq, 2, 0.0, b->stream);
+  cudaError_t e = fv::launch_batch_control(b->d_ctrl, b->n, b->d_queue, nq, mode_override, dt, b->stream);
   for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
     const Group& g = b->groups[gi];
     unsigned* q = b->d_queue + 2 * gi;
@@ -663,7 +668,9 @@ int fvgpu_batch_set_stream(fv_batch* b, void* stream) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   b->stream = stream ? (cudaStream_t)stream : b->own_stream;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_loop) cudaGraphExecDestroy(b->graph_loop);
   b->graph = nullptr;
+  b->graph_loop = nullptr;
   return FV_OK;
 }
 
@@ -697,3 +704,158 @@ int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_grou
 }
 
 }  // extern "C"
+
+// ---- one problem through the batch machinery --------------------------------
+// fvgpu_create hands a problem in the FP32-mixed form to a batch of one; these
+// give that handle the single-problem calls the batch API does not have.
+
+namespace fv {
+
+const char* batch_error(const fv_batch* b) { return b ? b->err.c_str() : "null handle"; }
+
+// ComputeDtFunctor::computeDt of problem i's current state.
+int batch_compute_dt(fv_batch* b, int i, double* dt, double inv[3]) {
+  if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "no state set");
+  int rc = Prepare(b);
+  if (rc) return rc;
+  rc = EnsureSlots(b);
+  if (rc) return rc;
+  rc = ReadCtrl(b);
+  if (rc) return rc;
+  const StepCtrl& c = b->h_ctrl[i];
+  double inv_hyp;
+  const unsigned long long bits = c.slot[c.step & 1];
+  std::memcpy(&inv_hyp, &bits, sizeof(inv_hyp));
+  double m = inv_hyp;
+  if (b->inv_tc[i] > m) m = b->inv_tc[i];
+  if (b->inv_visc[i] > m) m = b->inv_visc[i];
+  const double d = b->p[i].CFL / m;
+  if (inv) {
+    inv[0] = inv_hyp;
+    inv[1] = b->inv_tc[i];
+    inv[2] = b->inv_visc[i];
+  }
+  if (dt) *dt = d;
+  if (c.err || !std::isfinite(d)) return Fail(b, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
+  return FV_OK;
+}
+
+// One step of every problem with the given dt (UpdateFunctor::update(Q, U, dt)).
+int batch_step_dt(fv_batch* b, double dt) {
+  for (int i = 0; i < b->n; ++i)
+    if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "problem %d has no state", i);
+  int rc = Prepare(b);
+  if (rc) return rc;
+  rc = EnqueueStep(b, 0, dt);
+  if (rc) return rc;
+  b->launches += KernelsPerStep(b);
+  for (int i = 0; i < b->n; ++i) b->slot_valid[i] = 1;  // the last stage reduced the next slot
+  return FV_OK;
+}
+
+// The main.cpp:51-74 loop (while t + epsilon < tend, at most max_steps) for
+// a batch of one, steps replayed from a graph in the control blocks' own
+// mode, the control block read back between replays.
+int batch_advance(fv_batch* b, double tend, long max_steps, double* t, long* nsteps) {
+  if (b->n != 1) return Fail(b, FV_ERR_PARAM, "batch_advance runs a batch of one");
+  if (!b->state_set[0]) return Fail(b, FV_ERR_STATE, "no state set");
+  int rc = Prepare(b);
+  if (rc) return rc;
+  rc = EnsureSlots(b);
+  if (rc) return rc;
+  rc = ReadCtrl(b);
+  if (rc) return rc;
+  StepCtrl c = b->h_ctrl[0];
+  const long long step0 = c.step;
+  c.mode = 1;
+  c.t = *t;
+  c.tend = tend;
+  c.max_steps = max_steps > 0 ? step0 + max_steps : 0;
+  BCUDA(b, cudaMemcpyAsync(b->d_ctrl, &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, b->stream));
+  const bool short_run = max_steps > 0 && max_steps < kGraphSteps;
+  for (;;) {
+    if (short_run) {
+      for (long k = 0; k < max_steps; ++k) {
+        rc = EnqueueStep(b, -1, 0.0);
+        if (rc) return rc;
+        b->launches += KernelsPerStep(b);
+      }
+    } else {
+      if (!b->graph_loop || (b->ts != FV_TS_RK2 && b->flip)) {
+        // Euler ping-pong: a graph is captured for an even start (state in A)
+        if (b->ts != FV_TS_RK2 && b->flip) {
+          rc = EnqueueStep(b, -1, 0.0);
+          if (rc) return rc;
+          b->launches += KernelsPerStep(b);
+        }
+        if (!b->graph_loop) {
+          cudaGraph_t g;
+          const int flip0 = b->flip;
+          BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+          for (int k = 0; k < kGraphSteps; ++k) {
+            rc = EnqueueStep(b, -1, 0.0);
+            if (rc) {
+              cudaStreamEndCapture(b->stream, &g);
+              return rc;
+            }
+          }
+          BCUDA(b, cudaStreamEndCapture(b->stream, &g));
+          cudaError_t e = cudaGraphInstantiate(&b->graph_loop, g, 0);
+          cudaGraphDestroy(g);
+          if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+          b->flip = flip0;
+        }
+      }
+      BCUDA(b, cudaGraphLaunch(b->graph_loop, b->stream));
+      b->launches += (long)kGraphSteps * KernelsPerStep(b);
+      if (b->ts != FV_TS_RK2 && (kGraphSteps & 1)) b->flip ^= 1;
+    }
+    rc = ReadCtrl(b);
+    if (rc) return rc;
+    if (short_run || b->h_ctrl[0].err || !b->h_ctrl[0].active) break;
+  }
+  b->slot_valid[0] = 1;
+  *t = b->h_ctrl[0].t;
+  if (nsteps) *nsteps = (long)(b->h_ctrl[0].step - step0);
+  if (b->h_ctrl[0].err) return Fail(b, FV_ERR_NONFINITE, "non-finite state or dt during advance");
+  return FV_OK;
+}
+
+// Conserved totals of problem i (compensated sums on the host, in the
+// reference's field order).
+int batch_totals(fv_batch* b, int i, double out[5]) {
+  if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "no state set");
+  const Grid& G = b->G[i];
+  Fields S;
+  for (int k = 0; k < 5; ++k) S.f[k] = b->scratch + (size_t)k * G.fstride;
+  cudaError_t e = b->precision == FV_PREC_FP64
+                      ? cudaSuccess
+                      : fv::launch_double_from_pairs(G, Current(b, i), S, b->stream);
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "totals: %s", cudaGetErrorString(e));
+  const Fields& src = b->precision == FV_PREC_FP64 ? Current(b, i) : S;
+  int slot_of[5];
+  StorageOrder(G.plane, slot_of);
+  std::vector<double> h((size_t)G.na * G.rows);
+  for (int k = 0; k < 5; ++k) {
+    const int v = slot_of[k];
+    if (v == 3 && !b->wact[i]) {
+      out[k] = 0.0;
+      continue;
+    }
+    BCUDA(b, cudaMemcpy2DAsync(h.data(), (size_t)G.na * sizeof(double), src.f[v], (size_t)G.pitch * sizeof(double),
+                               (size_t)G.na * sizeof(double), G.rows, cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+    double sum = 0.0, comp = 0.0;
+    for (double x : h) {
+      const double t = sum + x;
+      comp += std::fabs(sum) >= std::fabs(x) ? (sum - t) + x : (x - t) + sum;
+      sum = t;
+    }
+    out[k] = sum + comp;
+  }
+  return FV_OK;
+}
+
+cudaStream_t batch_stream(const fv_batch* b) { return b->stream; }
+
+}  // namespace fv
