@@ -120,8 +120,11 @@ int fv_parse_ini(const char* text, fv_params* out);
 typedef struct fv_sim fv_sim;
 
 /* Allocate device state for one problem on the current CUDA device.
- * FV_ERR_UNSUPPORTED names settings this build does not run (see
- * fvgpu_last_error). */
+ * precision FV_PREC_FP64 (default) is the bit-exact form; FV_PREC_FP32_MIXED
+ * runs the problem in the FP32-mixed form through the batch machinery (a
+ * batch of one): every call below works except set_cons / get_cons and
+ * per-kernel profiling (FV_ERR_UNSUPPORTED).  FV_ERR_UNSUPPORTED names
+ * settings this build does not run (see fvgpu_last_error). */
 int fvgpu_create(const fv_params* params, fv_sim** out);
 int fvgpu_destroy(fv_sim* sim);
 /* Message for the last failing call on this handle ("" if none). */
