@@ -522,8 +522,8 @@ def run_profile_case(args):
     workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
     batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
     512-instance set, to keep captures small), shear_mixed / shear_fp64 (the
-    4096^2 shear layer, a state larger than L2), fp64_3d (a 160^3 random
-    state, HLLC, PLM, RK2, conduction + viscosity: the 3-D kernel)."""
+    4096^2 shear layer, a state larger than L2), fp64_3d / mixed_3d (a 160^3
+    random state, HLLC, PLM, RK2, conduction + viscosity: the 3-D kernels)."""
     import fv3d_gb300 as fv
     from fv3d_gb300 import problems
     case = args.profile_case
@@ -540,6 +540,8 @@ def run_profile_case(args):
             probs = [problem()]
         elif case.startswith("shear"):
             probs = [problems.shear_layer(4096)]
+        elif case == "mixed_3d":
+            probs = [random_3d(160)]
         else:
             probs = problems.batch_sod_sedov(64)
         plist = [p.params if case.endswith("fp64") else _mixed(p.params) for p in probs]
@@ -559,8 +561,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-case", nargs="?", const="fp64_rt", default=None,
-                    choices=["fp64_rt", "fp64_3d", "mixed_rt", "batch_sod_sedov_mixed", "batch_sod_sedov_fp64",
-                             "shear_mixed", "shear_fp64"],
+                    choices=["fp64_rt", "fp64_3d", "mixed_3d", "mixed_rt", "batch_sod_sedov_mixed",
+                             "batch_sod_sedov_fp64", "shear_mixed", "shear_fp64"],
                     help="run only a workload's steps (for ncu); prints no JSON")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other configurations (mixed, batched, shear layer)")

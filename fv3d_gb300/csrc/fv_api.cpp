@@ -263,6 +263,10 @@ int Configure(fv_sim* s) {
   G.bctc_zmax_value = p.bctc_zmax_value;
   G.zmin = p.zmin;
   G.theta1 = p.theta1;
+  G.zmin_f = (float)p.zmin;
+  G.theta1_f = (float)p.theta1;
+  G.bctc_zmin_value_f = (float)p.bctc_zmin_value;
+  G.bctc_zmax_value_f = (float)p.bctc_zmax_value;
   G.kappa_z = nullptr;  // B02 table: set by fvgpu_create
   SetExactConstants(G);
   DtConstants(p, &s->inv_tc, &s->inv_visc);

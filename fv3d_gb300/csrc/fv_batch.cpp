@@ -474,6 +474,10 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
         if (n_ax[a] == 1 && bc_ax[a] == FV_BC_REFLECTING)
           return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: a reflecting one-cell axis runs with fvgpu_create", i);
     }
+    if (params[i].thermal_conductivity_active && params[i].thermal_conductivity_mode == FV_TCM_B02)
+      return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: B02 conductivity runs with the FP64 handle (fvgpu_create)", i);
+    if (b->precision != FV_PREC_FP64 && b->G[i].fstride >= (1LL << 32))
+      return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: the FP32-mixed kernels address fields below 2^32 cells", i);
     b->wact[i] = (params[i].viscosity_active || b->G[i].ndim == 3) ? 1 : 0;
     off[i] = total;
     total += (size_t)10 * b->G[i].fstride;

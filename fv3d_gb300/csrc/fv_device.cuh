@@ -71,6 +71,7 @@ struct Grid {
   int bctc_zmin, bctc_zmax;        // fv_bctc_mode
   double bctc_zmin_value, bctc_zmax_value;
   double zmin, theta1;             // C91 ghost temperature profile
+  float zmin_f, theta1_f, bctc_zmin_value_f, bctc_zmax_value_f;  // FP32 copies
   // Face conductivities per interior z layer when kappa varies with z
   // (B02): kappa_z[3k + {0,1,2}] = in-plane faces, face k-1/2, face k+1/2.
   // Null for constant kappa.

@@ -12,8 +12,8 @@
 // turned into dt in FP64 by the control kernel.  Every reference feature of
 // the 3-D FP64 kernel is kept: C91 ghosts, the well-balanced / C91 z-flux
 // overrides, gravity, fixed-temperature / fixed-gradient conduction
-// boundaries, B02 conductivity, viscosity with the reference's z-branch
-// quirks.  Built with fast-math.
+// boundaries, viscosity with the reference's z-branch quirks (B02
+// conductivity runs on the FP64 handle only).  Built with fast-math.
 #include "fv_tile32.cuh"
 
 namespace fv {
@@ -51,7 +51,7 @@ struct MixedIn {
   const float2* const* pairs;  // src (STAGE_RK_1 / STAGE_EULER)
   const float* const* us;      // U* (STAGE_RK_2)
   bool in_pairs;
-  __device__ __forceinline__ void load(long long o, float u[5], float& e_lo) const {
+  __device__ __forceinline__ void load(unsigned o, float u[5], float& e_lo) const {
     if (in_pairs) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -67,20 +67,21 @@ struct MixedIn {
   }
 };
 
-__device__ __forceinline__ void load_prim32(const MixedIn& in, long long o, float gm1, float q[5]) {
+__device__ __forceinline__ void load_prim32(const MixedIn& in, unsigned o, float gm1, float q[5]) {
   float u[5], e_lo;
   in.load(o, u, e_lo);
   cons_to_prim32<PLANE_XY, true>(u, e_lo, gm1, q);
 }
 
 // fillC91 (BoundaryConditions.h:87-134) in FP32, as the FP64 kernel's.
-__device__ __forceinline__ void c91_ghost32(const Grid& G, const MixedIn& in, long long col, bool fa, bool fb, int kg,
+__device__ __forceinline__ void c91_ghost32(const Grid& G, const MixedIn& in, unsigned col, bool fa, bool fb, int kg,
                                             float res[5]) {
   const int kref = kg < 0 ? 0 : G.nc - 1;
   const int ksym = kg < 0 ? -kg - 1 : 2 * G.nc - kg - 1;
   float qref[5], qsym[5];
-  load_prim32(in, (long long)kref * G.nb * G.pitch + col, G.gm1_f, qref);
-  load_prim32(in, (long long)ksym * G.nb * G.pitch + col, G.gm1_f, qsym);
+  const unsigned zs = (unsigned)G.nb * (unsigned)G.pitch;
+  load_prim32(in, (unsigned)kref * zs + col, G.gm1_f, qref);
+  load_prim32(in, (unsigned)ksym * zs + col, G.gm1_f, qsym);
   if (fa) {
     qref[1] = -qref[1];
     qsym[1] = -qsym[1];
@@ -90,10 +91,10 @@ __device__ __forceinline__ void c91_ghost32(const Grid& G, const MixedIn& in, lo
     qsym[2] = -qsym[2];
   }
   const float grav = G.gravity_flag ? 1.0f : 0.0f;
-  const float posz = (float)(G.zmin + ((double)kg + 0.5) * G.dz);
+  const float posz = G.zmin_f + ((float)kg + 0.5f) * G.dz_f;
   if (kg < 0) {
     const float dz = posz - 0.5f * G.dz_f;
-    const float T = 1.0f + posz * (float)G.theta1;
+    const float T = 1.0f + posz * G.theta1_f;
     float p = qref[4] + dz * qref[0] * grav;
     float r = p / T;
     p = fmaxf(p, 1.0e-6f);
@@ -107,7 +108,7 @@ __device__ __forceinline__ void c91_ghost32(const Grid& G, const MixedIn& in, lo
   } else {
     const float Tref = qref[4] / qref[0];
     const float dz = posz - (1.0f - 0.5f * G.dz_f);
-    const float T = Tref + dz * (float)G.theta1;
+    const float T = Tref + dz * G.theta1_f;
     const float P = qref[4] + dz * qref[0] * grav;
     const float rho = P / T;
     res[4] = fmaxf(P, 1.0e-6f);
@@ -125,13 +126,13 @@ __device__ __forceinline__ void load_layer32(const Grid& G, const MixedIn& in, i
   const bool c91 = G.bc_c == DBC_C91 && (kg < 0 || kg >= G.nc);
   bool fz = false;
   const int sz = c91 ? 0 : bc_source(kg, G.nc, G.bc_c, fz);
-  const long long zoff = (long long)sz * G.nb * G.pitch;
+  const unsigned zoff = (unsigned)sz * (unsigned)G.nb * (unsigned)G.pitch;
   for (int idx = tid; idx < kLayer; idx += kThreads) {
     const int hy = idx / kHX, hx = idx - hy * kHX;
     bool fa, fb;
     const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
     const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
-    const long long col = (long long)sb * G.pitch + sa;
+    const unsigned col = (unsigned)sb * (unsigned)G.pitch + (unsigned)sa;
     float q[5];
     if (!c91) {
       load_prim32(in, zoff + col, G.gm1_f, q);
@@ -223,13 +224,15 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
   const int cx = tid % kTX, cy = tid / kTX;
   const int x = x0 + cx, y = y0 + cy;
   const bool own = x < G.na && y < G.nb;
-  const long long col = (long long)y * G.pitch + x;
-  const long long zstride = (long long)G.nb * G.pitch;
+  // 32-bit offsets: 64-bit integer arithmetic issues on the slow FP64 pipe;
+  // the host keeps every field below 2^32 elements for this kernel
+  const unsigned col = (unsigned)y * (unsigned)G.pitch + (unsigned)x;
+  const unsigned zstride = (unsigned)G.nb * (unsigned)G.pitch;
 
   if (!ctrl->active) {
     if (kind == STAGE_EULER && own) {
       for (int k = k0; k < k1; ++k) {
-        const long long o = k * zstride + col;
+        const unsigned o = (unsigned)k * zstride + col;
 #pragma unroll
         for (int v = 0; v < 5; ++v) dst[v][o] = src[v][o];
       }
@@ -298,7 +301,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k - 1 + m), v, cy + 2, cx + 2);
         face3f<2>(c, RS, recon, G, fzR, need_pout ? &poutR : nullptr);
       }
-      const long long o = k * zstride + col;
+      const unsigned o = (unsigned)k * zstride + col;
       float fL[5], fR[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -343,14 +346,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         }
       }
       if (G.tc) {  // ThermalConduction.h:38-96
-        float kC, kF, kB;
-        if (G.kappa_z) {
-          kC = (float)G.kappa_z[3 * k];
-          kF = (float)G.kappa_z[3 * k + 1];
-          kB = (float)G.kappa_z[3 * k + 2];
-        } else {
-          kC = kF = kB = G.kappa_f;
-        }
+        const float kC = G.kappa_f, kF = G.kappa_f, kB = G.kappa_f;  // batches take constant kappa
         const int hy = cy + 2, hx = cx + 2;
         const float TC = S.temp(sk, hy, hx);
         const float FL = kC * (TC - S.temp(sk, hy, hx - 1)) * G.inv_dx_f;
@@ -360,11 +356,9 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         float FF = kF * (TC - S.temp(slot_of(k - 1), hy, hx)) * G.inv_dz_f;
         float FB = kB * (S.temp(slot_of(k + 1), hy, hx) - TC) * G.inv_dz_f;
         if (k == 0 && G.bctc_zmin != 0)
-          FF = G.bctc_zmin == 1 ? kF * 2.0f * (TC - (float)G.bctc_zmin_value) * G.inv_dz_f
-                                : kF * (float)G.bctc_zmin_value;
+          FF = G.bctc_zmin == 1 ? kF * 2.0f * (TC - G.bctc_zmin_value_f) * G.inv_dz_f : kF * G.bctc_zmin_value_f;
         if (k == G.nc - 1 && G.bctc_zmax != 0)
-          FB = G.bctc_zmax == 1 ? kB * 2.0f * ((float)G.bctc_zmax_value - TC) * G.inv_dz_f
-                                : kB * (float)G.bctc_zmax_value;
+          FB = G.bctc_zmax == 1 ? kB * 2.0f * (G.bctc_zmax_value_f - TC) * G.inv_dz_f : kB * G.bctc_zmax_value_f;
         du[4] += dtdx * (FR - FL) + dtdy * (FD - FU) + dtdz * (FB - FF);
       }
       if (G.visc) {  // Viscosity.h:145-151

@@ -99,3 +99,14 @@ def test_batch3d_rejects_what_it_does_not_run():
     with pytest.raises(fv.FvError) as e:
         fv.Batch([pr.params])
     assert e.value.status == 2
+    # B02 conductivity (a per-layer kappa table) runs with the FP64 handle only
+    b02 = _rand3d("z", M(8, 8, 12), ("periodic", "periodic", "reflecting"), "hllc", 606,
+                  extra={"thermal_conduction": {"active": True, "kappa": 0.02, "conductivity_mode": "B02"}})
+    b02.params.b02_zmid, b02.params.b02_kappa1, b02.params.b02_kappa2, b02.params.b02_thickness = 0.5, 1.0, 3.0, 0.1
+    for params in (b02.params, _mixed(b02.params)):
+        with pytest.raises(fv.FvError) as e:
+            fv.Batch([params])
+        assert e.value.status == 2
+    with pytest.raises(fv.FvError) as e:
+        fv.Simulation(_mixed(b02.params))
+    assert e.value.status == 2
