@@ -44,13 +44,13 @@ WORKLOAD = "rayleigh_taylor_512x1536_fp64"
 ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2-D)
 # dram__bytes_read.sum + dram__bytes_write.sum of the two stage launches of one
 # RK2 step of this workload, from one ncu --set full capture
-# (profiles/stage2d_fp64_rt512x1536.md: 25.23+0.07 MB and 50.40+0.10 MB).
-NCU_TRAFFIC_BYTES_PER_STEP = 75.80e6
+# (profiles/stage2d_fp64_rt512x1536.md: 25.23+0.07 MB and 50.40+0.09 MB).
+NCU_TRAFFIC_BYTES_PER_STEP = 75.79e6
 # FP64 arithmetic lane operations (DADD + DMUL + DFMA thread instructions)
-# per cell-update of this workload from the same capture (stage 1: 395.9,
-# stage 2: 436.4).  The FP64 kernel is bound by the FP64 pipe: its roofline
+# per cell-update of this workload from the same capture (stage 1: 384.0,
+# stage 2: 425.0).  The FP64 kernel is bound by the FP64 pipe: its roofline
 # against the FP64 FMA rate measured live by fvgpu_probe_fp64_rate.
-FP64_OPS_PER_CELL_UPDATE = 832
+FP64_OPS_PER_CELL_UPDATE = 809
 
 
 def peaks():
@@ -481,17 +481,17 @@ def run_variants(torch, args, flush):
     add("batch64_rt_fp32_mixed", r, 160, l1_vs_fp64(torch, b4, args.rt_batch_l1_steps,
                                                     [_mixed(p.params) for p in b4]))
 
+    # Single problems: FP64 through the single-problem handle (fvgpu_create),
+    # the FP32-mixed form as a batch of one.
     # config 0: Sedov 256^2 (HLLC, absorbing), FP64 and mixed
     se = problems.sedov(256)
-    _, r = time_batch(torch, [se.params], [se.prim], 64, 8)
-    add("sedov_256_fp64", r, 160)
+    add("sedov_256_fp64", time_sim(torch, se, 64, 8), 160)
     _, r = time_batch(torch, [_mixed(se.params)], [se.prim], 64, 8)
     add("sedov_256_fp32_mixed", r, 128, l1_vs_fp64(torch, [se], 200, [_mixed(se.params)]))
 
     # config 1b: thermal pulse 1024^2 with conduction and viscosity, 200 fixed steps
     tp = problems.thermal_pulse(1024)
-    _, r = time_batch(torch, [tp.params], [tp.prim], 16, 4)
-    add("thermal_pulse_1024_fp64", r, 200)
+    add("thermal_pulse_1024_fp64", time_sim(torch, tp, 16, 4), 200)
     _, r = time_batch(torch, [_mixed(tp.params)], [tp.prim], 64, 8)
     add("thermal_pulse_1024_fp32_mixed", r, 160, l1_vs_fp64(torch, [tp], 200, [_mixed(tp.params)]))
 
@@ -509,8 +509,7 @@ def run_variants(torch, args, flush):
 
     # config 2: shear layer 4096^2 with conduction and viscosity, FP64 and mixed
     sh = problems.shear_layer(4096)
-    _, r = time_batch(torch, [sh.params], [sh.prim], 8, 3)
-    add("shear_layer_4096_fp64", r, 200)
+    add("shear_layer_4096_fp64", time_sim(torch, sh, 8, 3), 200)
     _, r = time_batch(torch, [_mixed(sh.params)], [sh.prim], 32, 8)
     add("shear_layer_4096_fp32_mixed", r, 160, l1_vs_fp64(torch, [sh], 50, [_mixed(sh.params)]))
     return out

