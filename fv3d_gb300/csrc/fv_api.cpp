@@ -527,12 +527,25 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
     *out = s;
     return Fail(s, FV_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
   }
-  cudaMemset(s->buf, 0, bytes);
+  // Every initialisation below is ordered on the handle's own (non-blocking)
+  // stream and waited for before returning: a legacy-stream cudaMemset or
+  // pageable cudaMemcpy is not ordered with non-blocking streams and could
+  // land after the first state upload while other work keeps the GPU busy.
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    *out = s;
+    return Fail(s, FV_ERR_CUDA, "stream creation failed");
+  }
+  s->stream = s->own_stream;
+  if (cudaMemsetAsync(s->buf, 0, bytes, s->own_stream) != cudaSuccess) {
+    *out = s;
+    return Fail(s, FV_ERR_CUDA, "state initialisation failed");
+  }
   if (B02(s->p)) {
     const std::vector<double> table = KappaTable(s->p);
     if (cudaMalloc(&s->d_kappa_z, table.size() * sizeof(double)) != cudaSuccess ||
-        cudaMemcpy(s->d_kappa_z, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice) !=
-            cudaSuccess) {
+        cudaMemcpyAsync(s->d_kappa_z, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice,
+                        s->own_stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->own_stream) != cudaSuccess) {
       *out = s;
       return Fail(s, FV_ERR_NOMEM, "conductivity table allocation failed");
     }
@@ -548,12 +561,10 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
     *out = s;
     return Fail(s, FV_ERR_NOMEM, "control block allocation failed");
   }
-  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
+  if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
     *out = s;
-    return Fail(s, FV_ERR_CUDA, "stream/event creation failed");
+    return Fail(s, FV_ERR_CUDA, "event creation failed");
   }
-  s->stream = s->own_stream;
   StepCtrl c{};
   c.cfl = s->p.CFL;
   c.inv_tc = s->inv_tc;

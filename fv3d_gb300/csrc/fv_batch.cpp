@@ -489,8 +489,14 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
       cudaMallocHost(&b->h_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
       cudaMalloc(&b->d_queue, sizeof(unsigned) * 2 * kMaxGroups) != cudaSuccess)
     return Fail(b, FV_ERR_NOMEM, "batch allocation of %zu bytes failed", total * sizeof(double));
-  cudaMemset(b->buf, 0, total * sizeof(double));
-  cudaMemset(b->d_queue, 0, sizeof(unsigned) * 2 * kMaxGroups);
+  // Initialisation is ordered on the batch's own non-blocking stream (a
+  // legacy-stream cudaMemset would not be ordered with it) and waited for
+  // below.
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return Fail(b, FV_ERR_CUDA, "stream creation failed");
+  b->stream = b->own_stream;
+  BCUDA(b, cudaMemsetAsync(b->buf, 0, total * sizeof(double), b->stream));
+  BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned) * 2 * kMaxGroups, b->stream));
   b->A.resize(n);
   b->B.resize(n);
   for (int i = 0; i < n; ++i)
@@ -498,9 +504,6 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
       b->A[i].f[v] = b->buf + off[i] + (size_t)v * b->G[i].fstride;
       b->B[i].f[v] = b->buf + off[i] + (size_t)(5 + v) * b->G[i].fstride;
     }
-  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
-    return Fail(b, FV_ERR_CUDA, "stream creation failed");
-  b->stream = b->own_stream;
   std::vector<StepCtrl> hc(n);
   for (int i = 0; i < n; ++i) {
     std::memset(&hc[i], 0, sizeof(StepCtrl));

@@ -43,21 +43,22 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   auto kern = stage2d_fp64<PLANE, RS, KIND, WACT>;
   static bool attr_set = false;  // per instantiation, once per process
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::bytes(true));
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(WACT ? SM::bytes_vface() : SM::bytes(true)));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  static int resident[2] = {0, 0};  // CTAs per SM without / with conduction
-  const int tc = G.tc != 0;
-  const size_t smem = SM::bytes(tc);
-  if (!resident[tc]) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[tc], kern, kTileThreads, smem);
+  static int resident[3] = {0, 0, 0};  // CTAs per SM: plain / conduction / shared-face viscosity
+  const int cfg = WACT && G.visc ? 2 : (G.tc != 0);
+  const size_t smem = cfg == 2 ? SM::bytes_vface() : SM::bytes(cfg == 1);
+  if (!resident[cfg]) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[cfg], kern, kTileThreads, smem);
     if (e != cudaSuccess) return e;
-    if (resident[tc] < 1) resident[tc] = 1;
+    if (resident[cfg] < 1) resident[cfg] = 1;
   }
   const long long units = (long long)((G.na + kTileX - 1) / kTileX) * G.nb;
   long long ctas = units / kMinRowsPerCta;
-  const long long slots = (long long)resident[tc] * sm_count();
+  const long long slots = (long long)resident[cfg] * sm_count();
   if (ctas > slots) ctas = slots;
   if (ctas < 1) ctas = 1;
   const Fields none{};

@@ -72,7 +72,73 @@ struct TileSmem {
   __device__ T& fa(int v, int fy, int fx) const { return base[kFA + (sv(v) * TL::TY + fy) * (TL::TX + 1) + fx]; }
   __device__ T& fb(int v, int fy, int fx) const { return base[kFB + (sv(v) * (TL::TY + 1) + fy) * TL::TX + fx]; }
   __device__ T& temp(int hy, int hx) const { return base[kT + hy * TL::HX + hx]; }
+  // Shared-face viscous fluxes (4 per face: three momentum components and
+  // energy), after the temperature tile.
+  static constexpr int kVA = kT + TL::HY * TL::HX;
+  static constexpr int kVB = kVA + 4 * TL::TY * (TL::TX + 1);
+  static constexpr int kVEnd = kVB + 4 * (TL::TY + 1) * TL::TX;
+  static constexpr size_t bytes_vface() { return sizeof(T) * (size_t)kVEnd; }
+  __device__ T& va(int k, int fy, int fx) const { return base[kVA + (k * TL::TY + fy) * (TL::TX + 1) + fx]; }
+  __device__ T& vb(int k, int fy, int fx) const { return base[kVB + (k * (TL::TY + 1) + fy) * TL::TX + fx]; }
 };
+
+// The IZ branch of Viscosity.h:214-239 in an x-y run (z is the one-cell
+// axis): qi is the centre, the z derivatives vanish, and its y terms do not
+// depend on the side.  Accumulates into vz[1..4].
+template <class T, class PA>
+__device__ __forceinline__ void viscous_iz_xy(const PA& P, T odx, T odz, T mu, T vz[5]) {
+  const T two_thirds = T(2.0 / 3.0);
+  const T c4x = half_of(half_of(odx)), c4z = half_of(half_of(odz));
+  const int U = 1, V = 2, W = 3;
+  const T cu = P(1, 1, U), cv = P(1, 1, V), cw = P(1, 1, W);
+  const T dvdy = c4z * (P(2, 1, W) - P(0, 1, V) + P(2, 1, W) - P(0, 1, V));
+  const T dwdy = c4z * (P(2, 1, V) - P(0, 1, W) + P(2, 1, V) - P(0, 1, W));
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {
+    const T sign = s == 1 ? T(-1) : T(1);
+    const T dudx = c4x * (P(1, 2, U) - P(s, 0, U) + P(1, 2, U) - P(s - 1, 0, U));
+    const T dwdx = c4x * (P(1, 2, V) - P(s, 0, W) + P(1, 2, V) - P(s - 1, 0, W));
+    const T tau_zz = -(two_thirds * (dudx + dvdy));
+    const T tau_xz = dwdx;
+    const T tau_yz = dwdy;
+    vz[1] += sign * mu * tau_xz;
+    vz[2] += sign * mu * tau_yz;
+    vz[3] += sign * mu * tau_zz;
+    vz[4] += sign * mu * (tau_xz * cu + tau_yz * cv + tau_zz * cw);
+  }
+}
+
+// The IZ branch in an x-z run, with the reference's index / field mix-ups
+// (Viscosity.h:214-239).  Some of its terms read the cell's own row, so its
+// flux belongs to the cell, not to the face.  Accumulates into vz[1..4].
+template <class T, class PA>
+__device__ __forceinline__ void viscous_iz_xz(const PA& P, T odx, T odz, T mu, T vz[5]) {
+  const T four_thirds = T(4.0 / 3.0);
+  const T two_thirds = T(2.0 / 3.0);
+  const T c4x = half_of(half_of(odx)), c4z = half_of(half_of(odz));
+  const int U = 1, V = 2, W = 3;
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {
+    const T sign = s == 1 ? T(-1) : T(1);
+    const T qiu = half_of(P(s, 1, U) + P(s - 1, 1, U));
+    const T qiv = half_of(P(s, 1, V) + P(s - 1, 1, V));
+    const T qiw = half_of(P(s, 1, W) + P(s - 1, 1, W));
+    const T dudz = odz * (P(s, 1, U) - P(s - 1, 1, U));
+    const T dvdz = odz * (P(s, 1, V) - P(s - 1, 1, V));
+    const T dwdz = odz * (P(s, 1, W) - P(s - 1, 1, W));
+    const T dudx = c4x * (P(s, 2, U) - P(1, 0, U) + P(s - 1, 2, U) - P(1, 0, U));
+    const T dwdx = c4x * (P(s, 2, V) - P(1, 0, W) + P(s - 1, 2, V) - P(1, 0, W));
+    const T dvdy = c4z * (P(s, 1, W) - P(s, 1, V) + P(s - 1, 1, W) - P(s - 1, 1, V));
+    const T dwdy = c4z * (P(s, 1, V) - P(s, 1, W) + P(s - 1, 1, V) - P(s - 1, 1, W));
+    const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+    const T tau_xz = dudz + dwdx;
+    const T tau_yz = dvdz + dwdy;
+    vz[1] += sign * mu * tau_xz;
+    vz[2] += sign * mu * tau_yz;
+    vz[3] += sign * mu * tau_zz;
+    vz[4] += sign * mu * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+  }
+}
 
 // Viscous fluxes of Viscosity.h:149-243 for a 2-D plane, with the reference's
 // arithmetic (including its z-branch index and field mix-ups) on every term
@@ -134,24 +200,7 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T odx, T ody, T odz, 
       vf[1][3] += sign * mu * tau_yz;
       vf[1][4] += sign * mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
     }
-    // IZ (Viscosity.h:214-239) on the one-cell axis: qi is the centre, the z
-    // derivatives vanish, and its y terms do not depend on the side.
-    const T cu = P(1, 1, U), cv = P(1, 1, V), cw = P(1, 1, W);
-    const T dvdy = c4z * (P(2, 1, W) - P(0, 1, V) + P(2, 1, W) - P(0, 1, V));
-    const T dwdy = c4z * (P(2, 1, V) - P(0, 1, W) + P(2, 1, V) - P(0, 1, W));
-#pragma unroll
-    for (int s = 1; s < 3; ++s) {
-      const T sign = s == 1 ? T(-1) : T(1);
-      const T dudx = c4x * (P(1, 2, U) - P(s, 0, U) + P(1, 2, U) - P(s - 1, 0, U));
-      const T dwdx = c4x * (P(1, 2, V) - P(s, 0, W) + P(1, 2, V) - P(s - 1, 0, W));
-      const T tau_zz = -(two_thirds * (dudx + dvdy));
-      const T tau_xz = dwdx;
-      const T tau_yz = dwdy;
-      vf[2][1] += sign * mu * tau_xz;
-      vf[2][2] += sign * mu * tau_yz;
-      vf[2][3] += sign * mu * tau_zz;
-      vf[2][4] += sign * mu * (tau_xz * cu + tau_yz * cv + tau_zz * cw);
-    }
+    viscous_iz_xy(P, odx, odz, mu, vf[2]);
   } else {
 #pragma unroll
     for (int s = 1; s < 3; ++s) {  // IX, y-derivatives vanish
@@ -173,27 +222,7 @@ __device__ __forceinline__ void viscous_plane(const PA& P, T odx, T ody, T odz, 
       vf[0][4] += sign * mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
     }
     // IY on the one-cell axis: every term is side-independent and cancels.
-#pragma unroll
-    for (int s = 1; s < 3; ++s) {  // IZ, with the reference's index/field mix-ups
-      const T sign = s == 1 ? T(-1) : T(1);
-      const T qiu = half_of(P(s, 1, U) + P(s - 1, 1, U));
-      const T qiv = half_of(P(s, 1, V) + P(s - 1, 1, V));
-      const T qiw = half_of(P(s, 1, W) + P(s - 1, 1, W));
-      const T dudz = odz * (P(s, 1, U) - P(s - 1, 1, U));
-      const T dvdz = odz * (P(s, 1, V) - P(s - 1, 1, V));
-      const T dwdz = odz * (P(s, 1, W) - P(s - 1, 1, W));
-      const T dudx = c4x * (P(s, 2, U) - P(1, 0, U) + P(s - 1, 2, U) - P(1, 0, U));
-      const T dwdx = c4x * (P(s, 2, V) - P(1, 0, W) + P(s - 1, 2, V) - P(1, 0, W));
-      const T dvdy = c4z * (P(s, 1, W) - P(s, 1, V) + P(s - 1, 1, W) - P(s - 1, 1, V));
-      const T dwdy = c4z * (P(s, 1, V) - P(s, 1, W) + P(s - 1, 1, V) - P(s - 1, 1, W));
-      const T tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
-      const T tau_xz = dudz + dwdx;
-      const T tau_yz = dvdz + dwdy;
-      vf[2][1] += sign * mu * tau_xz;
-      vf[2][2] += sign * mu * tau_yz;
-      vf[2][3] += sign * mu * tau_zz;
-      vf[2][4] += sign * mu * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
-    }
+    viscous_iz_xz(P, odx, odz, mu, vf[2]);
   }
 }
 
@@ -206,6 +235,96 @@ struct PlaneVel {
     return s.q(phys_slot<PLANE>(var), hy + r - 1, hx + c - 1);
   }
 };
+
+// The viscous flux of one face for the branches whose terms depend on the
+// face alone: IX (DIR 0) in both planes and IY (DIR 1) in the x-y plane.  The
+// reference evaluates it from each of the two cells, as
+// (sign * mu) * t with sign -1 on the cell's lower face and +1 on its upper
+// face, from identical operands; (-mu) * t = -(mu * t) exactly, so one
+// evaluation serves both cells: g = {mu*t1, mu*t2, mu*t3, mu*(t . qi)} in the
+// branch's component order (vf[d][1..4]).  P is centred on the cell above
+// the face (the s = 1 side of Viscosity.h's loop).
+template <int PLANE, int DIR, class PA>
+__device__ __forceinline__ void viscous_face(const PA& P, double odx, double ody, double odz, double mu, double g[4]) {
+  const double four_thirds = 4.0 / 3.0;
+  const double two_thirds = 2.0 / 3.0;
+  const int U = 1, V = 2, W = 3;
+  if (DIR == 0) {
+    const double qiu = half64(P(1, 1, U) + P(1, 0, U));
+    const double qiv = half64(P(1, 1, V) + P(1, 0, V));
+    const double qiw = half64(P(1, 1, W) + P(1, 0, W));
+    const double dudx = odx * (P(1, 1, U) - P(1, 0, U));
+    const double dvdx = odx * (P(1, 1, V) - P(1, 0, V));
+    const double dwdx = odx * (P(1, 1, W) - P(1, 0, W));
+    double tau_xx, tau_xy, tau_xz;
+    if (PLANE == PLANE_XY) {
+      const double c4y = half64(half64(ody));
+      const double dudy = c4y * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
+      const double dvdy = c4y * (P(2, 1, V) - P(0, 1, V) + P(2, 0, V) - P(0, 0, V));
+      tau_xx = four_thirds * dudx - two_thirds * dvdy;
+      tau_xy = dvdx + dudy;
+      tau_xz = dwdx;
+    } else {
+      const double c4z = half64(half64(odz));
+      const double dudz = c4z * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
+      const double dwdz = c4z * (P(2, 1, W) - P(0, 1, W) + P(2, 0, W) - P(0, 0, W));
+      tau_xx = four_thirds * dudx - two_thirds * dwdz;
+      tau_xy = dvdx;
+      tau_xz = dwdx + dudz;
+    }
+    g[0] = mu * tau_xx;
+    g[1] = mu * tau_xy;
+    g[2] = mu * tau_xz;
+    g[3] = mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+  } else {
+    const double c4x = half64(half64(odx));
+    const double qiu = half64(P(1, 1, U) + P(0, 1, U));
+    const double qiv = half64(P(1, 1, V) + P(0, 1, V));
+    const double qiw = half64(P(1, 1, W) + P(0, 1, W));
+    const double dudy = ody * (P(1, 1, U) - P(0, 1, U));
+    const double dvdy = ody * (P(1, 1, V) - P(0, 1, V));
+    const double dwdy = ody * (P(1, 1, W) - P(0, 1, W));
+    const double dudx = c4x * (P(1, 2, U) - P(1, 0, U) + P(0, 2, U) - P(0, 0, U));
+    const double dvdx = c4x * (P(1, 2, V) - P(1, 0, V) + P(0, 2, V) - P(0, 0, V));
+    const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
+    const double tau_xy = dvdx + dudy;
+    const double tau_yz = dwdy;
+    g[0] = mu * tau_xy;
+    g[1] = mu * tau_yy;
+    g[2] = mu * tau_yz;
+    g[3] = mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+  }
+}
+
+// 0.0 + x without the FP64 pipe: x itself, except that -0 becomes +0.
+__device__ __forceinline__ double plus_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return b == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+// viscous_plane with the face-only branches taken from shared face fluxes:
+// gl[d] / gr[d] are viscous_face of the cell's lower / upper face along
+// branch d (d = 1 used in the x-y plane only).  vf[d][k+1] =
+// (0 + (-gl[d][k])) + gr[d][k], the reference's two accumulations; the
+// branches that read the cell itself are evaluated here.  Same bits as
+// viscous_plane.
+template <int PLANE, class PA>
+__device__ __forceinline__ void viscous_plane_shared(const PA& P, const double gl[2][4], const double gr[2][4],
+                                                     double odx, double odz, double mu, double vf[3][5]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) vf[d][v] = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) vf[0][k + 1] = plus_zero(-gl[0][k]) + gr[0][k];
+  if (PLANE == PLANE_XY) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) vf[1][k + 1] = plus_zero(-gl[1][k]) + gr[1][k];
+    viscous_iz_xy(P, odx, odz, mu, vf[2]);
+  } else {
+    viscous_iz_xz(P, odx, odz, mu, vf[2]);
+  }
+}
 
 // Slots of a sweep (swap_component, States.h:104-111) from storage order
 // (r, a, b, c, p): DIR 0 = reference IX (u, v, w); DIR 1 = IY (v, u, w) in
@@ -304,6 +423,8 @@ struct PrimView {
   __device__ __forceinline__ double& temp(int hy, int hx) const { return s.temp(rows(hy), hx); }
   __device__ __forceinline__ double& fa(int v, int fy, int fx) const { return s.fa(v, fy, fx); }
   __device__ __forceinline__ double& fb(int v, int fy, int fx) const { return s.fb(v, fy, fx); }
+  __device__ __forceinline__ double& va(int k, int fy, int fx) const { return s.va(k, fy, fx); }
+  __device__ __forceinline__ double& vb(int k, int fy, int fx) const { return s.vb(k, fy, fx); }
 };
 
 // Phase 1: halo rows [h0, h1) of the block whose first cell is (x0, y0),
@@ -338,10 +459,39 @@ __device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, c
   }
 }
 
+// Viscous fluxes of the same faces (VSH form): a faces along IX; b faces
+// along IY in the x-y plane (the x-z plane's IZ branch belongs to the cells).
+template <int PLANE, class TL, class PV>
+__device__ __forceinline__ void visc_faces64(const Grid& G, const PV& V, int nr, int fb0, int tid) {
+  constexpr int TX = TL::TX;
+  const int nfa = (TX + 1) * nr;
+  const int nfa_pad = (nfa + 31) & ~31;
+  const int n = nfa_pad + (PLANE == PLANE_XY ? TX * (nr + 1 - fb0) : 0);
+  for (int it = tid; it < n; it += kTileThreads) {
+    double g[4];
+    if (it < nfa_pad) {
+      if (it >= nfa) continue;
+      const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
+      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell right of a face
+      viscous_face<PLANE, 0>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) V.va(k, fy, fx) = g[k];
+    } else {
+      const int j = it - nfa_pad;
+      const int jy = j / TX, fx = j - jy * TX;
+      const int fy = fb0 + jy;
+      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell above b face fy
+      viscous_face<PLANE, 1>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) V.vb(k, fy, fx) = g[k];
+    }
+  }
+}
+
 // Phase 2: a faces of cell rows 0..nr-1 and b faces of face rows fb0..nr of
 // the block (b face row fy lies between cell rows fy-1 and fy), each solved
-// once.
-template <int PLANE, bool WACT, class TL, class PV>
+// once; with VSH, their viscous fluxes too.
+template <int PLANE, bool WACT, class TL, bool VSH, class PV>
 __device__ __forceinline__ void faces64(const Grid& G, const Consts64& K, const PV& V, int rs, int nr, int fb0,
                                         int tid) {
   constexpr int TX = TL::TX;
@@ -377,11 +527,12 @@ __device__ __forceinline__ void faces64(const Grid& G, const Consts64& K, const 
         if (WACT || v != 3) V.fb(v, fy, fx) = f[v];
     }
   }
+  if (VSH && WACT && G.visc) visc_faces64<PLANE, TL>(G, V, nr, fb0, tid);
 }
 
 // Phase 3-5: the cells of rows 0..nr-1 of the block -- conservative update,
 // sources, RK2 combination, CFL term (max folded into red).
-template <int PLANE, bool WACT, class TL, bool P2, class PV>
+template <int PLANE, bool WACT, class TL, bool P2, bool VSH, class PV>
 __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Fields& uin, const Fields& u0,
                                          const Fields& uout, StepCtrl* ctrl, int kind, double dt, int x0, int y0,
                                          int nr, int tid, const Fields* hout, unsigned long long& red) {
@@ -430,7 +581,19 @@ __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Field
     if (WACT && G.visc) {  // Viscosity.h:245-251
       PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
       double vf[3][5];
-      viscous_plane<PLANE, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
+      if (VSH) {
+        double gl[2][4], gr[2][4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          gl[0][k] = V.va(k, cy, cx);
+          gr[0][k] = V.va(k, cy, cx + 1);
+          gl[1][k] = PLANE == PLANE_XY ? V.vb(k, cy, cx) : 0.0;
+          gr[1][k] = PLANE == PLANE_XY ? V.vb(k, cy + 1, cx) : 0.0;
+        }
+        viscous_plane_shared<PLANE>(P, gl, gr, G.inv_dx, G.inv_dz, G.mu, vf);
+      } else {
+        viscous_plane<PLANE, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
+      }
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
@@ -508,10 +671,10 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
   const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
   load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, 0, HY, tid);
   __syncthreads();
-  faces64<PLANE, WACT, TL>(G, K, V, rs, TY, 0, tid);
+  faces64<PLANE, WACT, TL, false>(G, K, V, rs, TY, 0, tid);
   __syncthreads();
   unsigned long long red = 0ull;
-  update64<PLANE, WACT, TL, P2>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, TY, tid, hout, red);
+  update64<PLANE, WACT, TL, P2, false>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, TY, tid, hout, red);
   if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
@@ -521,7 +684,8 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
 // rows through a ring of TY + 4 primitive rows, so each block converts only
 // its TY new rows and reuses the b-face fluxes on the boundary with the
 // previous block (the arithmetic of every face and cell is that of the tile
-// body, so results are bit-identical).  Host code splits the units evenly
+// body, so results are bit-identical; viscous fluxes of the face-only
+// branches are computed once per face, viscous_face).  Host code splits the units evenly
 // over the CTAs that fit on the GPU at once, which balances the FP64 work
 // per SM whatever the grid shape.
 template <int PLANE, bool WACT, class TL, bool P2>
@@ -537,6 +701,7 @@ __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, 
   const double dt = ctrl->dt_cur;
   const int parity = ctrl->parity;
   const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+  const bool vsh = WACT && G.visc;  // shared-face viscous fluxes (smem: bytes_vface)
   unsigned long long red = 0ull;
   for (long long u = u0_; u < u1_;) {
     const int strip = (int)(u / G.nb);
@@ -559,12 +724,17 @@ __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, 
           const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
           S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
         }
+        if (vsh && PLANE == PLANE_XY)
+          for (int i = tid; i < 4 * TX; i += kTileThreads) {
+            const int k = i / TX, fx = i - k * TX;
+            S.vb(k, 0, fx) = S.vb(k, TY, fx);
+          }
       }
       load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, first ? 0 : 4, nr + 4, tid);
       __syncthreads();
-      faces64<PLANE, WACT, TL>(G, K, V, rs, nr, first ? 0 : 1, tid);
+      faces64<PLANE, WACT, TL, WACT>(G, K, V, rs, nr, first ? 0 : 1, tid);
       __syncthreads();
-      update64<PLANE, WACT, TL, P2>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
+      update64<PLANE, WACT, TL, P2, WACT>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
       __syncthreads();
       base += TY;
       if (base >= HY) base -= HY;
