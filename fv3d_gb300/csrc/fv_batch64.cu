@@ -1,25 +1,34 @@
 // fv_batch64.cu -- persistent FP64 stage kernel for batches of problems.
 //
 // One launch per RK stage covers every problem of a group (same plane, same
-// third-momentum layout): `grid` resident CTAs repeatedly take the next tile
-// number from a global work-queue counter, find the problem owning it
-// (binary search over the problems' first tile numbers), copy its descriptor
-// to shared memory and run stage_tile64 on it.  Each problem keeps its own
-// control block, so its own dt and its own CFL reduction slot.  Compiled
-// without FMA contraction: a problem advanced in a batch is bit-identical to
-// the same problem advanced alone, and to the reference.
+// third-momentum layout): `grid` resident CTAs repeatedly take the next work
+// item from a global work-queue counter, find the problem owning it (binary
+// search over the problems' first item numbers), copy its descriptor to
+// shared memory and run it.  A work item is a tx x ty piece of one problem:
+// a strip segment of ty rows, marched in blocks of 512 cells
+// (stage_segment64), so consecutive blocks share boundary rows and faces.
+// Each problem keeps its own control block, so its own dt and its own CFL
+// reduction slot.  Compiled without FMA contraction: a problem advanced in a
+// batch is bit-identical to the same problem advanced alone, and to the
+// reference.
 #include "fv_tile64.cuh"
 
 namespace fv {
 
 namespace {
 
-constexpr TileShape kShapes64[] = {{32, 16}, {32, 8}, {64, 8}, {16, 16}};
+// Work-item shapes (cells along a x rows along b) the autotuner chooses from;
+// the rows are a whole number of marching blocks.
+constexpr TileShape kShapes64[] = {{32, 64}, {32, 32}, {32, 16}, {64, 32}};
 constexpr int kNumShapes64 = sizeof(kShapes64) / sizeof(kShapes64[0]);
+constexpr int block_rows(int tx) { return 2 * kTileThreads / tx; }  // 512-cell blocks
+static_assert(kShapes64[0].ty % block_rows(kShapes64[0].tx) == 0 && kShapes64[1].ty % block_rows(kShapes64[1].tx) == 0 &&
+                  kShapes64[2].ty % block_rows(kShapes64[2].tx) == 0 && kShapes64[3].ty % block_rows(kShapes64[3].tx) == 0,
+              "item rows must be whole marching blocks");
 
 static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
 
-// Finds the problem owning tile t and copies its descriptor to shared memory.
+// Finds the problem owning item t and copies its descriptor to shared memory.
 __device__ __forceinline__ void fetch_inst(const BatchInst* __restrict__ insts, int ninst, int t, BatchInst* s_inst) {
   int lo = 0, hi = ninst - 1;
   while (lo < hi) {
@@ -32,15 +41,15 @@ __device__ __forceinline__ void fetch_inst(const BatchInst* __restrict__ insts, 
   for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
 }
 
-template <int PLANE, bool WACT, class TL>
-__global__ void __launch_bounds__(kTileThreads)
+template <int PLANE, bool WACT, class TL, int ITEM_ROWS>
+__global__ void __launch_bounds__(kTileThreads, WACT ? FV_FP64_MIN_CTAS_W : FV_FP64_MIN_CTAS)
 batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
   for (;;) {
-    __syncthreads();  // the previous tile is finished with s_tile, s_inst and smem
+    __syncthreads();  // the previous item is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
     __syncthreads();
     const int t = s_tile;
@@ -58,23 +67,37 @@ batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
     } else {
       uin = flip ? I.B : I.A; u0 = uin; uout = flip ? I.A : I.B;
     }
+    StepCtrl* ctrl = I.ctrl;
+    const int x0 = bx * TL::TX, ya = by * ITEM_ROWS;
+    const int yb = ya + ITEM_ROWS < I.G.nb ? ya + ITEM_ROWS : I.G.nb;
+    if (!ctrl->active) {
+      if (kind == STAGE_EULER) pass_on64<WACT, TL::TX>(I.G, uin, uout, x0, ya, yb, threadIdx.x);
+      continue;
+    }
+    unsigned long long red = 0ull;
     if (I.G.pow2_all)
-      stage_tile64<PLANE, WACT, TL, true>(I.G, uin, u0, uout, I.ctrl, I.rs, kind, bx, by, smem_raw, s_red);
+      stage_segment64<PLANE, WACT, TL, true>(I.G, uin, u0, uout, ctrl, I.rs, kind, ctrl->dt_cur, x0, ya, yb, smem_raw,
+                                             nullptr, red);
     else
-      stage_tile64<PLANE, WACT, TL, false>(I.G, uin, u0, uout, I.ctrl, I.rs, kind, bx, by, smem_raw, s_red);
+      stage_segment64<PLANE, WACT, TL, false>(I.G, uin, u0, uout, ctrl, I.rs, kind, ctrl->dt_cur, x0, ya, yb,
+                                              smem_raw, nullptr, red);
+    if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[ctrl->parity ^ 1], s_red);
   }
 }
 
+template <int S>
+using BlockOf = Tile<kShapes64[S].tx, block_rows(kShapes64[S].tx)>;
+
 template <int PLANE, bool WACT, int S>
 auto kernel_for() {
-  using TL = Tile<kShapes64[S].tx, kShapes64[S].ty>;
-  return batch_stage64<PLANE, WACT, TL>;
+  return batch_stage64<PLANE, WACT, BlockOf<S>, kShapes64[S].ty>;
 }
 
+// wact groups (viscosity on, or a non-zero third velocity) get the largest
+// layout, the one with shared-face viscous fluxes.
 template <int S>
 size_t smem_for(bool wact, bool tc) {
-  using TL = Tile<kShapes64[S].tx, kShapes64[S].ty>;
-  return wact ? TileSmem<double, 5, TL>::bytes(tc) : TileSmem<double, 4, TL>::bytes(tc);
+  return wact ? TileSmem<double, 5, BlockOf<S>>::bytes_vface() : TileSmem<double, 4, BlockOf<S>>::bytes(tc);
 }
 
 typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);

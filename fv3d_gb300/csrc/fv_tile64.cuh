@@ -678,30 +678,69 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
   if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
-// One stage of a run of cell rows of problem G, marching down TX-wide strips.
-// The rows are numbered strip by strip (unit u = strip * nb + row) and the
-// CTA owns units [u0_, u1_); a strip segment is processed in blocks of TY
-// rows through a ring of TY + 4 primitive rows, so each block converts only
-// its TY new rows and reuses the b-face fluxes on the boundary with the
-// previous block (the arithmetic of every face and cell is that of the tile
-// body, so results are bit-identical; viscous fluxes of the face-only
-// branches are computed once per face, viscous_face).  Host code splits the units evenly
-// over the CTAs that fit on the GPU at once, which balances the FP64 work
-// per SM whatever the grid shape.
+// One strip segment: cell rows [ya, yb) of the TX-wide strip whose first
+// column is x0, marched in blocks of TY rows through a ring of TY + 4
+// primitive rows, so each block converts only its new rows and reuses the
+// b-face fluxes on the boundary with the previous block; with viscosity the
+// face-only viscous branches are computed once per face (viscous_face).  The
+// arithmetic of every face and cell is that of the tile body, so results are
+// bit-identical to it.  Every thread of the CTA calls it (ctrl active); the
+// CFL maximum is folded into red; smem holds bytes_vface() with viscosity,
+// else bytes(G.tc).
 template <int PLANE, bool WACT, class TL, bool P2>
-__device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
-                                              StepCtrl* ctrl, int rs, int kind, long long u0_, long long u1_,
-                                              double* smem, unsigned long long* s_red, const Fields* hout) {
+__device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin, const Fields& u0,
+                                                const Fields& uout, StepCtrl* ctrl, int rs, int kind, double dt,
+                                                int x0, int ya, int yb, double* smem, const Fields* hout,
+                                                unsigned long long& red) {
   constexpr int NV = WACT ? 5 : 4;
   constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
   using SM = TileSmem<double, NV, TL>;
   const SM S{smem};
   const int tid = threadIdx.x;
+  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
+  const bool vsh = WACT && G.visc;
+  int base = 0;
+  for (int y0 = ya; y0 < yb; y0 += TY) {
+    const int nr = yb - y0 < TY ? yb - y0 : TY;
+    const bool first = y0 == ya;
+    const PrimView<SM, RowsRing<HY>> V{S, RowsRing<HY>{base}};
+    if (!first) {  // b faces on the boundary with the previous (full) block
+      for (int i = tid; i < NV * TX; i += kTileThreads) {
+        const int v = i / TX, fx = i - v * TX;
+        const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
+        S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
+      }
+      if (vsh && PLANE == PLANE_XY)
+        for (int i = tid; i < 4 * TX; i += kTileThreads) {
+          const int k = i / TX, fx = i - k * TX;
+          S.vb(k, 0, fx) = S.vb(k, TY, fx);
+        }
+    }
+    load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, first ? 0 : 4, nr + 4, tid);
+    __syncthreads();
+    faces64<PLANE, WACT, TL, WACT>(G, K, V, rs, nr, first ? 0 : 1, tid);
+    __syncthreads();
+    update64<PLANE, WACT, TL, P2, WACT>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
+    __syncthreads();
+    base += TY;
+    if (base >= HY) base -= HY;
+  }
+}
+
+// One stage of a run of cell rows of problem G, marching down TX-wide strips.
+// The rows are numbered strip by strip (unit u = strip * nb + row) and the
+// CTA owns units [u0_, u1_), processed as strip segments (stage_segment64).
+// Host code splits the units evenly over the CTAs that fit on the GPU at
+// once, which balances the FP64 work per SM whatever the grid shape.
+template <int PLANE, bool WACT, class TL, bool P2>
+__device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                              StepCtrl* ctrl, int rs, int kind, long long u0_, long long u1_,
+                                              double* smem, unsigned long long* s_red, const Fields* hout) {
+  constexpr int TX = TL::TX;
+  const int tid = threadIdx.x;
   const int active = ctrl->active;
   const double dt = ctrl->dt_cur;
   const int parity = ctrl->parity;
-  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
-  const bool vsh = WACT && G.visc;  // shared-face viscous fluxes (smem: bytes_vface)
   unsigned long long red = 0ull;
   for (long long u = u0_; u < u1_;) {
     const int strip = (int)(u / G.nb);
@@ -713,32 +752,7 @@ __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, 
       if (kind == STAGE_EULER) pass_on64<WACT, TX>(G, uin, uout, x0, ya, yb, tid);
       continue;
     }
-    int base = 0;
-    for (int y0 = ya; y0 < yb; y0 += TY) {
-      const int nr = yb - y0 < TY ? yb - y0 : TY;
-      const bool first = y0 == ya;
-      const PrimView<SM, RowsRing<HY>> V{S, RowsRing<HY>{base}};
-      if (!first) {  // b faces on the boundary with the previous (full) block
-        for (int i = tid; i < NV * TX; i += kTileThreads) {
-          const int v = i / TX, fx = i - v * TX;
-          const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
-          S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
-        }
-        if (vsh && PLANE == PLANE_XY)
-          for (int i = tid; i < 4 * TX; i += kTileThreads) {
-            const int k = i / TX, fx = i - k * TX;
-            S.vb(k, 0, fx) = S.vb(k, TY, fx);
-          }
-      }
-      load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, first ? 0 : 4, nr + 4, tid);
-      __syncthreads();
-      faces64<PLANE, WACT, TL, WACT>(G, K, V, rs, nr, first ? 0 : 1, tid);
-      __syncthreads();
-      update64<PLANE, WACT, TL, P2, WACT>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
-      __syncthreads();
-      base += TY;
-      if (base >= HY) base -= HY;
-    }
+    stage_segment64<PLANE, WACT, TL, P2>(G, uin, u0, uout, ctrl, rs, kind, dt, x0, ya, yb, smem, hout, red);
   }
   if (active && kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
