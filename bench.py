@@ -521,14 +521,16 @@ def run_profile_case(args):
     workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
     batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
     512-instance set, to keep captures small), shear_mixed / shear_fp64 (the
-    4096^2 shear layer, a state larger than L2), fp64_3d / mixed_3d (a 160^3
-    random state, HLLC, PLM, RK2, conduction + viscosity: the 3-D kernels)."""
+    4096^2 shear layer, a state larger than L2; FP64 through fvgpu_create as
+    the bench times it), fp64_3d / mixed_3d (a 160^3 random state, HLLC, PLM,
+    RK2, conduction + viscosity: the 3-D kernels)."""
     import fv3d_gb300 as fv
     from fv3d_gb300 import problems
     case = args.profile_case
     n = args.warmup + args.steps
-    if case in ("fp64_rt", "fp64_3d"):
-        pr = problem() if case == "fp64_rt" else random_3d(160)
+    if case in ("fp64_rt", "fp64_3d", "shear_fp64"):
+        pr = {"fp64_rt": problem, "fp64_3d": lambda: random_3d(160),
+              "shear_fp64": lambda: problems.shear_layer(4096)}[case]()
         sim = fv.Simulation(pr.params)
         sim.set_prim(*pr.prim)
         sim.enqueue_steps(n)

@@ -44,11 +44,11 @@ constexpr int kTileY = FV_TILE2D_Y;
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                            Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
 
-// The same stage over a 3-D grid (G.ndim == 3): one CTA per 16 x 16 block of
-// columns and stage3d_layers_per_cta(G) z layers; always carries w.
+// The same stage over a 3-D grid (G.ndim == 3): 16 x 16 blocks of columns
+// marched over z, the (column block, layer) units split evenly over the
+// resident CTAs; always carries w.
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
                            StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
-int stage3d_layers_per_cta(const Grid& G);
 
 // The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
 inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,

@@ -32,6 +32,7 @@ namespace fv {
 namespace {
 
 constexpr int kTX = 16, kTY = 16;                // columns per CTA
+constexpr int kMinLayersPerCta = 8;              // the prologue loads 4 layers and one extra z face
 constexpr int kThreads = kTX * kTY;              // one thread per column
 constexpr int kHX = kTX + 4, kHY = kTY + 4;      // layer with halo
 constexpr int kLayer = kHX * kHY;
@@ -221,20 +222,20 @@ struct RingVel {
   }
 };
 
-// One stage for the columns (bx, by) and z chunk bz of tz layers; rs 0 HLL /
+// One stage for the columns (bx, by) and z layers [k0, k1); rs 0 HLL /
 // 1 HLLC, kind a StageKind (constants in the one-problem kernel, per work
 // item in the batch kernel); P2: every cell size is a power of two (callers
-// branch on it once, uniformly).  Every thread of the CTA must call it.
+// branch on it once, uniformly).  Every thread of the CTA must call it; the
+// CFL maximum is folded into red (the caller reduces it once per CTA or work
+// item).
 template <bool P2, bool CORR>
-__device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
-                                             StepCtrl* __restrict__ ctrl, int rs, int kind, int bx, int by, int bz,
-                                             int tz, const Fields& hout, double* smem_raw,
-                                             unsigned long long* s_red) {
+__device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin, const Fields& u0,
+                                                const Fields& uout, StepCtrl* __restrict__ ctrl, int rs, int kind,
+                                                int bx, int by, int k0, int k1, const Fields& hout, double* smem_raw,
+                                                unsigned long long& red) {
   const Smem3 S{smem_raw};
   const int tid = threadIdx.x;
   const int x0 = bx * kTX, y0 = by * kTY;
-  const int k0 = bz * tz;
-  const int k1 = min(k0 + tz, G.nc);
   const int cx = tid % kTX, cy = tid / kTX;
   const int x = x0 + cx, y = y0 + cy;
   const bool own = x < G.na && y < G.nb;
@@ -252,7 +253,6 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
     return;
   }
   const double dt = ctrl->dt_cur;
-  const int parity = ctrl->parity;
   const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
   const int recon = G.recon;
   const bool need_pout = G.wb_flux_z || G.bc_c == DBC_C91;
@@ -271,7 +271,6 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
   }
   __syncthreads();
 
-  unsigned long long red = 0ull;
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     // ---- 1. layer k+2 in, x and y faces of layer k ----
@@ -427,21 +426,67 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
     }
     __syncthreads();
   }
-  if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
+// One stage for the columns (bx, by) and z chunk bz of tz layers, reduced
+// (the batch kernel's work item).
+template <bool P2, bool CORR>
+__device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
+                                             StepCtrl* __restrict__ ctrl, int rs, int kind, int bx, int by, int bz,
+                                             int tz, const Fields& hout, double* smem_raw,
+                                             unsigned long long* s_red) {
+  const int active = ctrl->active, parity = ctrl->parity;
+  const int k0 = bz * tz;
+  const int k1 = min(k0 + tz, G.nc);
+  unsigned long long red = 0ull;
+  stage3d_segment<P2, CORR>(G, uin, u0, uout, ctrl, rs, kind, bx, by, k0, k1, hout, smem_raw, red);
+  if (active && kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+// Units [ub, ue) of the (column block, z layer) numbering, column block by
+// column block; returns the CTA's CFL maximum.
+template <bool P2, bool CORR, int RS, int KIND>
+__device__ __forceinline__ unsigned long long march3d(const Grid& G, const Fields& uin, const Fields& u0,
+                                                      const Fields& uout, StepCtrl* __restrict__ ctrl, long long ub,
+                                                      long long ue, const Fields& hout, double* smem_raw) {
+  const int tiles_x = (G.na + kTX - 1) / kTX;
+  unsigned long long red = 0ull;
+  for (long long u = ub; u < ue;) {
+    const int cb = (int)(u / G.nc);
+    const int k0 = (int)(u - (long long)cb * G.nc);
+    const int k1 = (int)(k0 + (ue - u) < (long long)G.nc ? k0 + (ue - u) : (long long)G.nc);
+    u += k1 - k0;
+    stage3d_segment<P2, CORR>(G, uin, u0, uout, ctrl, RS, KIND, cb % tiles_x, cb / tiles_x, k0, k1, hout, smem_raw,
+                              red);
+  }
+  return red;
+}
+
+// The one-problem kernel: the (column block, z layer) units, numbered column
+// block by column block, are split evenly over the CTAs that fit on the GPU
+// at once; a CTA marches each column block of its range over its layers.
 template <int RS, int KIND, bool CORR>
 __global__ void __launch_bounds__(kThreads, 2)
 stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             int tz, const Fields hout) {
+             long long units, const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
-  if (G.pow2_all)
-    stage3d_body<true, CORR>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, blockIdx.z, tz, hout,
-                             smem_raw, s_red);
-  else
-    stage3d_body<false, CORR>(G, uin, u0, uout, ctrl, RS, KIND, blockIdx.x, blockIdx.y, blockIdx.z, tz, hout,
-                              smem_raw, s_red);
+  const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
+  const int active = ctrl->active, parity = ctrl->parity;
+  const unsigned long long red =
+      G.pow2_all ? march3d<true, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw)
+                 : march3d<false, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw);
+  if (active && KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+}
+
+int sm_count3d() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 1;
+  }
+  return n;
 }
 
 template <int RS, int KIND, bool CORR>
@@ -454,11 +499,21 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  const int tx = (G.na + kTX - 1) / kTX, ty = (G.nb + kTY - 1) / kTY;
-  const int tz = stage3d_layers_per_cta(G);
-  dim3 grid(tx, ty, (G.nc + tz - 1) / tz);
+  static int resident[2] = {0, 0};  // CTAs per SM without / with conduction
+  const int tc = G.tc != 0;
+  if (!resident[tc]) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[tc], kern, kThreads, Smem3::bytes(tc));
+    if (e != cudaSuccess) return e;
+    if (resident[tc] < 1) resident[tc] = 1;
+  }
+  const long long cols = (long long)((G.na + kTX - 1) / kTX) * ((G.nb + kTY - 1) / kTY);
+  const long long units = cols * G.nc;
+  long long ctas = units / kMinLayersPerCta;
+  const long long slots = (long long)resident[tc] * sm_count3d();
+  if (ctas > slots) ctas = slots;
+  if (ctas < 1) ctas = 1;
   const Fields none{};
-  kern<<<grid, kThreads, Smem3::bytes(G.tc != 0), st>>>(G, uin, u0, uout, ctrl, tz, hout ? *hout : none);
+  kern<<<(unsigned)ctas, kThreads, Smem3::bytes(tc), st>>>(G, uin, u0, uout, ctrl, units, hout ? *hout : none);
   return cudaGetLastError();
 }
 
@@ -575,20 +630,6 @@ cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles
   if (!batch3d_prepare()) return cudaErrorInvalidConfiguration;
   batch3d_kernel(kind, rs)<<<grid, kThreads, Smem3::bytes(tc), st>>>(insts, ninst, ntiles, queue, flip);
   return cudaGetLastError();
-}
-
-// z layers per CTA: enough CTAs to fill two waves of 2 CTAs on each of the
-// 152 SMs where the grid allows, at least 4 layers (the prologue loads four
-// layers and solves one extra z face per column).
-int stage3d_layers_per_cta(const Grid& G) {
-  const long long cols = (long long)((G.na + kTX - 1) / kTX) * ((G.nb + kTY - 1) / kTY);
-  const long long target = 2LL * 2 * 152;
-  long long chunks = (target + cols - 1) / cols;
-  if (chunks < 1) chunks = 1;
-  long long tz = (G.nc + chunks - 1) / chunks;
-  if (tz < 4) tz = 4;
-  if (tz > G.nc) tz = G.nc;
-  return (int)tz;
 }
 
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
