@@ -8,8 +8,15 @@ namespace fv {
 
 namespace {
 
-constexpr TileShape kShapes32[] = {{32, 16}, {64, 16}, {32, 32}, {64, 8}};
+// Work-item shapes (cells along a x rows along b): strip segments marched in
+// blocks of kBlockRows32 rows (32x16 or 64x16 cells), the item rows a whole
+// number of blocks; a one-block item is a plain tile.
+constexpr TileShape kShapes32[] = {{32, 32}, {64, 16}, {32, 16}, {64, 32}};
+constexpr int kBlockRows32[] = {16, 16, 16, 16};
 constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
+static_assert(kShapes32[0].ty % kBlockRows32[0] == 0 && kShapes32[1].ty % kBlockRows32[1] == 0 &&
+                  kShapes32[2].ty % kBlockRows32[2] == 0 && kShapes32[3].ty % kBlockRows32[3] == 0,
+              "item rows must be whole marching blocks");
 
 __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts, int ninst, int t,
                                              BatchInst* s_inst) {
@@ -30,7 +37,7 @@ __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts
 #define FV_MIXED_BOUNDS __launch_bounds__(kTileThreads)
 #endif
 
-template <int PLANE, bool WACT, class TL>
+template <int PLANE, bool WACT, class TL, int ITEM_ROWS>
 __global__ void FV_MIXED_BOUNDS
 batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ float smem_f[];
@@ -60,20 +67,35 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
       src[v] = (kind == STAGE_EULER && flip) ? b : a;
       dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
     }
-    stage_tile32<PLANE, WACT, TL>(I.G, M, src, dst, I.ctrl, I.rs, kind, bx, by, smem_f, s_red);
+    StepCtrl* ctrl = I.ctrl;
+    const int x0 = bx * TL::TX, ya = by * ITEM_ROWS;
+    const int yb = ya + ITEM_ROWS < I.G.nb ? ya + ITEM_ROWS : I.G.nb;
+    if (!ctrl->active) {
+      if (kind == STAGE_EULER) pass_on32<WACT, TL::TX>(I.G, src, dst, x0, ya, yb, threadIdx.x);
+      continue;
+    }
+    const float dt = (float)ctrl->dt_cur;  // the one FP64 -> FP32 conversion per item
+    float red = 0.0f;
+    bool bad = false;
+    stage_segment32<PLANE, WACT, TL>(I.G, M, src, dst, I.rs, kind, dt, x0, ya, yb, smem_f, red, bad);
+    if (kind != STAGE_RK_1) {
+      if (bad) atomicOr(&ctrl->err, 1);
+      block_max_atomic((unsigned long long)__double_as_longlong((double)red), &ctrl->slot[ctrl->parity ^ 1], s_red);
+    }
   }
 }
 
+template <int S>
+using BlockOf32 = Tile<kShapes32[S].tx, kBlockRows32[S]>;
+
 template <int PLANE, bool WACT, int S>
 auto kernel_for() {
-  using TL = Tile<kShapes32[S].tx, kShapes32[S].ty>;
-  return batch_stage32<PLANE, WACT, TL>;
+  return batch_stage32<PLANE, WACT, BlockOf32<S>, kShapes32[S].ty>;
 }
 
 template <int S>
 size_t smem_for(bool wact, bool tc) {
-  using TL = Tile<kShapes32[S].tx, kShapes32[S].ty>;
-  return wact ? TileSmem<float, 5, TL>::bytes(tc) : TileSmem<float, 4, TL>::bytes(tc);
+  return wact ? TileSmem<float, 5, BlockOf32<S>>::bytes(tc) : TileSmem<float, 4, BlockOf32<S>>::bytes(tc);
 }
 
 typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);

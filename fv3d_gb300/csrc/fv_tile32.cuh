@@ -216,54 +216,27 @@ __device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool pl
   from_slots<PLANE, DIR>(f, out);
 }
 
-// One mixed-precision stage of tile (bx, by).  Inputs per kind:
-//   STAGE_RK_1 : read U^n (pairs) -> write U* (FP32)
-//   STAGE_RK_2 : read U* (FP32) and U^n (pairs) -> write U^n+1 (pairs, over U^n)
-//   STAGE_EULER: read U^n (pairs in `src`) -> write U^n+1 (pairs in `dst`)
-template <int PLANE, bool WACT, class TL>
-__device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M, float2* const src[5],
-                                             float2* const dst[5], StepCtrl* ctrl, int rs, int kind, int bx, int by,
-                                             float* smem, unsigned long long* s_red) {
-  constexpr int NV = WACT ? 5 : 4;
-  constexpr int TX = TL::TX, TY = TL::TY, HX = TL::HX, HY = TL::HY;
-  const TileSmem<float, NV, TL> S{smem};
-  const int tid = threadIdx.x;
-  const int x0 = bx * TX, y0 = by * TY;
-  const int active = ctrl->active;
-  const int parity = ctrl->parity;
-  const bool in_pairs = kind != STAGE_RK_2;
-
-  if (!active) {
-    if (kind == STAGE_EULER) {
-      for (int c = tid; c < TL::CELLS; c += kTileThreads) {
-        const int x = x0 + c % TX, y = y0 + c / TX;
-        if (x < G.na && y < G.nb) {
-          const long long o = (long long)y * G.pitch + x;
-#pragma unroll
-          for (int v = 0; v < 5; ++v)
-            if (WACT || v != 3) dst[v][o] = src[v][o];
-        }
-      }
-    }
-    return;
-  }
-  const float dt = (float)ctrl->dt_cur;  // the one FP64 -> FP32 conversion per tile
-  const float gamma = G.gamma_f, gm1 = G.gm1_f;
-
-  // ---- 1. tile + halo -> primitives (and temperature) ----
-  // Batches of KB cells per thread: every load of a batch is issued before
-  // any of them is used, to keep many requests in flight.
-  constexpr int NCELL = HX * HY, KB = FV_MIXED_LOAD_BATCH;
-  for (int base = 0; base < NCELL; base += KB * kTileThreads) {
+// Phase 1: halo rows [h0, h1) of the block whose first cell is (x0, y0)
+// (halo row hy is cell row y0 + hy - 2), columns x0-2 .. x0+TX+1: the stage
+// input (pairs or U*) -> FP32 primitives (and temperature).  Batches of KB
+// cells per thread: every load of a batch is issued before any of them is
+// used, to keep many requests in flight.
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void load_prims32(const Grid& G, const MixedFields& M, float2* const src[5],
+                                             bool in_pairs, const PV& V, int x0, int y0, int h0, int h1, int tid) {
+  constexpr int HX = TL::HX, KB = FV_MIXED_LOAD_BATCH;
+  const float gm1 = G.gm1_f;
+  const int ncell = (h1 - h0) * HX;
+  for (int base = 0; base < ncell; base += KB * kTileThreads) {
     float2 w[KB][5];
     bool ok[KB], fa[KB], fb[KB];
 #pragma unroll
     for (int k = 0; k < KB; ++k) {
       const int idx = base + tid + k * kTileThreads;
-      ok[k] = idx < NCELL;
-      const int hy = idx / HX, hx = idx - hy * HX;
+      ok[k] = idx < ncell;
+      const int r = idx / HX, hx = idx - r * HX;
       const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa[k]);
-      const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb[k]);
+      const int sb = bc_source(y0 + h0 + r - 2, G.nb, G.bc_b, fb[k]);
       const long long o = (long long)sb * G.pitch + sa;
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -276,7 +249,8 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     for (int k = 0; k < KB; ++k) {
       if (!ok[k]) continue;
       const int idx = base + tid + k * kTileThreads;
-      const int hy = idx / HX, hx = idx - hy * HX;
+      const int r = idx / HX, hx = idx - r * HX;
+      const int hy = h0 + r;
       float u[5], q[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) u[v] = v == 4 ? w[k][v].x : w[k][v].x + w[k][v].y;
@@ -285,52 +259,68 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
       if (fb[k]) q[2] = -q[2];
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) S.q(v, hy, hx) = q[v];
-      if (G.tc) S.temp(hy, hx) = q[4] / q[0];
+        if (WACT || v != 3) V.q(v, hy, hx) = q[v];
+      if (G.tc) V.temp(hy, hx) = q[4] / q[0];
     }
   }
-  __syncthreads();
+}
 
-  // ---- 2. faces ----
+// Phase 2: a faces of cell rows 0..nr-1 and b faces of face rows fb0..nr.
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void faces32(const Grid& G, const PV& V, int rs, int nr, int fb0, int tid) {
+  constexpr int TX = TL::TX;
   const bool plm = G.recon == R_PLM;
   const bool wb_z = PLANE == PLANE_XZ && G.recon == R_PCM_WB;
-  const float g_dz = G.g_dz_f;
-  for (int it = tid; it < TL::NFA_PAD + TL::NFB; it += kTileThreads) {
+  const float g_dz = G.g_dz_f, gamma = G.gamma_f;
+  const int nfa = (TX + 1) * nr;
+  const int nfa_pad = (nfa + 31) & ~31;  // keeps each warp on one face kind
+  const int n = nfa_pad + TX * (nr + 1 - fb0);
+  for (int it = tid; it < n; it += kTileThreads) {
     float c[4][5], f[5];
-    if (it < TL::NFA_PAD) {
-      if (it >= TL::NFA) continue;
+    if (it < nfa_pad) {
+      if (it >= nfa) continue;
       const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + 2, fx + k) : 0.0f;
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? V.q(v, fy + 2, fx + k) : 0.0f;
       face_flux32<PLANE, 0>(c, rs, plm, wb_z, g_dz, gamma, G.inv_gm1_f, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) S.fa(v, fy, fx) = f[v];
+        if (WACT || v != 3) V.fa(v, fy, fx) = f[v];
     } else {
-      const int j = it - TL::NFA_PAD;
-      const int fy = j / TX, fx = j - fy * TX;
+      const int j = it - nfa_pad;
+      const int jy = j / TX, fx = j - jy * TX;
+      const int fy = fb0 + jy;
 #pragma unroll
       for (int k = 0; k < 4; ++k)
 #pragma unroll
-        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? S.q(v, fy + k, fx + 2) : 0.0f;
+        for (int v = 0; v < 5; ++v) c[k][v] = (WACT || v != 3) ? V.q(v, fy + k, fx + 2) : 0.0f;
       face_flux32<PLANE, 1>(c, rs, plm, wb_z, g_dz, gamma, G.inv_gm1_f, f);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        if (WACT || v != 3) S.fb(v, fy, fx) = f[v];
+        if (WACT || v != 3) V.fb(v, fy, fx) = f[v];
     }
   }
-  __syncthreads();
+}
 
-  // ---- 3-5. increments, accumulation on pairs, CFL term ----
+// Phase 3-5: increments, accumulation on pairs, CFL term for the cells of
+// rows 0..nr-1 of the block.  Inputs per kind:
+//   STAGE_RK_1 : read U^n (pairs) -> write U* (FP32)
+//   STAGE_RK_2 : read U* (FP32) and U^n (pairs) -> write U^n+1 (pairs, over U^n)
+//   STAGE_EULER: read U^n (pairs in `src`) -> write U^n+1 (pairs in `dst`)
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void update32(const Grid& G, const PV& V, const MixedFields& M, float2* const src[5],
+                                         float2* const dst[5], int kind, float dt, int x0, int y0, int nr, int tid,
+                                         float& red, bool& bad) {
+  constexpr int TX = TL::TX;
+  const bool in_pairs = kind != STAGE_RK_2;
   const float inv_db = PLANE == PLANE_XY ? G.inv_dy_f : G.inv_dz_f;
   const float dtdx = dt * G.inv_dx_f;
   const float dtdb = dt * inv_db;
-  float red = 0.0f;
-  bool bad = false;
+  const int ncell = TX * nr;
 #pragma unroll 1
-  for (int cidx = tid; cidx < TL::CELLS; cidx += kTileThreads) {
+  for (int cidx = tid; cidx < ncell; cidx += kTileThreads) {
     const int cx = cidx % TX, cy = cidx / TX;
     const int x = x0 + cx, y = y0 + cy;
     if (x >= G.na || y >= G.nb) continue;
@@ -338,10 +328,10 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     float du[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v)
-      du[v] = (S.fa(v, cy, cx) - S.fa(v, cy, cx + 1)) * dtdx + (S.fb(v, cy, cx) - S.fb(v, cy + 1, cx)) * dtdb;
+      du[v] = (V.fa(v, cy, cx) - V.fa(v, cy, cx + 1)) * dtdx + (V.fb(v, cy, cx) - V.fb(v, cy + 1, cx)) * dtdb;
     if (PLANE == PLANE_XZ && G.gravity) {
-      du[2] += dt * S.q(0, cy + 2, cx + 2) * G.g_f;
-      du[4] += dt * 0.5f * (S.fb(0, cy, cx) + S.fb(0, cy + 1, cx)) * G.g_f;
+      du[2] += dt * V.q(0, cy + 2, cx + 2) * G.g_f;
+      du[4] += dt * 0.5f * (V.fb(0, cy, cx) + V.fb(0, cy + 1, cx)) * G.g_f;
     }
     // stage input at this cell, as a pair
     float2 base[5];
@@ -361,15 +351,15 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     if (G.tc) {
       const float kf = G.kappa_f;
       const int hy = cy + 2, hx = cx + 2;
-      const float TC = S.temp(hy, hx);
-      const float FL = kf * (TC - S.temp(hy, hx - 1)) * G.inv_dx_f;
-      const float FR = kf * (S.temp(hy, hx + 1) - TC) * G.inv_dx_f;
-      const float FU = kf * (TC - S.temp(hy - 1, hx)) * inv_db;
-      const float FD = kf * (S.temp(hy + 1, hx) - TC) * inv_db;
+      const float TC = V.temp(hy, hx);
+      const float FL = kf * (TC - V.temp(hy, hx - 1)) * G.inv_dx_f;
+      const float FR = kf * (V.temp(hy, hx + 1) - TC) * G.inv_dx_f;
+      const float FU = kf * (TC - V.temp(hy - 1, hx)) * inv_db;
+      const float FD = kf * (V.temp(hy + 1, hx) - TC) * inv_db;
       du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
     }
     if (WACT && G.visc) {
-      PlaneVel<PLANE, TileSmem<float, NV, TL>> P{S, cy + 2, cx + 2};
+      PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
       float vf[3][5];
       viscous_plane<PLANE, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
 #pragma unroll
@@ -408,9 +398,78 @@ __device__ __forceinline__ void stage_tile32(const Grid& G, const MixedFields& M
     bad |= !(inv <= 3.0e38f);  // NaN / inf: reported through the error flag
     red = fmaxf(red, inv);
   }
-  if (kind != STAGE_RK_1) {
-    if (bad) atomicOr(&ctrl->err, 1);
-    block_max_atomic((unsigned long long)__double_as_longlong((double)red), &ctrl->slot[parity ^ 1], s_red);
+}
+
+// Moves halo rows TY..TY+3 of the previous block to rows 0..3 (the rows the
+// next block shares with it).  Each cell is moved by the thread that the
+// next load_prims32 (rows 4..) assigns to the cell's old row, so program
+// order alone keeps the move ahead of that thread's overwrite.
+template <bool WACT, class TL, class SM>
+__device__ __forceinline__ void carry_rows32(const Grid& G, const SM& S, int tid) {
+  constexpr int HX = TL::HX, TY = TL::TY;
+  int idx = tid;  // load index (rows from 4) of this thread's cells
+  while (idx < (TY - 4) * HX) idx += kTileThreads;
+  for (; idx < TY * HX; idx += kTileThreads) {
+    const int hy = 4 + idx / HX, hx = idx % HX;
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3) S.q(v, hy - TY, hx) = S.q(v, hy, hx);
+    if (G.tc) S.temp(hy - TY, hx) = S.temp(hy, hx);
+  }
+}
+
+// One mixed-precision stage of the strip segment of cell rows [ya, yb) of
+// the TX-wide strip whose first column is x0, marched in blocks of TY rows
+// (each block converts only its new rows: the 4 rows it shares with the
+// previous block are moved down, carry_rows32, and the b faces on the
+// boundary are reused), the arithmetic of every face and cell that of the
+// tile form.  Every thread of the CTA calls it; the CFL maximum and the
+// non-finite flag are folded into red / bad; smem holds
+// TileSmem<float, NV, TL>::bytes(G.tc) bytes.
+template <int PLANE, bool WACT, class TL>
+__device__ __forceinline__ void stage_segment32(const Grid& G, const MixedFields& M, float2* const src[5],
+                                                float2* const dst[5], int rs, int kind, float dt, int x0, int ya,
+                                                int yb, float* smem, float& red, bool& bad) {
+  constexpr int NV = WACT ? 5 : 4;
+  constexpr int TX = TL::TX, TY = TL::TY;
+  using SM = TileSmem<float, NV, TL>;
+  const SM S{smem};
+  const int tid = threadIdx.x;
+  const bool in_pairs = kind != STAGE_RK_2;
+  const PrimView<SM, RowsDirect> V{S, RowsDirect{}};
+  for (int y0 = ya; y0 < yb; y0 += TY) {
+    const int nr = yb - y0 < TY ? yb - y0 : TY;
+    const bool first = y0 == ya;
+    if (!first) {  // rows and b faces shared with the previous (full) block
+      for (int i = tid; i < NV * TX; i += kTileThreads) {
+        const int v = i / TX, fx = i - v * TX;
+        const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
+        S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
+      }
+      carry_rows32<WACT, TL>(G, S, tid);
+    }
+    load_prims32<PLANE, WACT, TL>(G, M, src, in_pairs, V, x0, y0, first ? 0 : 4, nr + 4, tid);
+    __syncthreads();
+    faces32<PLANE, WACT, TL>(G, V, rs, nr, first ? 0 : 1, tid);
+    __syncthreads();
+    update32<PLANE, WACT, TL>(G, V, M, src, dst, kind, dt, x0, y0, nr, tid, red, bad);
+    __syncthreads();
+  }
+}
+
+// An inactive mixed Euler step hands its state on (ping-pong pairs).
+template <bool WACT, int TX>
+__device__ __forceinline__ void pass_on32(const Grid& G, float2* const src[5], float2* const dst[5], int x0, int y0,
+                                          int y1, int tid) {
+  const int n = TX * (y1 - y0);
+  for (int c = tid; c < n; c += kTileThreads) {
+    const int x = x0 + c % TX, y = y0 + c / TX;
+    if (x < G.na && y < G.nb) {
+      const long long o = (long long)y * G.pitch + x;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) dst[v][o] = src[v][o];
+    }
   }
 }
 

@@ -419,12 +419,12 @@ template <class SM, class RM>
 struct PrimView {
   SM s;
   RM rows;
-  __device__ __forceinline__ double& q(int v, int hy, int hx) const { return s.q(v, rows(hy), hx); }
-  __device__ __forceinline__ double& temp(int hy, int hx) const { return s.temp(rows(hy), hx); }
-  __device__ __forceinline__ double& fa(int v, int fy, int fx) const { return s.fa(v, fy, fx); }
-  __device__ __forceinline__ double& fb(int v, int fy, int fx) const { return s.fb(v, fy, fx); }
-  __device__ __forceinline__ double& va(int k, int fy, int fx) const { return s.va(k, fy, fx); }
-  __device__ __forceinline__ double& vb(int k, int fy, int fx) const { return s.vb(k, fy, fx); }
+  __device__ __forceinline__ auto& q(int v, int hy, int hx) const { return s.q(v, rows(hy), hx); }
+  __device__ __forceinline__ auto& temp(int hy, int hx) const { return s.temp(rows(hy), hx); }
+  __device__ __forceinline__ auto& fa(int v, int fy, int fx) const { return s.fa(v, fy, fx); }
+  __device__ __forceinline__ auto& fb(int v, int fy, int fx) const { return s.fb(v, fy, fx); }
+  __device__ __forceinline__ auto& va(int k, int fy, int fx) const { return s.va(k, fy, fx); }
+  __device__ __forceinline__ auto& vb(int k, int fy, int fx) const { return s.vb(k, fy, fx); }
 };
 
 // Phase 1: halo rows [h0, h1) of the block whose first cell is (x0, y0),
