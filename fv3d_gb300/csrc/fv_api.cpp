@@ -41,6 +41,8 @@ struct fv_sim {
   double* d_kappa_z = nullptr;  // B02 face conductivities per z layer
   double* buf = nullptr;      // 3 states x 5 fields x fstride doubles
   Fields A{}, B{}, S{};       // A: state, B: U* / ping-pong, S: scratch
+  fv::TmaState tma[2];        // TMA descriptors of A and B (2-D plane kernels)
+  bool tma_ok = false;
   int cur = 0;                // Euler ping-pong: state in A (0) or B (1)
   StepCtrl* d_ctrl = nullptr;
   StepCtrl* h_ctrl = nullptr; // pinned mirror (read after synchronisation only)
@@ -321,6 +323,14 @@ enum StepMode { STEP_LOOP = -1, STEP_GIVEN_DT = 0, STEP_FIXED = 2 };
 // Launches the kernels of one time step (control + stages) on the stream.
 // STEP_GIVEN_DT uses the host-supplied dt; STEP_LOOP derives dt from the CFL
 // reduction and stops at the loop bound; STEP_FIXED derives dt with no bound.
+// The TMA descriptors of state u, when the stage kernel can use them.
+const fv::TmaState* TmaOf(const fv_sim* s, const Fields& u) {
+  if (!s->tma_ok) return nullptr;
+  if (u.f[0] == s->A.f[0]) return &s->tma[0];
+  if (u.f[0] == s->B.f[0]) return &s->tma[1];
+  return nullptr;
+}
+
 int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fields* hout = nullptr) {
   {
     Timed t(s, KC_DT);
@@ -332,14 +342,16 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fiel
   if (s->p.time_stepping == FV_TS_RK2) {
     {
       Timed t(s, KC_STAGE);
-      cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream);
+      cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream,
+                                       nullptr, TmaOf(s, s->A));
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 1 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
     {
       Timed t(s, KC_STAGE);
       cudaError_t e =
-          fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream, hout);
+          fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream, hout,
+                           TmaOf(s, s->B));
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 2 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
@@ -347,7 +359,8 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fiel
     Timed t(s, KC_STAGE);
     const Fields& in = Current(s);
     const Fields& out = s->cur == 0 ? s->B : s->A;
-    cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream, hout);
+    cudaError_t e =
+        fv::launch_stage(s->G, rs, fv::STAGE_EULER, s->wact, in, in, out, s->d_ctrl, s->stream, hout, TmaOf(s, in));
     if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "euler stage launch: %s", cudaGetErrorString(e));
     if (counting) t.done();
     s->cur ^= 1;
@@ -554,6 +567,8 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
   s->A = StateAt(s->buf, s->G.fstride);
   s->B = StateAt(s->buf + 5 * s->G.fstride, s->G.fstride);
   s->S = StateAt(s->buf + 10 * s->G.fstride, s->G.fstride);
+  s->tma_ok = s->G.ndim == 2 && fv::encode_tma_state(s->G, s->A, &s->tma[0]) &&
+              fv::encode_tma_state(s->G, s->B, &s->tma[1]);
   if (cudaMalloc(&s->d_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
       cudaMallocHost(&s->h_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
       cudaMalloc(&s->d_partial, kMaxTotalsBlocks * 10 * sizeof(double)) != cudaSuccess ||

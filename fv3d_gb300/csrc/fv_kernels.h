@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "fv_device.cuh"
+#include "fv_tma.cuh"
 
 namespace fv {
 
@@ -41,8 +42,17 @@ constexpr int kTileY = FV_TILE2D_Y;
 // the stage also writes the primitives of its result, storage order, to
 // unpadded arrays of na x rows values that the GPU can address (device or
 // host memory).
+// tin (optional): TMA descriptors of uin (encode_tma_state); interior
+// blocks are then staged by tensor copies instead of per-thread loads.
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                           Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
+                           Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
+                           const TmaState* tin = nullptr);
+
+// Encodes the TMA descriptors of state u of the 2-D problem G for the stage
+// kernel (tensor na x rows of doubles, row pitch G.pitch, boxes of
+// (kTileX + 4) x kTmaRows).  False when the driver's encoder is unavailable
+// or refuses the layout; the stage kernel then loads with plain loads.
+bool encode_tma_state(const Grid& G, const Fields& u, TmaState* tin);
 
 // The same stage over a 3-D grid (G.ndim == 3): 16 x 16 blocks of columns
 // marched over z, the (column block, layer) units split evenly over the
@@ -52,9 +62,10 @@ cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields u
 
 // The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
 inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                                Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr) {
+                                Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
+                                const TmaState* tin = nullptr) {
   if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream, hout);
-  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout);
+  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout, tin);
 }
 
 // primToCons (States.h:20-31) from primitive arrays the GPU can address

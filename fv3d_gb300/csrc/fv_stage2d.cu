@@ -4,6 +4,7 @@
 // the reference).  The strip rows are split evenly over as many CTAs as the
 // GPU holds at once, so every SM gets the same FP64 work.
 #include "fv_tile64.cuh"
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
 namespace fv {
 
@@ -12,18 +13,35 @@ namespace {
 using SingleTile = Tile<kTileX, kTileY>;
 constexpr int kMinRowsPerCta = 4;
 
+// Dynamic shared memory is over-allocated by this much and aligned up, so
+// that tensor copies land on 128-byte boundaries.
+constexpr size_t kSmemAlign = 128;
+
 template <int PLANE, int RS, int KIND, bool WACT>
 __global__ void __launch_bounds__(kTileThreads, WACT ? FV_FP64_MIN_CTAS_W : FV_FP64_MIN_CTAS)
 stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             const Fields hout, long long units) {
-  extern __shared__ double smem_raw[];
+             const Fields hout, long long units, const __grid_constant__ TmaState tin, int use_tma) {
+  extern __shared__ __align__(128) unsigned char smem_bytes[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
+  __shared__ __align__(8) unsigned long long s_mbar;
+  const unsigned sa = smem_u32(smem_bytes);
+  double* smem = reinterpret_cast<double*>(smem_bytes + (((sa + kSmemAlign - 1) & ~(unsigned)(kSmemAlign - 1)) - sa));
+  if (use_tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(&s_mbar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+  }
+  const TmaState* tp = use_tma ? &tin : nullptr;
   const Fields* ho = hout.f[0] ? &hout : nullptr;
   const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   if (G.pow2_all)
-    stage_strip64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem_raw, s_red, ho);
+    stage_strip64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem, s_red, ho, tp,
+                                                 &s_mbar);
   else
-    stage_strip64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem_raw, s_red, ho);
+    stage_strip64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem, s_red, ho, tp,
+                                                  &s_mbar);
 }
 
 int sm_count() {
@@ -38,19 +56,19 @@ int sm_count() {
 
 template <int PLANE, int RS, int KIND, bool WACT>
 cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, const Fields* hout,
-                       cudaStream_t st) {
+                       const TmaState* tin, cudaStream_t st) {
   using SM = TileSmem<double, WACT ? 5 : 4, SingleTile>;
   auto kern = stage2d_fp64<PLANE, RS, KIND, WACT>;
   static bool attr_set = false;  // per instantiation, once per process
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(WACT ? SM::bytes_vface() : SM::bytes(true)));
+                                         (int)((WACT ? SM::bytes_vface() : SM::bytes(true)) + kSmemAlign));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   static int resident[3] = {0, 0, 0};  // CTAs per SM: plain / conduction / shared-face viscosity
   const int cfg = WACT && G.visc ? 2 : (G.tc != 0);
-  const size_t smem = cfg == 2 ? SM::bytes_vface() : SM::bytes(cfg == 1);
+  const size_t smem = (cfg == 2 ? SM::bytes_vface() : SM::bytes(cfg == 1)) + kSmemAlign;
   if (!resident[cfg]) {
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[cfg], kern, kTileThreads, smem);
     if (e != cudaSuccess) return e;
@@ -62,36 +80,65 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   if (ctas > slots) ctas = slots;
   if (ctas < 1) ctas = 1;
   const Fields none{};
-  kern<<<(unsigned)ctas, kTileThreads, smem, st>>>(G, uin, u0, uout, ctrl, hout ? *hout : none, units);
+  static const TmaState no_tma{};
+  kern<<<(unsigned)ctas, kTileThreads, smem, st>>>(G, uin, u0, uout, ctrl, hout ? *hout : none, units,
+                                                   tin ? *tin : no_tma, tin ? 1 : 0);
   return cudaGetLastError();
 }
 
 template <int PLANE, int RS, bool WACT>
 cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                        const Fields* hout, cudaStream_t st) {
+                        const Fields* hout, const TmaState* tin, cudaStream_t st) {
   switch (kind) {
-    case STAGE_EULER: return launch_one<PLANE, RS, STAGE_EULER, WACT>(G, uin, u0, uout, ctrl, hout, st);
-    case STAGE_RK_1: return launch_one<PLANE, RS, STAGE_RK_1, WACT>(G, uin, u0, uout, ctrl, nullptr, st);
-    default: return launch_one<PLANE, RS, STAGE_RK_2, WACT>(G, uin, u0, uout, ctrl, hout, st);
+    case STAGE_EULER: return launch_one<PLANE, RS, STAGE_EULER, WACT>(G, uin, u0, uout, ctrl, hout, tin, st);
+    case STAGE_RK_1: return launch_one<PLANE, RS, STAGE_RK_1, WACT>(G, uin, u0, uout, ctrl, nullptr, tin, st);
+    default: return launch_one<PLANE, RS, STAGE_RK_2, WACT>(G, uin, u0, uout, ctrl, hout, tin, st);
   }
 }
 
 template <int PLANE, int RS>
 cudaError_t launch_w(const Grid& G, int kind, bool wact, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                     const Fields* hout, cudaStream_t st) {
-  return wact ? launch_kind<PLANE, RS, true>(G, kind, uin, u0, uout, ctrl, hout, st)
-              : launch_kind<PLANE, RS, false>(G, kind, uin, u0, uout, ctrl, hout, st);
+                     const Fields* hout, const TmaState* tin, cudaStream_t st) {
+  return wact ? launch_kind<PLANE, RS, true>(G, kind, uin, u0, uout, ctrl, hout, tin, st)
+              : launch_kind<PLANE, RS, false>(G, kind, uin, u0, uout, ctrl, hout, tin, st);
 }
 
 }  // namespace
 
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                           Fields uout, StepCtrl* ctrl, cudaStream_t st, const Fields* hout) {
+                           Fields uout, StepCtrl* ctrl, cudaStream_t st, const Fields* hout, const TmaState* tin) {
   if (G.plane == PLANE_XY)
-    return riemann_solver == 0 ? launch_w<PLANE_XY, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, st)
-                               : launch_w<PLANE_XY, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, st);
-  return riemann_solver == 0 ? launch_w<PLANE_XZ, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, st)
-                             : launch_w<PLANE_XZ, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, st);
+    return riemann_solver == 0 ? launch_w<PLANE_XY, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st)
+                               : launch_w<PLANE_XY, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st);
+  return riemann_solver == 0 ? launch_w<PLANE_XZ, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st)
+                             : launch_w<PLANE_XZ, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st);
+}
+
+bool encode_tma_state(const Grid& G, const Fields& u, TmaState* tin) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (!encode || G.ndim != 2) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)G.na, (cuuint64_t)G.rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)G.pitch * sizeof(double)};  // bytes, a multiple of 128
+  const cuuint32_t box[2] = {(cuuint32_t)(kTileX + 4), (cuuint32_t)kTmaRows};
+  const cuuint32_t estr[2] = {1, 1};
+  for (int v = 0; v < 5; ++v) {
+    if (!u.f[v] || (reinterpret_cast<uintptr_t>(u.f[v]) & 15u)) return false;
+    if (encode(&tin->m[v], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, u.f[v], dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
 }
 
 }  // namespace fv

@@ -488,6 +488,56 @@ __device__ __forceinline__ void visc_faces64(const Grid& G, const PV& V, int nr,
   }
 }
 
+// Phase 1 for an interior block whose halo rows [h0, h1) were staged by
+// tensor copies: the conserved values sit in the primitive slots of their
+// own cells and are converted in place (the arithmetic of load_prims64; no
+// ghost cells, so no reflections).
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void convert_rows64(const Grid& G, const PV& V, int h0, int h1, int tid) {
+  constexpr int HX = TL::HX;
+  const int n = (h1 - h0) * HX;
+  for (int idx = tid; idx < n; idx += kTileThreads) {
+    const int r = idx / HX, hx = idx - r * HX;
+    const int hy = h0 + r;
+    double u[5], q[5], y;
+    u[0] = V.q(0, hy, hx);
+    u[1] = V.q(1, hy, hx);
+    u[2] = V.q(2, hy, hx);
+    u[3] = WACT ? V.q(3, hy, hx) : 0.0;
+    u[4] = V.q(4, hy, hx);
+    cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      if (WACT || v != 3) V.q(v, hy, hx) = q[v];
+    if (G.tc) V.temp(hy, hx) = div_by_rcp(q[4], q[0], y);
+  }
+}
+
+// Stages halo rows [h0, h1) (a multiple of kTmaRows, never wrapping the
+// ring inside a chunk) of the block whose first cell is (x0, y0) into the
+// primitive slots by tensor copies, and waits for them.  Every thread calls
+// it; thread 0 issues.  The caller has synchronised the CTA since the slots
+// were last read.  Returns false when the wait ran out (ctrl->err is set).
+template <bool WACT, class TL, class PV>
+__device__ __forceinline__ bool stage_rows_tma(const TmaState* tin, const PV& V, unsigned long long* mbar,
+                                               unsigned& phase, int x0, int y0, int h0, int h1, StepCtrl* ctrl) {
+  constexpr int HX = TL::HX;
+  if (threadIdx.x == 0) {
+    fence_proxy_async();
+    const unsigned nf = WACT ? 5u : 4u;
+    mbar_arrive_expect_tx(mbar, nf * (unsigned)(h1 - h0) * HX * (unsigned)sizeof(double));
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if (!WACT && v == 3) continue;
+      for (int hy = h0; hy < h1; hy += kTmaRows) tma_load_2d(&V.q(v, hy, 0), &tin->m[v], x0 - 2, y0 - 2 + hy, mbar);
+    }
+  }
+  const bool ok = mbar_wait(mbar, phase);
+  phase ^= 1u;
+  if (!ok) atomicOr(&ctrl->err, 2);
+  return ok;
+}
+
 // Phase 2: a faces of cell rows 0..nr-1 and b faces of face rows fb0..nr of
 // the block (b face row fy lies between cell rows fy-1 and fy), each solved
 // once; with VSH, their viscous fluxes too.
@@ -687,11 +737,16 @@ __device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, c
 // bit-identical to it.  Every thread of the CTA calls it (ctrl active); the
 // CFL maximum is folded into red; smem holds bytes_vface() with viscosity,
 // else bytes(G.tc).
+//
+// tin / mbar (optional, single-problem kernel): TMA descriptors of uin and
+// the CTA's mbarrier; full blocks whose halo lies inside the grid are then
+// staged by tensor copies (stage_rows_tma) and converted in place.
 template <int PLANE, bool WACT, class TL, bool P2>
 __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin, const Fields& u0,
                                                 const Fields& uout, StepCtrl* ctrl, int rs, int kind, double dt,
                                                 int x0, int ya, int yb, double* smem, const Fields* hout,
-                                                unsigned long long& red) {
+                                                unsigned long long& red, const TmaState* tin = nullptr,
+                                                unsigned long long* mbar = nullptr, unsigned* phase = nullptr) {
   constexpr int NV = WACT ? 5 : 4;
   constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
   using SM = TileSmem<double, NV, TL>;
@@ -716,7 +771,14 @@ __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin
           S.vb(k, 0, fx) = S.vb(k, TY, fx);
         }
     }
-    load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, first ? 0 : 4, nr + 4, tid);
+    const int h0 = first ? 0 : 4;
+    const bool staged = tin && nr == TY && x0 >= 2 && x0 + TX + 2 <= G.na && y0 + h0 >= 2 && y0 + TY + 2 <= G.nb;
+    if (staged) {
+      stage_rows_tma<WACT, TL>(tin, V, mbar, *phase, x0, y0, h0, TY + 4, ctrl);
+      convert_rows64<PLANE, WACT, TL>(G, V, h0, TY + 4, tid);
+    } else {
+      load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, h0, nr + 4, tid);
+    }
     __syncthreads();
     faces64<PLANE, WACT, TL, WACT>(G, K, V, rs, nr, first ? 0 : 1, tid);
     __syncthreads();
@@ -735,13 +797,15 @@ __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin
 template <int PLANE, bool WACT, class TL, bool P2>
 __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                               StepCtrl* ctrl, int rs, int kind, long long u0_, long long u1_,
-                                              double* smem, unsigned long long* s_red, const Fields* hout) {
+                                              double* smem, unsigned long long* s_red, const Fields* hout,
+                                              const TmaState* tin = nullptr, unsigned long long* mbar = nullptr) {
   constexpr int TX = TL::TX;
   const int tid = threadIdx.x;
   const int active = ctrl->active;
   const double dt = ctrl->dt_cur;
   const int parity = ctrl->parity;
   unsigned long long red = 0ull;
+  unsigned phase = 0u;
   for (long long u = u0_; u < u1_;) {
     const int strip = (int)(u / G.nb);
     const int ya = (int)(u - (long long)strip * G.nb);
@@ -752,7 +816,8 @@ __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, 
       if (kind == STAGE_EULER) pass_on64<WACT, TX>(G, uin, uout, x0, ya, yb, tid);
       continue;
     }
-    stage_segment64<PLANE, WACT, TL, P2>(G, uin, u0, uout, ctrl, rs, kind, dt, x0, ya, yb, smem, hout, red);
+    stage_segment64<PLANE, WACT, TL, P2>(G, uin, u0, uout, ctrl, rs, kind, dt, x0, ya, yb, smem, hout, red, tin,
+                                         mbar, &phase);
   }
   if (active && kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
