@@ -2,7 +2,7 @@
 // main.cpp (main.cpp:12-89) on the GB300 path.
 //
 //   fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]
-//                     [--write-ic state.bin]
+//                     [--write-ic state.bin] [--restart]
 //
 // Reads the same .ini file (readInifile semantics), sets the initial state,
 // and runs the reference's time loop: while (t + epsilon < tend) { dt =
@@ -23,6 +23,14 @@
 //
 // --device-loop runs the steps between two saves with fvgpu_advance (dt stays
 // on the GPU) instead of one compute_dt/step round trip per step.
+//
+// Checkpoint / restart: every save also writes <prefix>_restart.bin (the
+// conserved state, so a restarted run continues bit for bit; primitives in
+// the FP32-mixed form, which keeps no FP64 conserved state) and
+// <prefix>_restart.txt (time, next save time, counters, the snapshot list).
+// --restart resumes the run of the same prefix from its last save: the same
+// steps follow, the snapshots continue their numbering and the XDMF index
+// keeps the earlier ones.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -221,6 +229,40 @@ bool WriteXdmf(const std::string& path, const fv_params& p, const std::string& g
   return ok;
 }
 
+// The loop's position at a save, enough to resume it exactly.
+struct Checkpoint {
+  double t = 0.0, next_save = 0.0;
+  int ite = 0, next_log = 0, conserved = 1;
+  long steps = 0;
+  std::vector<std::pair<std::string, double>> snaps;
+};
+
+bool WriteCheckpoint(const std::string& prefix, const Checkpoint& c, const Fields& state) {
+  if (!WriteRaw(prefix + "_restart.bin", state)) return false;
+  FILE* f = std::fopen((prefix + "_restart.txt").c_str(), "w");
+  if (!f) return false;
+  std::fprintf(f, "fv3d-restart 1\nt %.17g\nnext_save %.17g\nite %d\nnext_log %d\nsteps %ld\nconserved %d\n", c.t,
+               c.next_save, c.ite, c.next_log, c.steps, c.conserved);
+  for (const auto& sn : c.snaps) std::fprintf(f, "snap %.17g %s\n", sn.second, sn.first.c_str());
+  const bool ok = std::ferror(f) == 0;
+  std::fclose(f);
+  return ok;
+}
+
+bool ReadCheckpoint(const std::string& prefix, size_t n, Checkpoint& c, Fields& state) {
+  FILE* f = std::fopen((prefix + "_restart.txt").c_str(), "r");
+  if (!f) return false;
+  char key[64], name[1024];
+  int version = 0;
+  bool ok = std::fscanf(f, "%63s %d", key, &version) == 2 && !std::strcmp(key, "fv3d-restart") && version == 1 &&
+            std::fscanf(f, " t %lg next_save %lg ite %d next_log %d steps %ld conserved %d", &c.t, &c.next_save,
+                        &c.ite, &c.next_log, &c.steps, &c.conserved) == 6;
+  double ts;
+  while (ok && std::fscanf(f, " snap %lg %1023s", &ts, name) == 2) c.snaps.emplace_back(name, ts);
+  std::fclose(f);
+  return ok && ReadRaw(prefix + "_restart.bin", n, state);
+}
+
 int Check(fv_sim* s, int rc, const char* what) {
   if (rc != FV_OK) std::fprintf(stderr, "%s: %s (%s)\n", what, fv_status_string(rc), fvgpu_last_error(s));
   return rc;
@@ -231,13 +273,15 @@ int Check(fv_sim* s, int rc, const char* what) {
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr,
-                 "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop] [--write-ic state.bin]\n");
+                 "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop] [--write-ic state.bin] "
+                 "[--restart]\n");
     return 2;
   }
   std::string ini = argv[1], ic, out, write_ic;
-  bool device_loop = false;
+  bool device_loop = false, restart = false;
   for (int a = 2; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--ic") && a + 1 < argc) ic = argv[++a];
+    else if (!std::strcmp(argv[a], "--restart")) restart = true;
     else if (!std::strcmp(argv[a], "--out") && a + 1 < argc) out = argv[++a];
     else if (!std::strcmp(argv[a], "--device-loop")) device_loop = true;
     else if (!std::strcmp(argv[a], "--write-ic") && a + 1 < argc) write_ic = argv[++a];
@@ -251,7 +295,13 @@ int main(int argc, char** argv) {
   if (out.empty()) out = p.filename_out;
   const size_t n = (size_t)p.Nx * p.Ny * p.Nz;
   Fields q;
-  if (!ic.empty()) {
+  Checkpoint ck;
+  if (restart) {
+    if (!ReadCheckpoint(out, n, ck, q)) {
+      std::fprintf(stderr, "cannot read the checkpoint %s_restart.txt / .bin\n", out.c_str());
+      return 1;
+    }
+  } else if (!ic.empty()) {
     if (!ReadRaw(ic, n, q)) {
       std::fprintf(stderr, "cannot read %zu cells from %s\n", n, ic.c_str());
       return 1;
@@ -266,17 +316,22 @@ int main(int argc, char** argv) {
   }
   fv_sim* s = nullptr;
   if (Check(s, fvgpu_create(&p, &s), "fvgpu_create")) return 1;
-  if (Check(s, fvgpu_set_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data()),
-            "set_prim"))
+  const double* qs[5] = {q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data()};
+  if (restart && ck.conserved) {
+    if (Check(s, fvgpu_set_cons(s, qs[0], qs[1], qs[2], qs[3], qs[4]), "set_cons")) return 1;
+  } else if (Check(s, fvgpu_set_prim(s, qs[0], qs[1], qs[2], qs[3], qs[4]), "set_prim")) {
     return 1;
+  }
+  const bool fp64 = p.precision == FV_PREC_FP64;
 
-  double t = 0.0, dt = 0.0, next_save = 0.0;
-  int ite = 0, next_log = 0;
-  long steps = 0;
+  double t = ck.t, dt = 0.0, next_save = ck.next_save;
+  int ite = ck.ite, next_log = ck.next_log;
+  long steps = ck.steps;
   // the loop announces its saves (main.cpp:64); the final one is silent (main.cpp:76)
-  std::vector<std::pair<std::string, double>> snaps;
+  std::vector<std::pair<std::string, double>> snaps = ck.snaps;
   const std::string grid = out + "_grid.bin";
-  auto save = [&](double tt, bool announce) {
+  Fields cons;
+  auto save = [&](double tt, bool announce, double next) {
     fvgpu_get_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data());
     char name[512];
     std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite++);
@@ -285,6 +340,20 @@ int main(int argc, char** argv) {
     WriteRaw(name, q);
     snaps.emplace_back(BaseName(name), tt);
     WriteXdmf(out + ".xdmf", p, BaseName(grid), snaps);
+    Checkpoint c;
+    c.t = tt;
+    c.next_save = next;
+    c.ite = ite;
+    c.next_log = next_log;
+    c.steps = steps;
+    c.conserved = fp64 ? 1 : 0;
+    c.snaps = snaps;
+    if (fp64) {
+      for (auto& v : cons.f) v.resize(n);
+      fvgpu_get_cons(s, cons.f[0].data(), cons.f[1].data(), cons.f[2].data(), cons.f[3].data(), cons.f[4].data());
+    }
+    if (!WriteCheckpoint(out, c, fp64 ? cons : q))
+      std::fprintf(stderr, "cannot write the checkpoint of %s\n", out.c_str());
   };
   while (t + p.epsilon < p.tend) {
     const bool save_needed = (t + p.epsilon > next_save);
@@ -298,7 +367,7 @@ int main(int argc, char** argv) {
       next_log--;
     }
     if (save_needed) {
-      save(t, true);
+      save(t, true, next_save + p.save_freq);
       next_save += p.save_freq;
     }
     if (device_loop) {
@@ -318,7 +387,7 @@ int main(int argc, char** argv) {
       ++steps;
     }
   }
-  save(t, false);
+  save(t, false, next_save);
   std::printf("done: %ld steps, t = %.17g\n", steps, t);
   fvgpu_destroy(s);
   return 0;

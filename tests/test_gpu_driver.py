@@ -295,3 +295,46 @@ def test_driver_rejects_unknown_problem(tmp_path):
     r = subprocess.run([exe, str(ini)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1
     assert "unknown problem" in r.stderr
+
+
+@pytest.mark.parametrize("mode", ["host", "device"])
+def test_driver_restart_continues_bit_for_bit(tmp_path, mode):
+    """A run stopped at tend/2 and resumed with --restart ends in the same
+    state, bit for bit, as the uninterrupted run (the checkpoint holds the
+    conserved state), and the XDMF index keeps every snapshot."""
+    exe = os.path.join(build.lib_dir(), "fv3d")
+    extra = ["--device-loop"] if mode == "device" else []
+    full = tmp_path / "full"
+    part = tmp_path / "part"
+    full.mkdir()
+    part.mkdir()
+    (full / "run.ini").write_text(INI)
+    r = subprocess.run([exe, str(full / "run.ini"), "--out", str(full / "snap")] + extra, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    n_full = int(re.search(r"done: (\d+) steps", r.stdout).group(1))
+    (part / "half.ini").write_text(INI.replace("tend=0.05", "tend=0.025"))
+    (part / "run.ini").write_text(INI)
+    r = subprocess.run([exe, str(part / "half.ini"), "--out", str(part / "snap")] + extra, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    n_half = int(re.search(r"done: (\d+) steps", r.stdout).group(1))
+    r = subprocess.run([exe, str(part / "run.ini"), "--out", str(part / "snap"), "--restart"] + extra,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
+    assert int(m.group(1)) == n_full > n_half
+    last = lambda d: sorted(f for f in os.listdir(d) if re.fullmatch(r"snap_\d{4}\.bin", f))[-1]
+    a = np.fromfile(str(full / last(full)), dtype=np.float64)
+    b = np.fromfile(str(part / last(part)), dtype=np.float64)
+    np.testing.assert_array_equal(a, b)
+    nsnaps = len([f for f in os.listdir(part) if re.fullmatch(r"snap_\d{4}\.bin", f)])
+    _check_xdmf(part, (1, 8, 64), nsnaps)
+
+
+def test_driver_restart_needs_a_checkpoint(tmp_path):
+    exe = os.path.join(build.lib_dir(), "fv3d")
+    (tmp_path / "run.ini").write_text(INI)
+    r = subprocess.run([exe, str(tmp_path / "run.ini"), "--out", str(tmp_path / "none"), "--restart"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "checkpoint" in r.stderr
