@@ -359,6 +359,9 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
       du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
     }
     if (WACT && G.visc) {
+      // per cell: the shared-face form (viscous_face) needs 17 KB more shared
+      // memory per CTA, which costs this issue-bound kernel a resident CTA
+      // per SM and measured 5-14 % slower
       PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
       float vf[3][5];
       viscous_plane<PLANE, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);

@@ -244,30 +244,30 @@ struct PlaneVel {
 // evaluation serves both cells: g = {mu*t1, mu*t2, mu*t3, mu*(t . qi)} in the
 // branch's component order (vf[d][1..4]).  P is centred on the cell above
 // the face (the s = 1 side of Viscosity.h's loop).
-template <int PLANE, int DIR, class PA>
-__device__ __forceinline__ void viscous_face(const PA& P, double odx, double ody, double odz, double mu, double g[4]) {
-  const double four_thirds = 4.0 / 3.0;
-  const double two_thirds = 2.0 / 3.0;
+template <int PLANE, int DIR, class T, class PA>
+__device__ __forceinline__ void viscous_face(const PA& P, T odx, T ody, T odz, T mu, T g[4]) {
+  const T four_thirds = T(4.0 / 3.0);
+  const T two_thirds = T(2.0 / 3.0);
   const int U = 1, V = 2, W = 3;
   if (DIR == 0) {
-    const double qiu = half64(P(1, 1, U) + P(1, 0, U));
-    const double qiv = half64(P(1, 1, V) + P(1, 0, V));
-    const double qiw = half64(P(1, 1, W) + P(1, 0, W));
-    const double dudx = odx * (P(1, 1, U) - P(1, 0, U));
-    const double dvdx = odx * (P(1, 1, V) - P(1, 0, V));
-    const double dwdx = odx * (P(1, 1, W) - P(1, 0, W));
-    double tau_xx, tau_xy, tau_xz;
+    const T qiu = half_of(P(1, 1, U) + P(1, 0, U));
+    const T qiv = half_of(P(1, 1, V) + P(1, 0, V));
+    const T qiw = half_of(P(1, 1, W) + P(1, 0, W));
+    const T dudx = odx * (P(1, 1, U) - P(1, 0, U));
+    const T dvdx = odx * (P(1, 1, V) - P(1, 0, V));
+    const T dwdx = odx * (P(1, 1, W) - P(1, 0, W));
+    T tau_xx, tau_xy, tau_xz;
     if (PLANE == PLANE_XY) {
-      const double c4y = half64(half64(ody));
-      const double dudy = c4y * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
-      const double dvdy = c4y * (P(2, 1, V) - P(0, 1, V) + P(2, 0, V) - P(0, 0, V));
+      const T c4y = half_of(half_of(ody));
+      const T dudy = c4y * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
+      const T dvdy = c4y * (P(2, 1, V) - P(0, 1, V) + P(2, 0, V) - P(0, 0, V));
       tau_xx = four_thirds * dudx - two_thirds * dvdy;
       tau_xy = dvdx + dudy;
       tau_xz = dwdx;
     } else {
-      const double c4z = half64(half64(odz));
-      const double dudz = c4z * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
-      const double dwdz = c4z * (P(2, 1, W) - P(0, 1, W) + P(2, 0, W) - P(0, 0, W));
+      const T c4z = half_of(half_of(odz));
+      const T dudz = c4z * (P(2, 1, U) - P(0, 1, U) + P(2, 0, U) - P(0, 0, U));
+      const T dwdz = c4z * (P(2, 1, W) - P(0, 1, W) + P(2, 0, W) - P(0, 0, W));
       tau_xx = four_thirds * dudx - two_thirds * dwdz;
       tau_xy = dvdx;
       tau_xz = dwdx + dudz;
@@ -277,18 +277,18 @@ __device__ __forceinline__ void viscous_face(const PA& P, double odx, double ody
     g[2] = mu * tau_xz;
     g[3] = mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
   } else {
-    const double c4x = half64(half64(odx));
-    const double qiu = half64(P(1, 1, U) + P(0, 1, U));
-    const double qiv = half64(P(1, 1, V) + P(0, 1, V));
-    const double qiw = half64(P(1, 1, W) + P(0, 1, W));
-    const double dudy = ody * (P(1, 1, U) - P(0, 1, U));
-    const double dvdy = ody * (P(1, 1, V) - P(0, 1, V));
-    const double dwdy = ody * (P(1, 1, W) - P(0, 1, W));
-    const double dudx = c4x * (P(1, 2, U) - P(1, 0, U) + P(0, 2, U) - P(0, 0, U));
-    const double dvdx = c4x * (P(1, 2, V) - P(1, 0, V) + P(0, 2, V) - P(0, 0, V));
-    const double tau_yy = four_thirds * dvdy - two_thirds * dudx;
-    const double tau_xy = dvdx + dudy;
-    const double tau_yz = dwdy;
+    const T c4x = half_of(half_of(odx));
+    const T qiu = half_of(P(1, 1, U) + P(0, 1, U));
+    const T qiv = half_of(P(1, 1, V) + P(0, 1, V));
+    const T qiw = half_of(P(1, 1, W) + P(0, 1, W));
+    const T dudy = ody * (P(1, 1, U) - P(0, 1, U));
+    const T dvdy = ody * (P(1, 1, V) - P(0, 1, V));
+    const T dwdy = ody * (P(1, 1, W) - P(0, 1, W));
+    const T dudx = c4x * (P(1, 2, U) - P(1, 0, U) + P(0, 2, U) - P(0, 0, U));
+    const T dvdx = c4x * (P(1, 2, V) - P(1, 0, V) + P(0, 2, V) - P(0, 0, V));
+    const T tau_yy = four_thirds * dvdy - two_thirds * dudx;
+    const T tau_xy = dvdx + dudy;
+    const T tau_yz = dwdy;
     g[0] = mu * tau_xy;
     g[1] = mu * tau_yy;
     g[2] = mu * tau_yz;
@@ -301,20 +301,21 @@ __device__ __forceinline__ double plus_zero(double x) {
   const long long b = __double_as_longlong(x);
   return b == (long long)0x8000000000000000ull ? 0.0 : x;
 }
+__device__ __forceinline__ float plus_zero(float x) { return 0.0f + x; }
 
 // viscous_plane with the face-only branches taken from shared face fluxes:
 // gl[d] / gr[d] are viscous_face of the cell's lower / upper face along
 // branch d (d = 1 used in the x-y plane only).  vf[d][k+1] =
 // (0 + (-gl[d][k])) + gr[d][k], the reference's two accumulations; the
 // branches that read the cell itself are evaluated here.  Same bits as
-// viscous_plane.
-template <int PLANE, class PA>
-__device__ __forceinline__ void viscous_plane_shared(const PA& P, const double gl[2][4], const double gr[2][4],
-                                                     double odx, double odz, double mu, double vf[3][5]) {
+// viscous_plane in FP64.
+template <int PLANE, class T, class PA>
+__device__ __forceinline__ void viscous_plane_shared(const PA& P, const T gl[2][4], const T gr[2][4], T odx, T odz,
+                                                     T mu, T vf[3][5]) {
 #pragma unroll
   for (int d = 0; d < 3; ++d)
 #pragma unroll
-    for (int v = 0; v < 5; ++v) vf[d][v] = 0.0;
+    for (int v = 0; v < 5; ++v) vf[d][v] = T(0);
 #pragma unroll
   for (int k = 0; k < 4; ++k) vf[0][k + 1] = plus_zero(-gl[0][k]) + gr[0][k];
   if (PLANE == PLANE_XY) {
@@ -324,6 +325,51 @@ __device__ __forceinline__ void viscous_plane_shared(const PA& P, const double g
   } else {
     viscous_iz_xz(P, odx, odz, mu, vf[2]);
   }
+}
+
+// Viscous fluxes of the face-only branches for the faces of a block: a
+// faces of cell rows 0..nr-1 along IX; b faces of face rows fb0..nr along IY
+// in the x-y plane (the x-z plane's IZ branch belongs to the cells).
+template <int PLANE, class TL, class T, class PV>
+__device__ __forceinline__ void visc_faces(const PV& V, T odx, T ody, T odz, T mu, int nr, int fb0, int tid) {
+  constexpr int TX = TL::TX;
+  const int nfa = (TX + 1) * nr;
+  const int nfa_pad = (nfa + 31) & ~31;
+  const int n = nfa_pad + (PLANE == PLANE_XY ? TX * (nr + 1 - fb0) : 0);
+  for (int it = tid; it < n; it += kTileThreads) {
+    T g[4];
+    if (it < nfa_pad) {
+      if (it >= nfa) continue;
+      const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
+      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell right of a face
+      viscous_face<PLANE, 0>(P, odx, ody, odz, mu, g);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) V.va(k, fy, fx) = g[k];
+    } else {
+      const int j = it - nfa_pad;
+      const int jy = j / TX, fx = j - jy * TX;
+      const int fy = fb0 + jy;
+      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell above b face fy
+      viscous_face<PLANE, 1>(P, odx, ody, odz, mu, g);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) V.vb(k, fy, fx) = g[k];
+    }
+  }
+}
+
+// The shared-face viscous fluxes of cell (cy, cx) of a block.
+template <int PLANE, class T, class PV>
+__device__ __forceinline__ void visc_cell_shared(const PV& V, int cy, int cx, T odx, T odz, T mu, T vf[3][5]) {
+  const PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
+  T gl[2][4], gr[2][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    gl[0][k] = V.va(k, cy, cx);
+    gr[0][k] = V.va(k, cy, cx + 1);
+    gl[1][k] = PLANE == PLANE_XY ? V.vb(k, cy, cx) : T(0);
+    gr[1][k] = PLANE == PLANE_XY ? V.vb(k, cy + 1, cx) : T(0);
+  }
+  viscous_plane_shared<PLANE>(P, gl, gr, odx, odz, mu, vf);
 }
 
 // Slots of a sweep (swap_component, States.h:104-111) from storage order
@@ -459,35 +505,6 @@ __device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, c
   }
 }
 
-// Viscous fluxes of the same faces (VSH form): a faces along IX; b faces
-// along IY in the x-y plane (the x-z plane's IZ branch belongs to the cells).
-template <int PLANE, class TL, class PV>
-__device__ __forceinline__ void visc_faces64(const Grid& G, const PV& V, int nr, int fb0, int tid) {
-  constexpr int TX = TL::TX;
-  const int nfa = (TX + 1) * nr;
-  const int nfa_pad = (nfa + 31) & ~31;
-  const int n = nfa_pad + (PLANE == PLANE_XY ? TX * (nr + 1 - fb0) : 0);
-  for (int it = tid; it < n; it += kTileThreads) {
-    double g[4];
-    if (it < nfa_pad) {
-      if (it >= nfa) continue;
-      const int fy = it / (TX + 1), fx = it - fy * (TX + 1);
-      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell right of a face
-      viscous_face<PLANE, 0>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) V.va(k, fy, fx) = g[k];
-    } else {
-      const int j = it - nfa_pad;
-      const int jy = j / TX, fx = j - jy * TX;
-      const int fy = fb0 + jy;
-      const PlaneVel<PLANE, PV> P{V, fy + 2, fx + 2};  // the cell above b face fy
-      viscous_face<PLANE, 1>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) V.vb(k, fy, fx) = g[k];
-    }
-  }
-}
-
 // Phase 1 for an interior block whose halo rows [h0, h1) were staged by
 // tensor copies: the conserved values sit in the primitive slots of their
 // own cells and are converted in place (the arithmetic of load_prims64; no
@@ -577,7 +594,7 @@ __device__ __forceinline__ void faces64(const Grid& G, const Consts64& K, const 
         if (WACT || v != 3) V.fb(v, fy, fx) = f[v];
     }
   }
-  if (VSH && WACT && G.visc) visc_faces64<PLANE, TL>(G, V, nr, fb0, tid);
+  if (VSH && WACT && G.visc) visc_faces<PLANE, TL>(V, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, nr, fb0, tid);
 }
 
 // Phase 3-5: the cells of rows 0..nr-1 of the block -- conservative update,
@@ -632,15 +649,7 @@ __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Field
       PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
       double vf[3][5];
       if (VSH) {
-        double gl[2][4], gr[2][4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          gl[0][k] = V.va(k, cy, cx);
-          gr[0][k] = V.va(k, cy, cx + 1);
-          gl[1][k] = PLANE == PLANE_XY ? V.vb(k, cy, cx) : 0.0;
-          gr[1][k] = PLANE == PLANE_XY ? V.vb(k, cy + 1, cx) : 0.0;
-        }
-        viscous_plane_shared<PLANE>(P, gl, gr, G.inv_dx, G.inv_dz, G.mu, vf);
+        visc_cell_shared<PLANE>(V, cy, cx, G.inv_dx, G.inv_dz, G.mu, vf);
       } else {
         viscous_plane<PLANE, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
       }

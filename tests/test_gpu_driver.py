@@ -88,7 +88,7 @@ def test_driver_matches_oracle(tmp_path, mode):
     assert "Computing dts at (t=0)" in r.stdout
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
+    snaps = sorted(f for f in os.listdir(tmp_path) if re.fullmatch(r"snap_\d{4}\.bin", f))
     assert len(snaps) == r.stdout.count("Saving at time") + 1
 
     p = fv.parse_ini(INI)
@@ -162,7 +162,7 @@ def test_driver_3d_matches_oracle(tmp_path, problem):
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
+    snaps = sorted(f for f in os.listdir(tmp_path) if re.fullmatch(r"snap_\d{4}\.bin", f))
     p = fv.parse_ini(text)
     ora = pyoracle.Oracle(p)
     ora.set_prim(*_ic_3d(p, problem))
@@ -283,7 +283,7 @@ def test_driver_random_generators_match_oracle(tmp_path, problem):
     ora.set_prim(*q0)
     t_o, n_o = ora.advance(p.tend)
     assert (steps, t_end) == (n_o, t_o)
-    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("snap_") and f != "snap_grid.bin")
+    snaps = sorted(f for f in os.listdir(tmp_path) if re.fullmatch(r"snap_\d{4}\.bin", f))
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, *shape)
     np.testing.assert_array_equal(got, np.stack(ora.get_prim()))
 
