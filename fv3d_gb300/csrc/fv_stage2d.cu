@@ -11,7 +11,10 @@ namespace fv {
 namespace {
 
 using SingleTile = Tile<kTileX, kTileY>;
-constexpr int kMinRowsPerCta = 4;
+#ifndef FV_STRIP_MIN_ROWS
+#define FV_STRIP_MIN_ROWS 4
+#endif
+constexpr int kMinRowsPerCta = FV_STRIP_MIN_ROWS;  // fewer CTAs than that many rows each on small grids
 
 // Dynamic shared memory is over-allocated by this much and aligned up, so
 // that tensor copies land on 128-byte boundaries.

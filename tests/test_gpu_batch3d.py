@@ -110,3 +110,16 @@ def test_batch3d_rejects_what_it_does_not_run():
     with pytest.raises(fv.FvError) as e:
         fv.Simulation(_mixed(b02.params))
     assert e.value.status == 2
+
+
+def test_mixed_refuses_fields_of_2_32_cells_or_more():
+    """The FP32-mixed kernels address fields with 32-bit offsets; a grid
+    whose field reaches 2^32 cells is refused before anything is
+    allocated (the FP64 kernels use 64-bit offsets)."""
+    ini = ("[mesh]\nNx=1640\nNy=1640\nNz=1640\n[run]\nboundaries_x=periodic\nboundaries_y=periodic\n"
+           "boundaries_z=periodic\n[gpu]\nprecision=fp32_mixed\n")
+    p = fv.parse_ini(ini)
+    with pytest.raises(fv.FvError) as e:
+        fv.Batch([p])
+    assert e.value.status == 2
+    assert "2^32" in str(e.value)
