@@ -54,6 +54,7 @@ struct Group {
   bool tc = false;
   std::vector<int> members;
   int shape = 0;
+  int rows = 0;     // 2-D: rows per work item (0: the shape's)
   int ntiles = 0;
   int grid = 0;
   BatchInst* d_inst = nullptr;
@@ -201,13 +202,16 @@ cudaError_t LaunchStage(const fv_batch* b, const Group& g, const BatchInst* inst
                                         flip, grid, g.tc, b->stream);
 }
 
-// Descriptors of group g for tile shape `shape` (tile numbering per group).
-// 3-D groups: 16 x 16 column blocks and chunks of up to 16 z layers.
-std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, StepCtrl* ctrl_base, int* ntiles) {
+// Descriptors of group g for work-item shape `shape` with `rows` rows per
+// item (0: the shape's), work items numbered per group.  2-D items are strip
+// segments (BatchInst::tz = rows per item); 3-D groups: 16 x 16 column
+// blocks and chunks of up to 16 z layers.
+std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, StepCtrl* ctrl_base, int* ntiles,
+                                int rows = 0) {
   const fv::TileShape* shapes;
   NumShapes(b->precision, &shapes);
   const int tx = g.ndim == 3 ? fv::batch3d_columns() : shapes[shape].tx;
-  const int ty = g.ndim == 3 ? fv::batch3d_columns() : shapes[shape].ty;
+  const int ty = g.ndim == 3 ? fv::batch3d_columns() : (rows > 0 ? rows : shapes[shape].ty);
   std::vector<BatchInst> out;
   int t0 = 0;
   for (int i : g.members) {
@@ -219,7 +223,7 @@ std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, St
     I.ctrl = ctrl_base + i;
     I.tiles_x = (I.G.na + tx - 1) / tx;
     I.tiles_y = (I.G.nb + ty - 1) / ty;
-    I.tz = g.ndim == 3 ? std::min(I.G.nc, 16) : 1;
+    I.tz = g.ndim == 3 ? std::min(I.G.nc, 16) : ty;
     const int chunks = g.ndim == 3 ? (I.G.nc + I.tz - 1) / I.tz : 1;
     I.tile0 = t0;
     I.rs = b->p[i].riemann_solver == FV_HLL ? 0 : 1;
@@ -248,26 +252,52 @@ int Autotune(fv_batch* b, Group& g) {
   }
   const fv::TileShape* shapes;
   const int ns = NumShapes(b->precision, &shapes);
+  // the first shape of a strip width (its kernel serves every row count)
+  auto shape_of_tx = [&](int tx) {
+    for (int s = 0; s < ns; ++s)
+      if (shapes[s].tx == tx && Occupancy(b, g, s) > 0) return s;
+    return -1;
+  };
   if (const char* force = std::getenv("FV3D_TILE")) {
     int tx = 0, ty = 0;
-    if (std::sscanf(force, "%dx%d", &tx, &ty) == 2)
-      for (int s = 0; s < ns; ++s)
-        if (shapes[s].tx == tx && shapes[s].ty == ty && Occupancy(b, g, s) > 0) {
-          g.shape = s;
-          return FV_OK;
-        }
+    if (std::sscanf(force, "%dx%d", &tx, &ty) == 2 && ty > 0) {
+      const int s = shape_of_tx(tx);
+      if (s >= 0) {
+        g.shape = s;
+        g.rows = ty;
+        return FV_OK;
+      }
+    }
   }
   const std::string key = GroupKey(b, g);
   {
     std::lock_guard<std::mutex> lock(g_cache_mutex);
     LoadCache();
     auto it = g_cache.find(key);
-    if (it != g_cache.end())
-      for (int s = 0; s < ns; ++s)
-        if (shapes[s].tx == it->second.first && shapes[s].ty == it->second.second && Occupancy(b, g, s) > 0) {
-          g.shape = s;
-          return FV_OK;
-        }
+    if (it != g_cache.end() && it->second.second > 0) {
+      const int s = shape_of_tx(it->second.first);
+      if (s >= 0) {
+        g.shape = s;
+        g.rows = it->second.second;
+        return FV_OK;
+      }
+    }
+  }
+  // Candidates: every shape with its own rows, and per strip width the rows
+  // that give each resident CTA one work item's worth of strip rows (the
+  // balanced split for a few large problems).
+  std::vector<std::pair<int, int>> cand;
+  for (int s = 0; s < ns; ++s) cand.push_back({s, shapes[s].ty});
+  for (int s = 0; s < ns; ++s) {
+    if (shape_of_tx(shapes[s].tx) != s) continue;
+    long long units = 0;
+    for (int i : g.members) units += (long long)((b->G[i].na + shapes[s].tx - 1) / shapes[s].tx) * b->G[i].nb;
+    const long long slots = (long long)Occupancy(b, g, s) * SmCount();
+    if (slots <= 0) continue;
+    const int rows = (int)std::max(4LL, (units + slots - 1) / slots);
+    bool dup = false;
+    for (auto& c : cand) dup = dup || (shapes[c.first].tx == shapes[s].tx && c.second == rows);
+    if (!dup) cand.push_back({s, rows});
   }
   StepCtrl* tune_ctrl = nullptr;
   BatchInst* tune_inst = nullptr;
@@ -287,13 +317,14 @@ int Autotune(fv_batch* b, Group& g) {
   cudaEventCreate(&e1);
   const int kind = b->ts == FV_TS_RK2 ? fv::STAGE_RK_1 : fv::STAGE_EULER;
   float best = 1e30f;
-  int best_s = -1;
+  int best_c = -1;
   const int saved = g.shape;
-  for (int s = 0; s < ns; ++s) {
+  for (int c = 0; c < (int)cand.size(); ++c) {
+    const int s = cand[c].first;
     const int occ = Occupancy(b, g, s);
     if (occ <= 0) continue;
     int ntiles = 0;
-    std::vector<BatchInst> d = Describe(b, g, s, tune_ctrl, &ntiles);
+    std::vector<BatchInst> d = Describe(b, g, s, tune_ctrl, &ntiles, cand[c].second);
     cudaMemcpyAsync(tune_inst, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice, b->stream);
     g.shape = s;
     const int grid = std::min(occ * SmCount(), ntiles);
@@ -314,20 +345,21 @@ int Autotune(fv_batch* b, Group& g) {
     }
     if (tot < best) {
       best = tot;
-      best_s = s;
+      best_c = c;
     }
   }
-  g.shape = best_s < 0 ? saved : best_s;
+  g.shape = best_c < 0 ? saved : cand[best_c].first;
+  g.rows = best_c < 0 ? 0 : cand[best_c].second;
   cudaStreamSynchronize(b->stream);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(tune_ctrl);
   cudaFree(tune_inst);
   cudaFree(tune_queue);
-  if (best_s < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
+  if (best_c < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
   std::lock_guard<std::mutex> lock(g_cache_mutex);
-  g_cache[key] = {shapes[best_s].tx, shapes[best_s].ty};
-  SaveCacheEntry(key, shapes[best_s].tx, shapes[best_s].ty);
+  g_cache[key] = {shapes[g.shape].tx, g.rows};
+  SaveCacheEntry(key, shapes[g.shape].tx, g.rows);
   return FV_OK;
 }
 
@@ -368,7 +400,7 @@ int Prepare(fv_batch* b) {
   for (auto& g : b->groups) {
     int rc = Autotune(b, g);
     if (rc) return rc;
-    std::vector<BatchInst> d = Describe(b, g, g.shape, b->d_ctrl, &g.ntiles);
+    std::vector<BatchInst> d = Describe(b, g, g.shape, b->d_ctrl, &g.ntiles, g.rows);
     BCUDA(b, cudaMalloc(&g.d_inst, sizeof(BatchInst) * d.size()));
     BCUDA(b, cudaMemcpyAsync(g.d_inst, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice, b->stream));
     g.grid = std::max(1, std::min(Occupancy(b, g, g.shape) * SmCount(), g.ntiles));
@@ -705,7 +737,8 @@ int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_grou
   for (int g = 0; g < *ngroups && g < max_groups; ++g) {
     const bool d3 = b->groups[g].ndim == 3;
     if (tx) tx[g] = d3 ? fv::batch3d_columns() : shapes[b->groups[g].shape].tx;
-    if (ty) ty[g] = d3 ? fv::batch3d_columns() : shapes[b->groups[g].shape].ty;
+    if (ty) ty[g] = d3 ? fv::batch3d_columns()
+                       : (b->groups[g].rows > 0 ? b->groups[g].rows : shapes[b->groups[g].shape].ty);
   }
   return FV_OK;
 }

@@ -8,15 +8,14 @@ namespace fv {
 
 namespace {
 
-// Work-item shapes (cells along a x rows along b): strip segments marched in
-// blocks of kBlockRows32 rows (32x16 or 64x16 cells), the item rows a whole
-// number of blocks; a one-block item is a plain tile.
+// Work-item shapes (cells along a x rows along b) the autotuner starts from:
+// strip segments marched in blocks of 16 rows (32x16 or 64x16 cells); the
+// rows of an item are a run-time value (BatchInst::tz), so shapes of one
+// strip width share a kernel (kKernelOf32).
 constexpr TileShape kShapes32[] = {{32, 32}, {64, 16}, {32, 16}, {64, 32}};
 constexpr int kBlockRows32[] = {16, 16, 16, 16};
+constexpr int kKernelOf32[] = {0, 1, 0, 1};
 constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
-static_assert(kShapes32[0].ty % kBlockRows32[0] == 0 && kShapes32[1].ty % kBlockRows32[1] == 0 &&
-                  kShapes32[2].ty % kBlockRows32[2] == 0 && kShapes32[3].ty % kBlockRows32[3] == 0,
-              "item rows must be whole marching blocks");
 
 __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts, int ninst, int t,
                                              BatchInst* s_inst) {
@@ -37,7 +36,7 @@ __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts
 #define FV_MIXED_BOUNDS __launch_bounds__(kTileThreads)
 #endif
 
-template <int PLANE, bool WACT, class TL, int ITEM_ROWS>
+template <int PLANE, bool WACT, class TL>
 __global__ void FV_MIXED_BOUNDS
 batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ float smem_f[];
@@ -68,8 +67,8 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
       dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
     }
     StepCtrl* ctrl = I.ctrl;
-    const int x0 = bx * TL::TX, ya = by * ITEM_ROWS;
-    const int yb = ya + ITEM_ROWS < I.G.nb ? ya + ITEM_ROWS : I.G.nb;
+    const int x0 = bx * TL::TX, ya = by * I.tz;  // tz: rows per work item
+    const int yb = ya + I.tz < I.G.nb ? ya + I.tz : I.G.nb;
     if (!ctrl->active) {
       if (kind == STAGE_EULER) pass_on32<WACT, TL::TX>(I.G, src, dst, x0, ya, yb, threadIdx.x);
       continue;
@@ -90,7 +89,7 @@ using BlockOf32 = Tile<kShapes32[S].tx, kBlockRows32[S]>;
 
 template <int PLANE, bool WACT, int S>
 auto kernel_for() {
-  return batch_stage32<PLANE, WACT, BlockOf32<S>, kShapes32[S].ty>;
+  return batch_stage32<PLANE, WACT, BlockOf32<S>>;
 }
 
 template <int S>
@@ -102,12 +101,7 @@ typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
 
 template <int PLANE, bool WACT>
 BatchKernel pick(int shape) {
-  switch (shape) {
-    case 0: return kernel_for<PLANE, WACT, 0>();
-    case 1: return kernel_for<PLANE, WACT, 1>();
-    case 2: return kernel_for<PLANE, WACT, 2>();
-    default: return kernel_for<PLANE, WACT, 3>();
-  }
+  return kKernelOf32[shape] == 0 ? kernel_for<PLANE, WACT, 0>() : kernel_for<PLANE, WACT, 1>();
 }
 
 BatchKernel pick_any(int plane, bool wact, int shape) {

@@ -4,8 +4,8 @@
 // third-momentum layout): `grid` resident CTAs repeatedly take the next work
 // item from a global work-queue counter, find the problem owning it (binary
 // search over the problems' first item numbers), copy its descriptor to
-// shared memory and run it.  A work item is a tx x ty piece of one problem:
-// a strip segment of ty rows, marched in blocks of 512 cells
+// shared memory and run it.  A work item is a piece of one problem: a strip
+// segment of tx columns and BatchInst::tz rows, marched in blocks of 512 cells
 // (stage_segment64), so consecutive blocks share boundary rows and faces.
 // Each problem keeps its own control block, so its own dt and its own CFL
 // reduction slot.  Compiled without FMA contraction: a problem advanced in a
@@ -17,14 +17,14 @@ namespace fv {
 
 namespace {
 
-// Work-item shapes (cells along a x rows along b) the autotuner chooses from;
-// the rows are a whole number of marching blocks.
+// Work-item shapes (cells along a x rows along b) the autotuner starts from;
+// the rows of an item are a run-time value (BatchInst::tz), so the shapes
+// that share a strip width share a kernel (kKernelOf64: the shape whose
+// instantiation serves it).
 constexpr TileShape kShapes64[] = {{32, 64}, {32, 32}, {32, 16}, {64, 32}};
+constexpr int kKernelOf64[] = {0, 0, 0, 3};
 constexpr int kNumShapes64 = sizeof(kShapes64) / sizeof(kShapes64[0]);
 constexpr int block_rows(int tx) { return 2 * kTileThreads / tx; }  // 512-cell blocks
-static_assert(kShapes64[0].ty % block_rows(kShapes64[0].tx) == 0 && kShapes64[1].ty % block_rows(kShapes64[1].tx) == 0 &&
-                  kShapes64[2].ty % block_rows(kShapes64[2].tx) == 0 && kShapes64[3].ty % block_rows(kShapes64[3].tx) == 0,
-              "item rows must be whole marching blocks");
 
 static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
 
@@ -41,7 +41,7 @@ __device__ __forceinline__ void fetch_inst(const BatchInst* __restrict__ insts, 
   for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
 }
 
-template <int PLANE, bool WACT, class TL, int ITEM_ROWS>
+template <int PLANE, bool WACT, class TL>
 __global__ void __launch_bounds__(kTileThreads, WACT ? FV_FP64_MIN_CTAS_W : FV_FP64_MIN_CTAS)
 batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ double smem_raw[];
@@ -68,8 +68,8 @@ batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
       uin = flip ? I.B : I.A; u0 = uin; uout = flip ? I.A : I.B;
     }
     StepCtrl* ctrl = I.ctrl;
-    const int x0 = bx * TL::TX, ya = by * ITEM_ROWS;
-    const int yb = ya + ITEM_ROWS < I.G.nb ? ya + ITEM_ROWS : I.G.nb;
+    const int x0 = bx * TL::TX, ya = by * I.tz;  // tz: rows per work item
+    const int yb = ya + I.tz < I.G.nb ? ya + I.tz : I.G.nb;
     if (!ctrl->active) {
       if (kind == STAGE_EULER) pass_on64<WACT, TL::TX>(I.G, uin, uout, x0, ya, yb, threadIdx.x);
       continue;
@@ -90,7 +90,7 @@ using BlockOf = Tile<kShapes64[S].tx, block_rows(kShapes64[S].tx)>;
 
 template <int PLANE, bool WACT, int S>
 auto kernel_for() {
-  return batch_stage64<PLANE, WACT, BlockOf<S>, kShapes64[S].ty>;
+  return batch_stage64<PLANE, WACT, BlockOf<S>>;
 }
 
 // wact groups (viscosity on, or a non-zero third velocity) get the largest
@@ -104,12 +104,7 @@ typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
 
 template <int PLANE, bool WACT>
 BatchKernel pick(int shape) {
-  switch (shape) {
-    case 0: return kernel_for<PLANE, WACT, 0>();
-    case 1: return kernel_for<PLANE, WACT, 1>();
-    case 2: return kernel_for<PLANE, WACT, 2>();
-    default: return kernel_for<PLANE, WACT, 3>();
-  }
+  return kKernelOf64[shape] == 0 ? kernel_for<PLANE, WACT, 0>() : kernel_for<PLANE, WACT, 3>();
 }
 
 BatchKernel pick_any(int plane, bool wact, int shape) {

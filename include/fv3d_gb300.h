@@ -242,9 +242,10 @@ int fvgpu_batch_set_stream(fv_batch* b, void* cuda_stream);
 int fvgpu_batch_synchronize(fv_batch* b);
 int fvgpu_batch_launch_count(const fv_batch* b, long* count);
 /* Problems sharing plane and layout form a group advanced by one persistent
- * launch per stage; reports the groups and the tile shape (cells along x by
- * cells along the second axis) the autotuner chose for each (tuning first if
- * needed; every problem must have a state). */
+ * launch per stage; reports the groups and the work-item shape the autotuner
+ * chose for each: cells along x by rows along the second axis (a strip
+ * segment; 3-D groups: 16 x 16 columns), tuning first if needed; every
+ * problem must have a state.  FV3D_TILE=WxH forces a shape. */
 int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_groups);
 
 #ifdef __cplusplus

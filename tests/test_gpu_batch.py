@@ -106,10 +106,10 @@ def _run_forced_tile(tile, nsteps):
     return code
 
 
-@pytest.mark.parametrize("tile", ["32x16", "32x32", "64x32", "32x64"])
+@pytest.mark.parametrize("tile", ["32x16", "32x32", "64x32", "32x64", "32x21", "64x13"])
 def test_fp64_batch_independent_of_tile_shape(tile, tmp_path):
-    """Forcing another work-item shape (FV3D_TILE: strip width x rows) gives
-    the same bits."""
+    """Forcing another work-item shape (FV3D_TILE: strip width x rows, rows
+    not a whole number of marching blocks included) gives the same bits."""
     nsteps = 5
     probs = mixed_set()
     ref, _ = run_singles(probs, nsteps)
