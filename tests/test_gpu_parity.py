@@ -180,6 +180,18 @@ def test_nonfinite_state_reported():
     assert e.value.status == 4
 
 
+@pytest.mark.parametrize("bcs", [("reflecting", "periodic", "periodic"), ("absorbing", "periodic", "periodic")])
+def test_one_dimensional_grid(bcs):
+    """A 1-D run (Ny = Nz = 1: two one-cell axes, each entering dt through
+    its cell size) steps like the oracle."""
+    pr = problems.random_problem(
+        "line", problems._mesh(300, 1, 1),
+        {"tend": 1.0, "boundaries_x": bcs[0], "boundaries_y": bcs[1], "boundaries_z": bcs[2]},
+        {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2", "CFL": 0.8},
+        {"gamma0": 1.4}, seed=808)
+    per_step_parity(pr.params, pr.prim, nsteps=3)
+
+
 def test_unsupported_and_state_errors():
     # viscosity reads the stale outer ghost layer of a reflecting one-cell axis
     p = fv.parse_ini("[mesh]\nNx=8\nNy=8\nNz=1\n[run]\nboundaries_z=reflecting\n"
