@@ -1,24 +1,29 @@
-// fv_tile64.cuh -- one FP64 stage of one tile: the body shared by the
-// single-problem kernel (fv_stage2d.cu) and the persistent batch kernel
-// (fv_batch64.cu).
+// fv_tile64.cuh -- the FP64 stage body shared by the single-problem kernel
+// (fv_stage2d.cu) and the persistent batch kernel (fv_batch64.cu).
 //
-// stage_tile64 performs a whole reference euler_step (Update.h:164-178) on a
-// TX x TY tile of cells with 256 threads:
-//   1. load the tile plus a 2-cell halo of the stage's input conserved state,
-//      synthesising ghost cells by index remapping (the X-then-Y ghost fill of
-//      BoundaryConditions.h:146-192, corners included), and convert to
-//      primitives (consToPrim, States.h:34-45) in shared memory;
-//   2. for every face of the tile: minmod slopes and PLM face states
+// stage_segment64 performs a whole reference euler_step (Update.h:164-178)
+// on a strip segment: TX columns and a run of rows, marched in blocks of
+// TX x TY cells with 256 threads.  Per block:
+//   1. the new halo rows of the block (all TY + 4 for the first block of a
+//      segment, TY afterwards: the 4 rows shared with the previous block stay
+//      in a ring of TY + 4 shared rows) -- loaded with the ghost cells
+//      synthesised by index remapping (the X-then-Y ghost fill of
+//      BoundaryConditions.h:146-192, corners included) or, for interior
+//      blocks of the single-problem kernel, staged by TMA tensor copies --
+//      and converted to primitives (consToPrim, States.h:34-45);
+//   2. every face of the block: minmod slopes and PLM face states
 //      (Update.h:14-33,55-88) and one Riemann solve (RiemannSolvers.h) -- the
 //      reference solves every face twice, from each side, with equal inputs;
+//      the b faces on the boundary with the previous block are reused; with
+//      viscosity, the face-only viscous branches once per face;
 //   3. the conservative update in the reference's X, Y, Z order with
 //      (F*dt)/d increments, gravity on the z sweep and the density floor
 //      (Update.h:145-160), then thermal conduction (ThermalConduction.h:38-96)
 //      and viscosity (Viscosity.h:127-253) from the same primitive tile;
 //   4. for RK2 stage 2 the SSP average 0.5*(U^n + U**) (Update.h:198-204);
 //   5. for the last stage of a step, consToPrim of the result and the
-//      hyperbolic CFL term of ComputeDt.h:28-54, reduced to one atomic max
-//      per tile (the TC/viscous terms are constants folded in by the control
+//      hyperbolic CFL term of ComputeDt.h:28-54, folded into one maximum per
+//      CTA (the TC/viscous terms are constants folded in by the control
 //      kernel).
 //
 // Rounding: every file including this one is compiled without FMA
@@ -699,42 +704,6 @@ __device__ __forceinline__ void pass_on64(const Grid& G, const Fields& uin, cons
         if (WACT || v != 3) uout.f[v][o] = uin.f[v][o];
     }
   }
-}
-
-// One stage of one tile (bx, by) of problem G; see the file comment.
-// rs: 0 HLL / 1 HLLC; kind: StageKind.  Every thread of the CTA must call it;
-// smem holds TileSmem<double, NV, TL>::bytes(G.tc) bytes.
-//
-// hout (optional, last stage of a step only): primitive output arrays in
-// storage order with rows of G.na values and no padding (a caller's host
-// arrays the GPU can address); the stage writes consToPrim of its result
-// there, the values the CFL term computes anyway.
-// P2: every cell size is a power of two (G.pow2_all); callers branch on it
-// once, uniformly, and instantiate both forms.
-template <int PLANE, bool WACT, class TL, bool P2>
-__device__ __forceinline__ void stage_tile64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
-                                             StepCtrl* ctrl, int rs, int kind, int bx, int by, double* smem,
-                                             unsigned long long* s_red, const Fields* hout = nullptr) {
-  constexpr int NV = WACT ? 5 : 4;
-  constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
-  using SM = TileSmem<double, NV, TL>;
-  const PrimView<SM, RowsDirect> V{SM{smem}, RowsDirect{}};
-  const int tid = threadIdx.x;
-  const int x0 = bx * TX, y0 = by * TY;
-  if (!ctrl->active) {
-    if (kind == STAGE_EULER) pass_on64<WACT, TX>(G, uin, uout, x0, y0, y0 + TY, tid);
-    return;
-  }
-  const double dt = ctrl->dt_cur;
-  const int parity = ctrl->parity;
-  const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
-  load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, 0, HY, tid);
-  __syncthreads();
-  faces64<PLANE, WACT, TL, false>(G, K, V, rs, TY, 0, tid);
-  __syncthreads();
-  unsigned long long red = 0ull;
-  update64<PLANE, WACT, TL, P2, false>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, TY, tid, hout, red);
-  if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
 }
 
 // One strip segment: cell rows [ya, yb) of the TX-wide strip whose first
