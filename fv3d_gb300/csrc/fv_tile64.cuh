@@ -711,10 +711,10 @@ __device__ __forceinline__ void pass_on64(const Grid& G, const Fields& uin, cons
 // primitive rows, so each block converts only its new rows and reuses the
 // b-face fluxes on the boundary with the previous block; with viscosity the
 // face-only viscous branches are computed once per face (viscous_face).  The
-// arithmetic of every face and cell is that of the tile body, so results are
-// bit-identical to it.  Every thread of the CTA calls it (ctrl active); the
-// CFL maximum is folded into red; smem holds bytes_vface() with viscosity,
-// else bytes(G.tc).
+// arithmetic of every face and cell is that of the reference's euler_step,
+// however the rows are split into segments.  Every thread of the CTA calls
+// it (ctrl active); the CFL maximum is folded into red; smem holds
+// bytes_vface() with viscosity, else bytes(G.tc).
 //
 // tin / mbar (optional, single-problem kernel): TMA descriptors of uin and
 // the CTA's mbarrier; full blocks whose halo lies inside the grid are then
