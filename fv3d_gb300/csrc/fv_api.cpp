@@ -377,6 +377,12 @@ int SetCtrl(fv_sim* s, const StepCtrl& c) {
   return FV_OK;
 }
 
+// The status of a non-zero sticky error flag of the control block.
+int CtrlError(fv_sim* s, const char* what) {
+  if (s->h_ctrl->err & 2) return Fail(s, FV_ERR_TIMEOUT, "%s: a staged tile load did not complete in time", what);
+  return Fail(s, FV_ERR_NONFINITE, "%s: non-finite state or dt", what);
+}
+
 int ReadCtrl(fv_sim* s) {
   CUDA_TRY(s, cudaMemcpyAsync(s->h_ctrl, s->d_ctrl, sizeof(StepCtrl), cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(s, cudaStreamSynchronize(s->stream));
@@ -737,7 +743,7 @@ int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double
   rc = ReadCtrl(s);
   if (rc) return rc;
   if (dt_used) *dt_used = s->h_ctrl->dt_cur;
-  if (s->h_ctrl->err) return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt");
+  if (s->h_ctrl->err) return CtrlError(s, "step_host");
   return FV_OK;
 }
 
@@ -765,8 +771,8 @@ int fvgpu_compute_dt(fv_sim* s, double* dt, double inv[3]) {
     inv[2] = s->inv_visc;
   }
   if (dt) *dt = d;
-  if (s->h_ctrl->err || !std::isfinite(d))
-    return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
+  if (s->h_ctrl->err) return CtrlError(s, "compute_dt");
+  if (!std::isfinite(d)) return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
   return FV_OK;
 }
 
@@ -871,7 +877,7 @@ int fvgpu_advance(fv_sim* s, double tend, long max_steps, double* t, long* nstep
   s->slot_valid = true;
   *t = s->h_ctrl->t;
   if (nsteps) *nsteps = (long)(s->h_ctrl->step - step0);
-  if (s->h_ctrl->err) return Fail(s, FV_ERR_NONFINITE, "non-finite state or dt during advance");
+  if (s->h_ctrl->err) return CtrlError(s, "advance");
   return FV_OK;
 }
 

@@ -31,7 +31,7 @@ struct StepCtrl {
   int active;          // 1 if the step in flight advances the state
   int parity;          // slot read by this step's control = step & 1
   int mode;            // 0: dt = dt_given; 1: CFL dt, loop bound t + eps < tend
-  int err;             // sticky: bit0 non-finite/negative state seen
+  int err;             // sticky: bit0 non-finite/negative state seen, bit1 a bounded wait (TMA staging) gave up
 };
 
 // Geometry and physics of one problem as the kernels need it.  A 2-D run
