@@ -1,4 +1,5 @@
-// fv_probe.cu -- measures the FP64 FMA throughput of the current GPU.
+// fv_probe.cu -- measures the FP64 FMA throughput of the current GPU, and
+// exercises the bounded mbarrier wait of the TMA staging path.
 //
 // The bit-exact FP64 stage kernels are bound by the FP64 pipe, not by HBM,
 // so their roofline is the FP64 instruction rate.  fvgpu_probe_fp64_rate
@@ -8,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "fv3d_gb300.h"
+#include "fv_tma.cuh"
 
 namespace {
 
@@ -28,7 +30,35 @@ __global__ void __launch_bounds__(kThreads) dfma_loop(double a, double b, int it
   if (s == -1.0) sink[0] = s;  // keeps the chains live; never true for these inputs
 }
 
+// One CTA waits on a fresh mbarrier with the stage kernels' bounded wait;
+// thread 0 arrives on it first only when `arrive` is set.  out[0] = 1 when
+// the wait completed, 0 when it gave up.
+__global__ void __launch_bounds__(kThreads) wait_probe(int arrive, int max_polls, int* out) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    fv::mbar_init(&bar, 1);
+    fv::fence_mbar_init();
+  }
+  __syncthreads();
+  if (arrive && threadIdx.x == 0) fv::mbar_arrive_expect_tx(&bar, 0);
+  const bool ok = fv::mbar_wait(&bar, 0, max_polls);
+  __syncthreads();
+  if (threadIdx.x == 0) out[0] = ok ? 1 : 0;
+}
+
 }  // namespace
+
+extern "C" int fvgpu_probe_wait(int arrive, int max_polls) {
+  if (max_polls < 1) return FV_ERR_PARAM;
+  int* d = nullptr;
+  int h = -1;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return FV_ERR_NOMEM;
+  wait_probe<<<1, kThreads>>>(arrive ? 1 : 0, max_polls, d);
+  const bool ok = cudaGetLastError() == cudaSuccess && cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(d);
+  if (!ok) return FV_ERR_CUDA;
+  return h == 1 ? FV_OK : FV_ERR_TIMEOUT;
+}
 
 extern "C" int fvgpu_probe_fp64_rate(double* lane_ops_per_s) {
   if (!lane_ops_per_s) return FV_ERR_PARAM;

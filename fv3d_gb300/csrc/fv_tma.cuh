@@ -65,10 +65,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* m, unsigned pa
   return ok != 0;
 }
 
-// Waits for phase `parity` of m to complete, at most ~2^22 polls (each poll
-// may suspend the thread for a while); false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity) {
-  for (int i = 0; i < (1 << 22); ++i)
+// Waits for phase `parity` of m to complete, at most max_polls polls (each
+// poll may suspend the thread for a while); false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity, int max_polls = 1 << 22) {
+  for (int i = 0; i < max_polls; ++i)
     if (mbar_try_wait(m, parity)) return true;
   return false;
 }

@@ -219,6 +219,12 @@ int fvgpu_step_noalloc(const fv_params* params, double* const fields[5], long pi
  * bench reports their FP64 roofline against it.  No reference counterpart. */
 int fvgpu_probe_fp64_rate(double* lane_ops_per_s);
 
+/* Exercises the bounded device-side wait of the TMA staging path on its own:
+ * one CTA waits on an mbarrier (at most max_polls polls); with arrive != 0 the
+ * barrier completes first.  FV_OK when the wait completed, FV_ERR_TIMEOUT when
+ * it gave up (the kernel then returns normally and the context stays usable). */
+int fvgpu_probe_wait(int arrive, int max_polls);
+
 /* ---- many independent problems (no reference counterpart) --------------- */
 typedef struct fv_batch fv_batch;
 

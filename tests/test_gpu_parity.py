@@ -216,3 +216,14 @@ def test_launch_count_and_profile():
     kt = sim.kernel_times()
     assert kt["stage"][0] >= 8 and kt["stage"][1] > 0
     assert sim.launch_count() - c0 >= 12
+
+
+def test_bounded_wait_gives_up_and_reports():
+    """The TMA staging wait is bounded: on a barrier nothing completes it
+    returns FV_ERR_TIMEOUT after its polls (no hang, the context stays
+    usable); on a completed barrier it passes."""
+    assert fv.probe_wait(True, 1000) == 0
+    assert fv.probe_wait(False, 1000) == 7  # FV_ERR_TIMEOUT
+    assert fv.probe_wait(True, 1) == 0
+    pr = problems.sedov(64)  # the context still runs the solver
+    per_step_parity(pr.params, pr.prim, nsteps=1)
