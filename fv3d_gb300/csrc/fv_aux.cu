@@ -71,12 +71,14 @@ __device__ __forceinline__ void step_control(StepCtrl& c, int mode_override, dou
 }
 
 __global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) step_control(ctrl[i], mode_override, dt_given);
 }
 
 __global__ void batch_control_kernel(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override,
                                      double dt_given) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) step_control(ctrl[i], mode_override, dt_given);
   if (i < nq) queue[i] = 0u;
@@ -210,14 +212,18 @@ cudaError_t launch_reduce2d(const Grid& G, bool wact, Fields u, StepCtrl* ctrl, 
 }
 
 cudaError_t launch_control(StepCtrl* ctrl, int n, int mode_override, double dt_given, cudaStream_t st) {
-  control_kernel<<<(n + 127) / 128, 128, 0, st>>>(ctrl, n, mode_override, dt_given);
+  const cudaError_t e = launch_pdl(control_kernel, dim3((n + 127) / 128), dim3(128), 0, st, ctrl, n, mode_override,
+                                   dt_given);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override, double dt_given,
                                  cudaStream_t st) {
   const int m = n > nq ? n : nq;
-  batch_control_kernel<<<(m + 127) / 128, 128, 0, st>>>(ctrl, n, queue, nq, mode_override, dt_given);
+  const cudaError_t e = launch_pdl(batch_control_kernel, dim3((m + 127) / 128), dim3(128), 0, st, ctrl, n, queue, nq,
+                                   mode_override, dt_given);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -43,6 +43,7 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
   __shared__ unsigned long long s_red[kTileThreads / 32];
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
+  pdl_enter();
   for (;;) {
     __syncthreads();  // the previous tile is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
@@ -214,9 +215,9 @@ cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchIns
   if (shape < 0 || shape >= kNumShapes32) return cudaErrorInvalidValue;
   cudaError_t e = prepare(plane, wact, shape);
   if (e != cudaSuccess) return e;
-  pick_any(plane, wact, shape)<<<grid, kTileThreads, smem_any(shape, wact, tc), st>>>(insts, ninst, ntiles, queue,
-                                                                                       kind, flip);
-  return cudaGetLastError();
+  e = launch_pdl(pick_any(plane, wact, shape), dim3(grid), dim3(kTileThreads), smem_any(shape, wact, tc), st, insts,
+                 ninst, ntiles, queue, kind, flip);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_reduce2d_mixed(const Grid& G, bool wact, Fields pairs, StepCtrl* ctrl, int slot,

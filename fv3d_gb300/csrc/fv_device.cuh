@@ -34,6 +34,16 @@ struct StepCtrl {
   int err;             // sticky: bit0 non-finite/negative state seen, bit1 a bounded wait (TMA staging) gave up
 };
 
+// Programmatic dependent launch (PTX griddepcontrol) for the kernels of the
+// step loop: each lets the next kernel of the stream be scheduled once all
+// its CTAs have started, and waits for the previous kernel to complete (its
+// memory visible) before touching memory.  Outside such a launch both are
+// no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Geometry and physics of one problem as the kernels need it.  A 2-D run
 // (ndim 2) has axes a, b and a one-cell axis c; a 3-D run (ndim 3) has
 // a = x, b = y, c = z, stored like the x-y plane (rho, m_x, m_y, m_z, E).

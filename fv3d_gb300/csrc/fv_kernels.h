@@ -3,10 +3,31 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "fv_device.cuh"
 #include "fv_tma.cuh"
 
 namespace fv {
+
+// Launches a step-loop kernel (one that starts with pdl_enter) with
+// programmatic stream serialisation, so that its launch overlaps the tail of
+// the previous kernel in the stream.
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // Pointers to the five field arrays of one state, in storage order
 // (rho, m_a, m_b, m_c, E): m_a = x-momentum, m_b = momentum along the second

@@ -29,6 +29,7 @@ stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
   __shared__ __align__(8) unsigned long long s_mbar;
   const unsigned sa = smem_u32(smem_bytes);
   double* smem = reinterpret_cast<double*>(smem_bytes + (((sa + kSmemAlign - 1) & ~(unsigned)(kSmemAlign - 1)) - sa));
+  pdl_enter();
   if (use_tma) {
     if (threadIdx.x == 0) {
       mbar_init(&s_mbar, 1);
@@ -84,9 +85,9 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   if (ctas < 1) ctas = 1;
   const Fields none{};
   static const TmaState no_tma{};
-  kern<<<(unsigned)ctas, kTileThreads, smem, st>>>(G, uin, u0, uout, ctrl, hout ? *hout : none, units,
-                                                   tin ? *tin : no_tma, tin ? 1 : 0);
-  return cudaGetLastError();
+  const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kTileThreads), smem, st, G, uin, u0, uout, ctrl,
+                                   hout ? *hout : none, units, tin ? *tin : no_tma, tin ? 1 : 0);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int PLANE, int RS, bool WACT>

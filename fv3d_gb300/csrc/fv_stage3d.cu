@@ -471,6 +471,7 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
              long long units, const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
+  pdl_enter();
   const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   const int active = ctrl->active, parity = ctrl->parity;
   const unsigned long long red =
@@ -513,8 +514,9 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   if (ctas > slots) ctas = slots;
   if (ctas < 1) ctas = 1;
   const Fields none{};
-  kern<<<(unsigned)ctas, kThreads, Smem3::bytes(tc), st>>>(G, uin, u0, uout, ctrl, units, hout ? *hout : none);
-  return cudaGetLastError();
+  const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kThreads), Smem3::bytes(tc), st, G, uin, u0, uout,
+                                   ctrl, units, hout ? *hout : none);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int RS, bool CORR>
@@ -549,6 +551,7 @@ batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsi
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
   const Fields none{};
+  pdl_enter();
   for (;;) {
     __syncthreads();  // the previous item is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
@@ -628,8 +631,9 @@ int batch_stage3d_occupancy64(bool tc) {
 cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
                                    int rs, int grid, bool tc, cudaStream_t st) {
   if (!batch3d_prepare()) return cudaErrorInvalidConfiguration;
-  batch3d_kernel(kind, rs)<<<grid, kThreads, Smem3::bytes(tc), st>>>(insts, ninst, ntiles, queue, flip);
-  return cudaGetLastError();
+  const cudaError_t e =
+      launch_pdl(batch3d_kernel(kind, rs), dim3(grid), dim3(kThreads), Smem3::bytes(tc), st, insts, ninst, ntiles, queue, flip);
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,

@@ -412,6 +412,7 @@ batch_stage3d32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsi
   __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
+  pdl_enter();
   for (;;) {
     __syncthreads();  // the previous item is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
@@ -479,7 +480,9 @@ int batch_stage3d_occupancy32(bool tc) {
 cudaError_t launch_batch_stage3d32(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
                                    int rs, int grid, bool tc, cudaStream_t st) {
   if (!prepare32()) return cudaErrorInvalidConfiguration;
-  kernel32(rs)<<<grid, kThreads, Smem3f::bytes(tc), st>>>(insts, ninst, ntiles, queue, kind, flip);
+  const cudaError_t e =
+      launch_pdl(kernel32(rs), dim3(grid), dim3(kThreads), Smem3f::bytes(tc), st, insts, ninst, ntiles, queue, kind, flip);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
