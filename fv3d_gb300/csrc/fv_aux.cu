@@ -71,17 +71,19 @@ __device__ __forceinline__ void step_control(StepCtrl& c, int mode_override, dou
 }
 
 __global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {
-  pdl_enter();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) step_control(ctrl[i], mode_override, dt_given);
+  pdl_trigger();
 }
 
 __global__ void batch_control_kernel(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override,
                                      double dt_given) {
-  pdl_enter();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) step_control(ctrl[i], mode_override, dt_given);
   if (i < nq) queue[i] = 0u;
+  pdl_trigger();
 }
 
 // primToCons in place (States.h:20-31).  Storage order in and out.

@@ -43,13 +43,16 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
   __shared__ unsigned long long s_red[kTileThreads / 32];
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
-  pdl_enter();
+  pdl_wait();
   for (;;) {
     __syncthreads();  // the previous tile is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
     __syncthreads();
     const int t = s_tile;
-    if (t >= ntiles) break;
+    if (t >= ntiles) {
+      pdl_trigger();  // no work left for this CTA
+      break;
+    }
     fetch_inst32(insts, ninst, t, &s_inst);
     __syncthreads();
     const BatchInst& I = s_inst;

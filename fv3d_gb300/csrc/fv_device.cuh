@@ -35,14 +35,15 @@ struct StepCtrl {
 };
 
 // Programmatic dependent launch (PTX griddepcontrol) for the kernels of the
-// step loop: each lets the next kernel of the stream be scheduled once all
-// its CTAs have started, and waits for the previous kernel to complete (its
-// memory visible) before touching memory.  Outside such a launch both are
-// no-ops.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
+// step loop: each waits for the previous kernel of the stream to complete
+// (its memory visible) before touching memory, and lets the next kernel be
+// launched once all its CTAs are done with their work, so that launch
+// overlaps this kernel's exit.  The trigger comes at the end, not the start:
+// an early trigger let the next grid's CTAs settle on the SMs that happened
+// to be free, two to an SM, and halved the speed of grids smaller than the
+// GPU.  Outside such a launch both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // Geometry and physics of one problem as the kernels need it.  A 2-D run
 // (ndim 2) has axes a, b and a one-cell axis c; a 3-D run (ndim 3) has

@@ -10,7 +10,11 @@
 
 namespace fv {
 
-// Launches a step-loop kernel (one that starts with pdl_enter) with
+#ifndef FV_PDL
+#define FV_PDL 1  // 0: plain stream order for the step-loop kernels
+#endif
+
+// Launches a step-loop kernel (one that waits with pdl_wait) with
 // programmatic stream serialisation, so that its launch overlaps the tail of
 // the previous kernel in the stream.
 template <class... KArgs, class... Args>
@@ -23,7 +27,7 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[0].val.programmaticStreamSerializationAllowed = FV_PDL;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);

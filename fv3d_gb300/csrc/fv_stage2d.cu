@@ -29,7 +29,7 @@ stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
   __shared__ __align__(8) unsigned long long s_mbar;
   const unsigned sa = smem_u32(smem_bytes);
   double* smem = reinterpret_cast<double*>(smem_bytes + (((sa + kSmemAlign - 1) & ~(unsigned)(kSmemAlign - 1)) - sa));
-  pdl_enter();
+  pdl_wait();
   if (use_tma) {
     if (threadIdx.x == 0) {
       mbar_init(&s_mbar, 1);
@@ -46,6 +46,7 @@ stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
   else
     stage_strip64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem, s_red, ho, tp,
                                                   &s_mbar);
+  pdl_trigger();
 }
 
 int sm_count() {

@@ -471,13 +471,14 @@ stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout,
              long long units, const Fields hout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
-  pdl_enter();
+  pdl_wait();
   const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   const int active = ctrl->active, parity = ctrl->parity;
   const unsigned long long red =
       G.pow2_all ? march3d<true, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw)
                  : march3d<false, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw);
   if (active && KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+  pdl_trigger();
 }
 
 int sm_count3d() {
@@ -551,13 +552,16 @@ batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsi
   __shared__ BatchInst s_inst;
   __shared__ int s_tile;
   const Fields none{};
-  pdl_enter();
+  pdl_wait();
   for (;;) {
     __syncthreads();  // the previous item is finished with s_tile, s_inst and smem
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(queue, 1u);
     __syncthreads();
     const int t = s_tile;
-    if (t >= ntiles) break;
+    if (t >= ntiles) {
+      pdl_trigger();  // no work left for this CTA
+      break;
+    }
     {
       int lo = 0, hi = ninst - 1;
       while (lo < hi) {
