@@ -217,8 +217,9 @@ def run_gpu(args):
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     replicas.barrier()
     torch.cuda.synchronize()
-    clk = Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else tempfile.mkdtemp(),
-                              "bench_clocks.csv"))
+    # the raw clock samples go to $FV3D_BENCH_OUT when set (the JSON line
+    # carries their summary either way)
+    clk = Clocks(os.path.join(os.environ.get("FV3D_BENCH_OUT") or tempfile.mkdtemp(), "bench_clocks.csv"))
     with clk:
         for k in range(args.steps):
             flush_l2()
@@ -447,7 +448,8 @@ def random_3d(n):
 
 
 def run_variants(torch, args, flush):
-    """The other BASELINE configurations, timed on the same GPU."""
+    """The other benchmark configurations (Sedov, diffusion, shear layer,
+    the two batches, two 3-D runs), timed on the same GPU."""
     from fv3d_gb300 import problems
     hbm_peak, _ = peaks()
     out = {}

@@ -1,8 +1,8 @@
 /*
  * fv3d_oracle.c -- CPU restatement of the reference fv3d FP64 hydro step.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU path (tests/, smoke())
- * and the timed CPU baseline of bench.py ("port").  The product never links
+ * TEST INFRASTRUCTURE ONLY: the results the GPU path is compared with
+ * (tests/, smoke()) and the timed CPU baseline of bench.py ("port").  The product never links
  * or calls this file.
  *
  * It restates, in plain C with OpenMP, the reference's own algorithm with

@@ -2,8 +2,8 @@
  * fv3d_oracle.h -- CPU restatement of the reference fv3d hydro step.
  *
  * TEST INFRASTRUCTURE ONLY.  Used by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker; the product never links,
- * imports or calls it.
+ * CPU-baseline leg of bench.py as the reference results the GPU path is
+ * compared with; the product never links, imports or calls it.
  *
  * The API mirrors the product's fvgpu_* calls (same field layout: interior
  * cells, C order [Nz][Ny][Nx]) so a test runs both on identical inputs.

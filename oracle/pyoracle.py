@@ -1,7 +1,7 @@
 """Python access to the oracle libraries -- TEST INFRASTRUCTURE ONLY.
 
 Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-leg, always as the checker.  Two back ends share one interface:
+leg, always for results to compare with.  Two back ends share one interface:
 
 * :class:`Oracle` -- the C restatement (oracle/fv3d_oracle.c), fed an
   ``FvParams``; available everywhere.
