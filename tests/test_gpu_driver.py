@@ -73,6 +73,16 @@ def _check_xdmf(tmp_path, shape, nsnaps):
             raw = np.fromfile(str(tmp_path / d.text), dtype=np.float64).reshape(5, nz * ny * nx)
             k = int(d.get("Seek")) // (8 * nz * ny * nx)
             np.testing.assert_array_equal(a, raw[k])
+    # the same run through the h5py-like reader the reference's tools can use
+    from fv3d_gb300 import snapshots
+    f = snapshots.File(str(tmp_path / "snap"))
+    assert len(f.keys()) == 3 + nsnaps and f.attrs["Nx"] == nx
+    for n, g in enumerate(grids):
+        assert f["ite_%d" % n].attrs["time"] == times[n]
+        name = g.find(".//Attribute/DataItem").text
+        raw = np.fromfile(str(tmp_path / name), dtype=np.float64).reshape(5, nz, ny, nx)
+        for v, field in enumerate(("rho", "u", "v", "w", "prs")):
+            np.testing.assert_array_equal(f["ite_%d/%s" % (n, field)], raw[v])
 
 
 @pytest.mark.parametrize("mode", ["host", "device"])
