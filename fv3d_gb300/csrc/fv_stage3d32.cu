@@ -31,18 +31,31 @@ constexpr int kNFB = kTX * (kTY + 1);
 static_assert(kThreads == kTileThreads, "one thread per column");
 
 // Shared memory (floats): Q[ring][v][hy][hx], FA, FB of the current layer,
-// TT[ring][hy][hx] (conduction only).
+// TT[ring][hy][hx] (conduction only).  Every row is kRowPitch = 20 floats
+// apart (FA and FB rows padded to it): a warp owns the columns of rows r and
+// r + 4 (column_of), 80 floats = 16 banks apart, so its per-column accesses
+// fall on disjoint banks.
+constexpr int kRowPitch = kHX;
+static_assert(kRowPitch >= kTX + 1 && (4 * kRowPitch) % 32 == 16, "rows r and r+4 on disjoint banks");
 struct Smem3f {
   float* base;
   static constexpr int kFA = kRing * 5 * kLayer;
-  static constexpr int kFB = kFA + 5 * kTY * (kTX + 1);
-  static constexpr int kT = kFB + 5 * (kTY + 1) * kTX;
+  static constexpr int kFB = kFA + 5 * kTY * kRowPitch;
+  static constexpr int kT = kFB + 5 * (kTY + 1) * kRowPitch;
   static constexpr size_t bytes(bool tc) { return sizeof(float) * (size_t)(kT + (tc ? kRing * kLayer : 0)); }
   __device__ float& q(int s, int v, int hy, int hx) const { return base[((s * 5 + v) * kHY + hy) * kHX + hx]; }
-  __device__ float& fa(int v, int fy, int fx) const { return base[kFA + (v * kTY + fy) * (kTX + 1) + fx]; }
-  __device__ float& fb(int v, int fy, int fx) const { return base[kFB + (v * (kTY + 1) + fy) * kTX + fx]; }
+  __device__ float& fa(int v, int fy, int fx) const { return base[kFA + (v * kTY + fy) * kRowPitch + fx]; }
+  __device__ float& fb(int v, int fy, int fx) const { return base[kFB + (v * (kTY + 1) + fy) * kRowPitch + fx]; }
   __device__ float& temp(int s, int hy, int hx) const { return base[kT + (s * kHY + hy) * kHX + hx]; }
 };
+
+// The column (cx, cy) of the 16 x 16 block a thread owns: the two half-warps
+// of warp w take rows r and r + 4 (r = (w & 3) + 8 * (w >> 2)).
+__device__ __forceinline__ void column_of(int tid, int& cx, int& cy) {
+  const int lane = tid & 31, w = tid >> 5;
+  cx = lane & 15;
+  cy = (w & 3) + ((w >> 2) << 3) + ((lane >> 4) << 2);
+}
 
 __device__ __forceinline__ int slot_of(int kg) { return (kg + 4) & 3; }
 
@@ -221,7 +234,8 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
   const int x0 = bx * kTX, y0 = by * kTY;
   const int k0 = bz * tz;
   const int k1 = min(k0 + tz, G.nc);
-  const int cx = tid % kTX, cy = tid / kTX;
+  int cx, cy;
+  column_of(tid, cx, cy);
   const int x = x0 + cx, y = y0 + cy;
   const bool own = x < G.na && y < G.nb;
   // 32-bit offsets (the host keeps every field below 2^32 elements for the
