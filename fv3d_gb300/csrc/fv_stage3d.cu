@@ -222,6 +222,90 @@ struct RingVel {
   }
 };
 
+// The viscous flux of one x face (DIR 0) or y face (DIR 1) of a layer for
+// Viscosity.h's IX / IY branch, whose terms depend on the face alone:
+// g = {mu*t1, mu*t2, mu*t3, mu*(t . qi)}.  The two cells of the face add it
+// as (-mu)*t and (+mu)*t, i.e. -(mu*t) and mu*t exactly, so one evaluation
+// serves both.  P is centred on the cell above the face (the s = 1 side of
+// the reference's loop).
+template <int DIR, class PA>
+__device__ __forceinline__ void viscous_face3d(const PA& P, double odx, double ody, double odz, double mu,
+                                               double g[4]) {
+  const double four_thirds = 4.0 / 3.0;
+  const double two_thirds = 2.0 / 3.0;
+  const double c4x = half64(half64(odx)), c4y = half64(half64(ody)), c4z = half64(half64(odz));
+  const int U = 1, V = 2, W = 3;
+  if (DIR == 0) {
+    const double qiu = half64(P(1, 1, 1, U) + P(1, 1, 0, U));
+    const double qiv = half64(P(1, 1, 1, V) + P(1, 1, 0, V));
+    const double qiw = half64(P(1, 1, 1, W) + P(1, 1, 0, W));
+    const double dudx = odx * (P(1, 1, 1, U) - P(1, 1, 0, U));
+    const double dvdx = odx * (P(1, 1, 1, V) - P(1, 1, 0, V));
+    const double dwdx = odx * (P(1, 1, 1, W) - P(1, 1, 0, W));
+    const double dudy = c4y * (P(1, 2, 1, U) - P(1, 0, 1, U) + P(1, 2, 0, U) - P(1, 0, 0, U));
+    const double dvdy = c4y * (P(1, 2, 1, V) - P(1, 0, 1, V) + P(1, 2, 0, V) - P(1, 0, 0, V));
+    const double dudz = c4z * (P(2, 1, 1, U) - P(0, 1, 1, U) + P(2, 1, 0, U) - P(0, 1, 0, U));
+    const double dwdz = c4z * (P(2, 1, 1, W) - P(0, 1, 1, W) + P(2, 1, 0, W) - P(0, 1, 0, W));
+    const double tau_xx = four_thirds * dudx - two_thirds * (dvdy + dwdz);
+    const double tau_xy = dvdx + dudy;
+    const double tau_xz = dwdx + dudz;
+    g[0] = mu * tau_xx;
+    g[1] = mu * tau_xy;
+    g[2] = mu * tau_xz;
+    g[3] = mu * (tau_xx * qiu + tau_xy * qiv + tau_xz * qiw);
+  } else {
+    const double qiu = half64(P(1, 1, 1, U) + P(1, 0, 1, U));
+    const double qiv = half64(P(1, 1, 1, V) + P(1, 0, 1, V));
+    const double qiw = half64(P(1, 1, 1, W) + P(1, 0, 1, W));
+    const double dudy = ody * (P(1, 1, 1, U) - P(1, 0, 1, U));
+    const double dvdy = ody * (P(1, 1, 1, V) - P(1, 0, 1, V));
+    const double dwdy = ody * (P(1, 1, 1, W) - P(1, 0, 1, W));
+    const double dudx = c4x * (P(1, 1, 2, U) - P(1, 1, 0, U) + P(1, 0, 2, U) - P(1, 0, 0, U));
+    const double dvdx = c4x * (P(1, 1, 2, V) - P(1, 1, 0, V) + P(1, 0, 2, V) - P(1, 0, 0, V));
+    const double dwdz = c4z * (P(2, 1, 1, W) - P(0, 1, 1, W) + P(2, 0, 1, W) - P(0, 0, 1, W));
+    const double dvdz = c4z * (P(2, 1, 1, V) - P(0, 1, 1, V) + P(2, 0, 1, V) - P(0, 0, 1, V));
+    const double tau_yy = four_thirds * dvdy - two_thirds * (dudx + dwdz);
+    const double tau_xy = dvdx + dudy;
+    const double tau_yz = dvdz + dwdy;
+    g[0] = mu * tau_xy;
+    g[1] = mu * tau_yy;
+    g[2] = mu * tau_yz;
+    g[3] = mu * (tau_xy * qiu + tau_yy * qiv + tau_yz * qiw);
+  }
+}
+
+// The IZ branch of Viscosity.h for one cell, with the reference's index /
+// field mix-ups (some terms read the cell's own row, so this flux belongs to
+// the cell): accumulates into vz[1..4] like viscous3d<false>.
+template <class PA>
+__device__ __forceinline__ void viscous_iz3d(const PA& P, double odx, double odz, double mu, double vz[5]) {
+  const double four_thirds = 4.0 / 3.0;
+  const double two_thirds = 2.0 / 3.0;
+  const double c4x = half64(half64(odx)), c4z = half64(half64(odz));
+  const int U = 1, V = 2, W = 3;
+#pragma unroll
+  for (int s = 1; s < 3; ++s) {
+    const double sm = (s == 1 ? -1.0 : 1.0) * mu;
+    const double qiu = half64(P(s, 1, 1, U) + P(s - 1, 1, 1, U));
+    const double qiv = half64(P(s, 1, 1, V) + P(s - 1, 1, 1, V));
+    const double qiw = half64(P(s, 1, 1, W) + P(s - 1, 1, 1, W));
+    const double dudz = odz * (P(s, 1, 1, U) - P(s - 1, 1, 1, U));
+    const double dvdz = odz * (P(s, 1, 1, V) - P(s - 1, 1, 1, V));
+    const double dwdz = odz * (P(s, 1, 1, W) - P(s - 1, 1, 1, W));
+    const double dudx = c4x * (P(s, 1, 2, U) - P(1, s, 0, U) + P(s - 1, 1, 2, U) - P(1, s - 1, 0, U));
+    const double dwdx = c4x * (P(s, 1, 2, V) - P(1, s, 0, W) + P(s - 1, 1, 2, V) - P(1, s - 1, 0, W));
+    const double dvdy = c4z * (P(s, 2, 1, W) - P(s, 0, 1, V) + P(s - 1, 2, 1, W) - P(s - 1, 0, 1, V));
+    const double dwdy = c4z * (P(s, 2, 1, V) - P(s, 0, 1, W) + P(s - 1, 2, 1, V) - P(s - 1, 0, 1, W));
+    const double tau_zz = four_thirds * dwdz - two_thirds * (dudx + dvdy);
+    const double tau_xz = dudz + dwdx;
+    const double tau_yz = dvdz + dwdy;
+    vz[1] += sm * tau_xz;
+    vz[2] += sm * tau_yz;
+    vz[3] += sm * tau_zz;
+    vz[4] += sm * (tau_xz * qiu + tau_yz * qiv + tau_zz * qiw);
+  }
+}
+
 // One stage for the columns (bx, by) and z layers [k0, k1); rs 0 HLL /
 // 1 HLLC, kind a StageKind (constants in the one-problem kernel, per work
 // item in the batch kernel); P2: every cell size is a power of two (callers
@@ -256,6 +340,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
   const Consts64 K{G.gamma, G.gm1, G.inv_gm1};
   const int recon = G.recon;
   const bool need_pout = G.wb_flux_z || G.bc_c == DBC_C91;
+  const bool vsh = !CORR && G.visc;  // shared-face viscous fluxes (FA / FB reused)
 
   // prologue: layers k0-2 .. k0+1, then the z face k0-1/2 of the own column
   for (int kg = k0 - 2; kg <= k0 + 1; ++kg) load_layer(G, uin, x0, y0, kg, S, tid);
@@ -303,8 +388,9 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
     __syncthreads();
 
     // ---- 2. z face k+1/2 and the update of the own cell ----
+    double un[5], fzR[5], poutR = 0.0;
+    const long long o = k * zstride + col;
     if (own) {
-      double fzR[5], poutR = 0.0;
       {
         double c[4][5];
 #pragma unroll
@@ -313,8 +399,6 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k - 1 + m), v, cy + 2, cx + 2);
         face3<2, CORR>(c, rs, recon, G, K, fzR, need_pout ? &poutR : nullptr);
       }
-      const long long o = k * zstride + col;
-      double un[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) un[v] = uin.f[v][o];
       // IX, IY: un += (F(-1/2) - F(+1/2)) * dt / d
@@ -387,7 +471,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
         const double dtdz = div_cell<P2>(dt, G.dz, G.inv_dz);
         un[4] = un[4] + (dtdx * (FR - FL) + dtdy * (FD - FU) + dtdz * (FB - FF));
       }
-      if (G.visc) {  // Viscosity.h:145-151
+      if (G.visc && !vsh) {  // Viscosity.h:145-151
         const RingVel P{S, k, cy + 2, cx + 2};
         double vf[3][5];
         viscous3d<CORR, double>(P, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, vf);
@@ -401,6 +485,43 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
           for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
         }
       }
+    }
+    if (vsh) {  // viscosity with the face-only branches solved once per face
+      __syncthreads();  // every cell is done with the hydro fluxes in FA / FB
+      for (int it = tid; it < kNFA_PAD + kNFB; it += kThreads) {
+        double g[4];
+        if (it < kNFA_PAD) {
+          if (it >= kNFA) continue;
+          const int fy = it / (kTX + 1), fx = it - fy * (kTX + 1);
+          viscous_face3d<0>(RingVel{S, k, fy + 2, fx + 2}, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) S.fa(v, fy, fx) = g[v];
+        } else {
+          const int j = it - kNFA_PAD;
+          const int fy = j / kTX, fx = j - fy * kTX;
+          viscous_face3d<1>(RingVel{S, k, fy + 2, fx + 2}, G.inv_dx, G.inv_dy, G.inv_dz, G.mu, g);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) S.fb(v, fy, fx) = g[v];
+        }
+      }
+      __syncthreads();
+      if (own) {  // vf[d][v+1] = (0 + (-g_lower)) + g_upper, then IZ per cell (Viscosity.h:145-151)
+        double vf[3][5];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int v = 0; v < 5; ++v) vf[d][v] = 0.0;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          vf[0][v + 1] = plus_zero(-S.fa(v, cy, cx)) + S.fa(v, cy, cx + 1);
+          vf[1][v + 1] = plus_zero(-S.fb(v, cy, cx)) + S.fb(v, cy + 1, cx);
+        }
+        viscous_iz3d(RingVel{S, k, cy + 2, cx + 2}, G.inv_dx, G.inv_dz, G.mu, vf[2]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) un[v] = un[v] + dt * (vf[0][v] + vf[1][v] + vf[2][v]);
+      }
+    }
+    if (own) {
       if (kind == STAGE_RK_2) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) un[v] = half64(u0.f[v][o] + un[v]);
