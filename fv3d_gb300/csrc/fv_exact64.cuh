@@ -65,6 +65,52 @@ __device__ __forceinline__ double minmod_exact(double dL, double dR) {
   return minmod_rare(dL, dR);
 }
 
+// Comparisons and C99 fmin / fmax on bit patterns (integer pipe; the FP64
+// pipe's DSETP / DMNMX issue at the FP64 rate).  For non-NaN operands each
+// returns what the FP64 instruction returns -- min / max give one operand
+// exactly; where the two operands are +0 and -0 the sign of the zero chosen
+// may differ, which none of the callers can observe (their results do not
+// depend on the sign of a zero speed or of a zero compared with zero).  A
+// NaN operand is handled as fmin / fmax and the IEEE comparisons do.
+__device__ __forceinline__ bool is_nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+
+// Signed-integer key that orders like the double (negative values reversed).
+__device__ __forceinline__ long long order_key(long long b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+
+__device__ __forceinline__ double fmin_bits(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if (is_nan_bits(x)) return b;
+  if (is_nan_bits(y)) return a;
+  return order_key(y) < order_key(x) ? b : a;
+}
+
+__device__ __forceinline__ double fmax_bits(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if (is_nan_bits(x)) return b;
+  if (is_nan_bits(y)) return a;
+  return order_key(y) > order_key(x) ? b : a;
+}
+
+// x >= 0.0, x > 0.0 and x <= 0.0 as IEEE comparisons (false for NaN).
+__device__ __forceinline__ bool ge0_bits(double v) {
+  const long long b = __double_as_longlong(v);
+  return (b >= 0 && b <= 0x7ff0000000000000LL) || b == (long long)0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool gt0_bits(double v) {
+  const long long b = __double_as_longlong(v);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool le0_bits(double v) {
+  const long long b = __double_as_longlong(v);
+  return b == 0 || (b < 0 && !is_nan_bits(b));
+}
+
+// !(v <= limit) for a limit > 0 and a v that is >= 0 or NaN (a CFL sum).
+__device__ __forceinline__ bool above_bits(double v, double limit) {
+  const long long b = __double_as_longlong(v);
+  return !(b >= 0 && b <= __double_as_longlong(limit));
+}
+
 // RN(0.5 * x) with integer instructions only.  For |x| >= 2^-1021 the
 // product is exact: x with its exponent decremented (only the high word
 // changes).  Below that the halved value is subnormal: the magnitude in units

@@ -439,7 +439,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
         un[3] = un[3] + dt * rho_c * G.g;
         un[4] = un[4] + half64(dt) * (fL[0] + fR[0]) * G.g;
       }
-      un[0] = fmax(1.0e-6, un[0]);
+      un[0] = fmax_bits(1.0e-6, un[0]);
 
       if (G.tc) {  // ThermalConduction.h:38-96
         double kC, kF, kB;
@@ -533,7 +533,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
         const double inv = inv_dt_hyp64<PLANE_XY, true, P2>(un, G, q);
         const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
         red = b > red ? b : red;
-        if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+        if (above_bits(inv, 1.0e300)) atomicOr(&ctrl->err, 1);
         if (hout.f[0]) {  // primitives to the caller's unpadded arrays
           const long long h = ((long long)k * G.nb + y) * G.na + x;
 #pragma unroll

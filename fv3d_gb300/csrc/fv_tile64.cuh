@@ -636,7 +636,7 @@ __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Field
       un[2] = un[2] + dt * V.q(0, cy + 2, cx + 2) * G.g;
       un[4] = un[4] + half64(dt) * (V.fb(0, cy, cx) + V.fb(0, cy + 1, cx)) * G.g;
     }
-    un[0] = fmax(1.0e-6, un[0]);
+    un[0] = fmax_bits(1.0e-6, un[0]);
 
     if (G.tc) {  // ThermalConduction.h:47-95, constant kappa, 2-D
       const double kf = half64(G.kappa + G.kappa);
@@ -677,7 +677,7 @@ __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Field
       const double inv = inv_dt_hyp64<PLANE, WACT, P2>(un, G, q);
       const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
       red = b > red ? b : red;
-      if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+      if (above_bits(inv, 1.0e300)) atomicOr(&ctrl->err, 1);
       if (hout) {
         const long long h = (long long)y * G.na + x;
 #pragma unroll
