@@ -39,9 +39,11 @@ struct fv_sim {
   int deg_bc = FV_BC_PERIODIC;  // boundary of the one-cell axis (2-D kernels)
   int refl_deg = 0;             // bit a: axis a has one cell and reflects
   double* d_kappa_z = nullptr;  // B02 face conductivities per z layer
-  double* buf = nullptr;      // 3 states x 5 fields x fstride doubles
+  double* buf = nullptr;      // 3 (4 with Q) states x 5 fields x fstride doubles
   Fields A{}, B{}, S{};       // A: state, B: U* / ping-pong, S: scratch
-  fv::TmaState tma[2];        // TMA descriptors of A and B (2-D plane kernels)
+  Fields Q{};                 // 2-D RK2: primitives of A, written by stage 2, read by stage 1
+  bool q_dirty = false;       // work that may set ctrl->q_valid was enqueued since it was last cleared
+  fv::TmaState tma[3];        // TMA descriptors of A, B and Q (2-D plane kernels)
   bool tma_ok = false;
   int cur = 0;                // Euler ping-pong: state in A (0) or B (1)
   StepCtrl* d_ctrl = nullptr;
@@ -331,6 +333,14 @@ const fv::TmaState* TmaOf(const fv_sim* s, const Fields& u) {
   return nullptr;
 }
 
+// Marks the primitive copy Q stale (stream-ordered): called whenever the
+// host replaces the state.
+int DropPrims(fv_sim* s) {
+  if (s->Q.f[0] && s->q_dirty) CUDA_TRY(s, cudaMemsetAsync(&s->d_ctrl->q_valid, 0, sizeof(int), s->stream));
+  s->q_dirty = false;
+  return FV_OK;
+}
+
 int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fields* hout = nullptr) {
   {
     Timed t(s, KC_DT);
@@ -340,10 +350,21 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fiel
   }
   const int rs = s->p.riemann_solver == FV_HLL ? 0 : 1;
   if (s->p.time_stepping == FV_TS_RK2) {
+    // A step that hands its result to the host (step_host) is followed by
+    // a new state, so it leaves no copy.
+    fv::PrimCopy read_q, write_q;
+    if (s->Q.f[0]) {
+      read_q.qin = &s->Q;
+      read_q.tq = s->tma_ok ? &s->tma[2] : nullptr;
+      if (!hout) {
+        write_q.qout = &s->Q;
+        s->q_dirty = true;
+      }
+    }
     {
       Timed t(s, KC_STAGE);
       cudaError_t e = fv::launch_stage(s->G, rs, fv::STAGE_RK_1, s->wact, s->A, s->A, s->B, s->d_ctrl, s->stream,
-                                       nullptr, TmaOf(s, s->A));
+                                       nullptr, TmaOf(s, s->A), &read_q);
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 1 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
@@ -351,7 +372,7 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fiel
       Timed t(s, KC_STAGE);
       cudaError_t e =
           fv::launch_stage(s->G, rs, fv::STAGE_RK_2, s->wact, s->B, s->A, s->A, s->d_ctrl, s->stream, hout,
-                           TmaOf(s, s->B));
+                           TmaOf(s, s->B), &write_q);
       if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "stage 2 launch: %s", cudaGetErrorString(e));
       if (counting) t.done();
     }
@@ -479,7 +500,9 @@ int SetState(fv_sim* s, const double* const ref_fields[5], bool prim) {
   }
   ResetGraph(s);
   s->cur = 0;
-  int rc = CopyIn(s, s->A, src, true);
+  int rc = DropPrims(s);
+  if (rc) return rc;
+  rc = CopyIn(s, s->A, src, true);
   if (rc) return rc;
   if (prim) {
     Timed t(s, KC_CONV);
@@ -541,7 +564,8 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
     s->buf = nullptr;
     return rc;
   }
-  const size_t bytes = (size_t)3 * 5 * s->G.fstride * sizeof(double);
+  const bool with_q = s->G.ndim == 2 && s->p.time_stepping == FV_TS_RK2;
+  const size_t bytes = (size_t)(with_q ? 4 : 3) * 5 * s->G.fstride * sizeof(double);
   if (cudaMalloc(&s->buf, bytes) != cudaSuccess) {
     *out = s;
     return Fail(s, FV_ERR_NOMEM, "cudaMalloc of %zu bytes failed", bytes);
@@ -573,8 +597,10 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
   s->A = StateAt(s->buf, s->G.fstride);
   s->B = StateAt(s->buf + 5 * s->G.fstride, s->G.fstride);
   s->S = StateAt(s->buf + 10 * s->G.fstride, s->G.fstride);
+  if (with_q) s->Q = StateAt(s->buf + 15 * s->G.fstride, s->G.fstride);
   s->tma_ok = s->G.ndim == 2 && fv::encode_tma_state(s->G, s->A, &s->tma[0]) &&
-              fv::encode_tma_state(s->G, s->B, &s->tma[1]);
+              fv::encode_tma_state(s->G, s->B, &s->tma[1]) &&
+              (!with_q || fv::encode_tma_state(s->G, s->Q, &s->tma[2]));
   if (cudaMalloc(&s->d_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
       cudaMallocHost(&s->h_ctrl, sizeof(StepCtrl)) != cudaSuccess ||
       cudaMalloc(&s->d_partial, kMaxTotalsBlocks * 10 * sizeof(double)) != cudaSuccess ||
@@ -727,6 +753,8 @@ int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double
   s->cur = 0;
   const bool cfl = !(dt > 0.0);
   const int slot = (int)(s->step & 1);
+  int rc0 = DropPrims(s);
+  if (rc0) return rc0;
   if (cfl) CUDA_TRY(s, cudaMemsetAsync(&s->d_ctrl->slot[slot], 0, sizeof(unsigned long long), s->stream));
   {
     Timed t(s, KC_CONV);
@@ -850,6 +878,7 @@ int fvgpu_advance(fv_sim* s, double tend, long max_steps, double* t, long* nstep
         s->graph_key = key;
         s->graph_stream = s->stream;
       }
+      s->q_dirty = true;
       CUDA_TRY(s, cudaGraphLaunch(s->graph, s->stream));
       s->launches += (long)kGraphSteps * KernelsPerStep(s);
       if (s->p.time_stepping != FV_TS_RK2 && (kGraphSteps & 1)) s->cur ^= 1;

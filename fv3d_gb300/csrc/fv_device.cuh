@@ -32,6 +32,7 @@ struct StepCtrl {
   int parity;          // slot read by this step's control = step & 1
   int mode;            // 0: dt = dt_given; 1: CFL dt, loop bound t + eps < tend
   int err;             // sticky: bit0 non-finite/negative state seen, bit1 a bounded wait (TMA staging) gave up
+  int q_valid;         // the primitive copy of the state (2-D RK2 handles) matches it
 };
 
 // Programmatic dependent launch (PTX griddepcontrol) for the kernels of the

@@ -69,9 +69,20 @@ constexpr int kTileY = FV_TILE2D_Y;
 // host memory).
 // tin (optional): TMA descriptors of uin (encode_tma_state); interior
 // blocks are then staged by tensor copies instead of per-thread loads.
+// prims (optional): a padded primitive copy Q of the state (same layout as
+// the conserved fields).  A stage given qout writes the primitives of its
+// result there and sets ctrl->q_valid; a stage given qin reads its halo
+// from Q instead of converting uin when ctrl->q_valid is set (the host
+// clears it whenever it writes the state).  Q holds the same bits
+// consToPrim gives, so the results are unchanged.
+struct PrimCopy {
+  const Fields* qin = nullptr;   // read by this stage (Q == primitives of uin)
+  const Fields* qout = nullptr;  // written by this stage (primitives of uout)
+  const TmaState* tq = nullptr;  // TMA descriptors of Q (with qin)
+};
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                            Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
-                           const TmaState* tin = nullptr);
+                           const TmaState* tin = nullptr, const PrimCopy* prims = nullptr);
 
 // Encodes the TMA descriptors of state u of the 2-D problem G for the stage
 // kernel (tensor na x rows of doubles, row pitch G.pitch, boxes of
@@ -88,9 +99,9 @@ cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields u
 // The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
 inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                                 Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
-                                const TmaState* tin = nullptr) {
+                                const TmaState* tin = nullptr, const PrimCopy* prims = nullptr) {
   if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream, hout);
-  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout, tin);
+  return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout, tin, prims);
 }
 
 // primToCons (States.h:20-31) from primitive arrays the GPU can address

@@ -23,29 +23,34 @@ constexpr size_t kSmemAlign = 128;
 template <int PLANE, int RS, int KIND, bool WACT>
 __global__ void __launch_bounds__(kTileThreads, WACT ? FV_FP64_MIN_CTAS_W : FV_FP64_MIN_CTAS)
 stage2d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             const Fields hout, long long units, const __grid_constant__ TmaState tin, int use_tma) {
+             const Fields hout, long long units, const __grid_constant__ TmaState tin, int use_tma, const Fields qin,
+             const Fields qout, const __grid_constant__ TmaState tq, int use_tq) {
   extern __shared__ __align__(128) unsigned char smem_bytes[];
   __shared__ unsigned long long s_red[kTileThreads / 32];
   __shared__ __align__(8) unsigned long long s_mbar;
   const unsigned sa = smem_u32(smem_bytes);
   double* smem = reinterpret_cast<double*>(smem_bytes + (((sa + kSmemAlign - 1) & ~(unsigned)(kSmemAlign - 1)) - sa));
   pdl_wait();
-  if (use_tma) {
+  if (use_tma || use_tq) {
     if (threadIdx.x == 0) {
       mbar_init(&s_mbar, 1);
       fence_mbar_init();
     }
     __syncthreads();
   }
-  const TmaState* tp = use_tma ? &tin : nullptr;
+  // the primitive copy of uin, when the last stage that wrote uin left one
+  const bool prims = qin.f[0] != nullptr && ctrl->q_valid != 0;
+  const Fields* qi = prims ? &qin : nullptr;
+  const Fields* qo = qout.f[0] ? &qout : nullptr;
+  const TmaState* tp = prims ? (use_tq ? &tq : nullptr) : (use_tma ? &tin : nullptr);
   const Fields* ho = hout.f[0] ? &hout : nullptr;
   const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   if (G.pow2_all)
     stage_strip64<PLANE, WACT, SingleTile, true>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem, s_red, ho, tp,
-                                                 &s_mbar);
+                                                 &s_mbar, qi, qo);
   else
     stage_strip64<PLANE, WACT, SingleTile, false>(G, uin, u0, uout, ctrl, RS, KIND, ub, ue, smem, s_red, ho, tp,
-                                                  &s_mbar);
+                                                  &s_mbar, qi, qo);
   pdl_trigger();
 }
 
@@ -61,7 +66,7 @@ int sm_count() {
 
 template <int PLANE, int RS, int KIND, bool WACT>
 cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, const Fields* hout,
-                       const TmaState* tin, cudaStream_t st) {
+                       const TmaState* tin, const PrimCopy& pc, cudaStream_t st) {
   using SM = TileSmem<double, WACT ? 5 : 4, SingleTile>;
   auto kern = stage2d_fp64<PLANE, RS, KIND, WACT>;
   static bool attr_set = false;  // per instantiation, once per process
@@ -87,36 +92,41 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   const Fields none{};
   static const TmaState no_tma{};
   const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kTileThreads), smem, st, G, uin, u0, uout, ctrl,
-                                   hout ? *hout : none, units, tin ? *tin : no_tma, tin ? 1 : 0);
+                                   hout ? *hout : none, units, tin ? *tin : no_tma, tin ? 1 : 0,
+                                   pc.qin ? *pc.qin : none, pc.qout ? *pc.qout : none, pc.tq ? *pc.tq : no_tma,
+                                   pc.tq ? 1 : 0);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int PLANE, int RS, bool WACT>
 cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                        const Fields* hout, const TmaState* tin, cudaStream_t st) {
+                        const Fields* hout, const TmaState* tin, const PrimCopy& pc, cudaStream_t st) {
   switch (kind) {
-    case STAGE_EULER: return launch_one<PLANE, RS, STAGE_EULER, WACT>(G, uin, u0, uout, ctrl, hout, tin, st);
-    case STAGE_RK_1: return launch_one<PLANE, RS, STAGE_RK_1, WACT>(G, uin, u0, uout, ctrl, nullptr, tin, st);
-    default: return launch_one<PLANE, RS, STAGE_RK_2, WACT>(G, uin, u0, uout, ctrl, hout, tin, st);
+    case STAGE_EULER: return launch_one<PLANE, RS, STAGE_EULER, WACT>(G, uin, u0, uout, ctrl, hout, tin, pc, st);
+    case STAGE_RK_1: return launch_one<PLANE, RS, STAGE_RK_1, WACT>(G, uin, u0, uout, ctrl, nullptr, tin, pc, st);
+    default: return launch_one<PLANE, RS, STAGE_RK_2, WACT>(G, uin, u0, uout, ctrl, hout, tin, pc, st);
   }
 }
 
 template <int PLANE, int RS>
 cudaError_t launch_w(const Grid& G, int kind, bool wact, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                     const Fields* hout, const TmaState* tin, cudaStream_t st) {
-  return wact ? launch_kind<PLANE, RS, true>(G, kind, uin, u0, uout, ctrl, hout, tin, st)
-              : launch_kind<PLANE, RS, false>(G, kind, uin, u0, uout, ctrl, hout, tin, st);
+                     const Fields* hout, const TmaState* tin, const PrimCopy& pc, cudaStream_t st) {
+  return wact ? launch_kind<PLANE, RS, true>(G, kind, uin, u0, uout, ctrl, hout, tin, pc, st)
+              : launch_kind<PLANE, RS, false>(G, kind, uin, u0, uout, ctrl, hout, tin, pc, st);
 }
 
 }  // namespace
 
 cudaError_t launch_stage2d(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
-                           Fields uout, StepCtrl* ctrl, cudaStream_t st, const Fields* hout, const TmaState* tin) {
+                           Fields uout, StepCtrl* ctrl, cudaStream_t st, const Fields* hout, const TmaState* tin,
+                           const PrimCopy* prims) {
+  static const PrimCopy no_prims{};
+  const PrimCopy& pc = prims ? *prims : no_prims;
   if (G.plane == PLANE_XY)
-    return riemann_solver == 0 ? launch_w<PLANE_XY, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st)
-                               : launch_w<PLANE_XY, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st);
-  return riemann_solver == 0 ? launch_w<PLANE_XZ, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st)
-                             : launch_w<PLANE_XZ, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, st);
+    return riemann_solver == 0 ? launch_w<PLANE_XY, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, pc, st)
+                               : launch_w<PLANE_XY, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, pc, st);
+  return riemann_solver == 0 ? launch_w<PLANE_XZ, 0>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, pc, st)
+                             : launch_w<PLANE_XZ, 1>(G, kind, wact, uin, u0, uout, ctrl, hout, tin, pc, st);
 }
 
 bool encode_tma_state(const Grid& G, const Fields& u, TmaState* tin) {

@@ -482,9 +482,13 @@ struct PrimView {
 // columns x0-2 .. x0+TX+1: conserved state -> primitives (and temperature),
 // ghost cells synthesised by index remapping (X-then-Y fill of
 // BoundaryConditions.h:146-192, corners included).
+//
+// prims: uin already holds the primitives of the state (the copy the last
+// RK2 stage wrote, bit-identical to consToPrim of the state), so only the
+// temperature's reciprocal is computed.
 template <int PLANE, bool WACT, class TL, class PV>
 __device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, const PV& V, int x0, int y0, int h0,
-                                             int h1, int tid) {
+                                             int h1, int tid, bool prims = false) {
   constexpr int HX = TL::HX;
   const int n = (h1 - h0) * HX;
   for (int idx = tid; idx < n; idx += kTileThreads) {
@@ -494,13 +498,19 @@ __device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, c
     const int sa = bc_source(x0 + hx - 2, G.na, G.bc_a, fa);
     const int sb = bc_source(y0 + hy - 2, G.nb, G.bc_b, fb);
     const long long o = (long long)sb * G.pitch + sa;
-    double u[5], q[5], y;
+    double u[5], q[5], y = 0.0;
     u[0] = uin.f[0][o];
     u[1] = uin.f[1][o];
     u[2] = uin.f[2][o];
     u[3] = WACT ? uin.f[3][o] : 0.0;
     u[4] = uin.f[4][o];
-    cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+    if (prims) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) q[v] = u[v];
+      if (G.tc) y = 1.0 / q[0];
+    } else {
+      cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+    }
     if (fa) q[1] = -q[1];
     if (fb) q[2] = -q[2];
 #pragma unroll
@@ -515,12 +525,19 @@ __device__ __forceinline__ void load_prims64(const Grid& G, const Fields& uin, c
 // own cells and are converted in place (the arithmetic of load_prims64; no
 // ghost cells, so no reflections).
 template <int PLANE, bool WACT, class TL, class PV>
-__device__ __forceinline__ void convert_rows64(const Grid& G, const PV& V, int h0, int h1, int tid) {
+__device__ __forceinline__ void convert_rows64(const Grid& G, const PV& V, int h0, int h1, int tid,
+                                               bool prims = false) {
   constexpr int HX = TL::HX;
+  if (prims && !G.tc) return;  // staged primitives need no conversion
   const int n = (h1 - h0) * HX;
   for (int idx = tid; idx < n; idx += kTileThreads) {
     const int r = idx / HX, hx = idx - r * HX;
     const int hy = h0 + r;
+    if (prims) {  // only the temperature
+      const double r = V.q(0, hy, hx), p = V.q(4, hy, hx);
+      V.temp(hy, hx) = div_by_rcp(p, r, 1.0 / r);
+      continue;
+    }
     double u[5], q[5], y;
     u[0] = V.q(0, hy, hx);
     u[1] = V.q(1, hy, hx);
@@ -604,10 +621,14 @@ __device__ __forceinline__ void faces64(const Grid& G, const Consts64& K, const 
 
 // Phase 3-5: the cells of rows 0..nr-1 of the block -- conservative update,
 // sources, RK2 combination, CFL term (max folded into red).
+//
+// qout (optional, last stage of a step): the primitives of the result are
+// also written there, in the state's own layout, for the next step's load.
 template <int PLANE, bool WACT, class TL, bool P2, bool VSH, class PV>
 __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Fields& uin, const Fields& u0,
                                          const Fields& uout, StepCtrl* ctrl, int kind, double dt, int x0, int y0,
-                                         int nr, int tid, const Fields* hout, unsigned long long& red) {
+                                         int nr, int tid, const Fields* hout, unsigned long long& red,
+                                         const Fields* qout = nullptr) {
   constexpr int TX = TL::TX;
   const double db = PLANE == PLANE_XY ? G.dy : G.dz;
   const double inv_db = PLANE == PLANE_XY ? G.inv_dy : G.inv_dz;
@@ -684,6 +705,11 @@ __device__ __forceinline__ void update64(const Grid& G, const PV& V, const Field
         for (int v = 0; v < 5; ++v)
           if (hout->f[v]) hout->f[v][h] = q[v];
       }
+      if (qout) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          if (WACT || v != 3) qout->f[v][o] = q[v];
+      }
     }
   }
 }
@@ -724,7 +750,8 @@ __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin
                                                 const Fields& uout, StepCtrl* ctrl, int rs, int kind, double dt,
                                                 int x0, int ya, int yb, double* smem, const Fields* hout,
                                                 unsigned long long& red, const TmaState* tin = nullptr,
-                                                unsigned long long* mbar = nullptr, unsigned* phase = nullptr) {
+                                                unsigned long long* mbar = nullptr, unsigned* phase = nullptr,
+                                                const Fields* qin = nullptr, const Fields* qout = nullptr) {
   constexpr int NV = WACT ? 5 : 4;
   constexpr int TX = TL::TX, TY = TL::TY, HY = TL::HY;
   using SM = TileSmem<double, NV, TL>;
@@ -753,14 +780,14 @@ __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin
     const bool staged = tin && nr == TY && x0 >= 2 && x0 + TX + 2 <= G.na && y0 + h0 >= 2 && y0 + TY + 2 <= G.nb;
     if (staged) {
       stage_rows_tma<WACT, TL>(tin, V, mbar, *phase, x0, y0, h0, TY + 4, ctrl);
-      convert_rows64<PLANE, WACT, TL>(G, V, h0, TY + 4, tid);
+      convert_rows64<PLANE, WACT, TL>(G, V, h0, TY + 4, tid, qin != nullptr);
     } else {
-      load_prims64<PLANE, WACT, TL>(G, uin, V, x0, y0, h0, nr + 4, tid);
+      load_prims64<PLANE, WACT, TL>(G, qin ? *qin : uin, V, x0, y0, h0, nr + 4, tid, qin != nullptr);
     }
     __syncthreads();
     faces64<PLANE, WACT, TL, WACT>(G, K, V, rs, nr, first ? 0 : 1, tid);
     __syncthreads();
-    update64<PLANE, WACT, TL, P2, WACT>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red);
+    update64<PLANE, WACT, TL, P2, WACT>(G, V, uin, u0, uout, ctrl, kind, dt, x0, y0, nr, tid, hout, red, qout);
     __syncthreads();
     base += TY;
     if (base >= HY) base -= HY;
@@ -772,11 +799,14 @@ __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin
 // CTA owns units [u0_, u1_), processed as strip segments (stage_segment64).
 // Host code splits the units evenly over the CTAs that fit on the GPU at
 // once, which balances the FP64 work per SM whatever the grid shape.
+// qin / qout: the primitive copy of the state read in place of uin's
+// conversion (when ctrl->q_valid) / written by the last stage of a step.
 template <int PLANE, bool WACT, class TL, bool P2>
 __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, const Fields& u0, const Fields& uout,
                                               StepCtrl* ctrl, int rs, int kind, long long u0_, long long u1_,
                                               double* smem, unsigned long long* s_red, const Fields* hout,
-                                              const TmaState* tin = nullptr, unsigned long long* mbar = nullptr) {
+                                              const TmaState* tin = nullptr, unsigned long long* mbar = nullptr,
+                                              const Fields* qin = nullptr, const Fields* qout = nullptr) {
   constexpr int TX = TL::TX;
   const int tid = threadIdx.x;
   const int active = ctrl->active;
@@ -795,9 +825,11 @@ __device__ __forceinline__ void stage_strip64(const Grid& G, const Fields& uin, 
       continue;
     }
     stage_segment64<PLANE, WACT, TL, P2>(G, uin, u0, uout, ctrl, rs, kind, dt, x0, ya, yb, smem, hout, red, tin,
-                                         mbar, &phase);
+                                         mbar, &phase, qin, qout);
   }
   if (active && kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+  // the copy is complete once this launch is (the next reader is a later kernel)
+  if (active && qout && tid == 0) ctrl->q_valid = 1;
 }
 
 // Viscous fluxes of Viscosity.h:40-143 with the reference's arithmetic,
