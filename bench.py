@@ -44,13 +44,15 @@ WORKLOAD = "rayleigh_taylor_512x1536_fp64"
 ALGO_BYTES_PER_CELL_UPDATE = 160  # 5 passes x 4 fields x 8 B (F = 4, inviscid 2-D)
 # dram__bytes_read.sum + dram__bytes_write.sum of the two stage launches of one
 # RK2 step of this workload, from one ncu --set full capture
-# (profiles/stage2d_fp64_rt512x1536.md: 25.23+0.07 MB and 50.40+0.09 MB).
-NCU_TRAFFIC_BYTES_PER_STEP = 75.79e6
+# (profiles/stage2d_fp64_rt512x1536.md: stage 1 50.70+2.03 MB -- the
+# primitive copy of U^n for its halo plus U^n at its own cells --, stage 2
+# 50.55+3.58 MB).
+NCU_TRAFFIC_BYTES_PER_STEP = 106.86e6
 # FP64 arithmetic lane operations (DADD + DMUL + DFMA thread instructions)
-# per cell-update of this workload from the same capture (stage 1: 384.0,
-# stage 2: 425.0).  The FP64 kernel is bound by the FP64 pipe: its roofline
+# per cell-update of this workload from the same capture (stage 1: 364.4,
+# stage 2: 425.5).  The FP64 kernel is bound by the FP64 pipe: its roofline
 # against the FP64 FMA rate measured live by fvgpu_probe_fp64_rate.
-FP64_OPS_PER_CELL_UPDATE = 809
+FP64_OPS_PER_CELL_UPDATE = 790
 
 
 def peaks():

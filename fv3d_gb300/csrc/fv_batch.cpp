@@ -302,8 +302,9 @@ int Autotune(fv_batch* b, Group& g) {
   StepCtrl* tune_ctrl = nullptr;
   BatchInst* tune_inst = nullptr;
   unsigned* tune_queue = nullptr;
+  const size_t nm = g.members.size();
   BCUDA(b, cudaMalloc(&tune_ctrl, sizeof(StepCtrl) * b->n));
-  BCUDA(b, cudaMalloc(&tune_inst, sizeof(BatchInst) * g.members.size()));
+  BCUDA(b, cudaMalloc(&tune_inst, sizeof(BatchInst) * nm * cand.size()));
   BCUDA(b, cudaMalloc(&tune_queue, sizeof(unsigned)));
   std::vector<StepCtrl> hc(b->n);
   for (int i = 0; i < b->n; ++i) {
@@ -316,38 +317,49 @@ int Autotune(fv_batch* b, Group& g) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const int kind = b->ts == FV_TS_RK2 ? fv::STAGE_RK_1 : fv::STAGE_EULER;
-  float best = 1e30f;
-  int best_c = -1;
   const int saved = g.shape;
-  for (int c = 0; c < (int)cand.size(); ++c) {
+  // Each candidate's descriptors get their own slice of tune_inst (host
+  // vectors kept alive until the copies are done).
+  std::vector<std::vector<BatchInst>> descs(cand.size());
+  std::vector<int> ntiles(cand.size(), 0), grid(cand.size(), 0);
+  for (size_t c = 0; c < cand.size(); ++c) {
     const int s = cand[c].first;
     const int occ = Occupancy(b, g, s);
     if (occ <= 0) continue;
-    int ntiles = 0;
-    std::vector<BatchInst> d = Describe(b, g, s, tune_ctrl, &ntiles, cand[c].second);
-    cudaMemcpyAsync(tune_inst, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice, b->stream);
-    g.shape = s;
-    const int grid = std::min(occ * SmCount(), ntiles);
-    float tot = 0.f;
-    for (int rep = 0; rep < 4; ++rep) {
+    descs[c] = Describe(b, g, s, tune_ctrl, &ntiles[c], cand[c].second);
+    cudaMemcpyAsync(tune_inst + c * nm, descs[c].data(), sizeof(BatchInst) * descs[c].size(),
+                    cudaMemcpyHostToDevice, b->stream);
+    grid[c] = std::min(occ * SmCount(), ntiles[c]);
+  }
+  // Rounds over all candidates (so that clock and power drift hits each
+  // alike), one warm-up round first; a candidate's time is its fastest run.
+  constexpr int kRounds = 5;
+  std::vector<float> best_ms(cand.size(), 1e30f);
+  for (int round = 0; round <= kRounds; ++round) {
+    for (size_t c = 0; c < cand.size(); ++c) {
+      if (!grid[c]) continue;
+      g.shape = cand[c].first;
       cudaMemsetAsync(tune_queue, 0, sizeof(unsigned), b->stream);
       cudaEventRecord(e0, b->stream);
-      cudaError_t e = LaunchStage(b, g, tune_inst, ntiles, grid, tune_queue, kind, b->flip);
+      cudaError_t e = LaunchStage(b, g, tune_inst + c * nm, ntiles[c], grid[c], tune_queue, kind, b->flip);
       cudaEventRecord(e1, b->stream);
       if (e != cudaSuccess) {
-        tot = 1e30f;
-        break;
+        grid[c] = 0;  // not launchable: drop it
+        continue;
       }
       cudaEventSynchronize(e1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      if (rep > 0) tot += ms;  // first launch is a warm-up
-    }
-    if (tot < best) {
-      best = tot;
-      best_c = c;
+      if (round > 0 && ms < best_ms[c]) best_ms[c] = ms;
     }
   }
+  float best = 1e30f;
+  int best_c = -1;
+  for (size_t c = 0; c < cand.size(); ++c)
+    if (grid[c] && best_ms[c] < best) {
+      best = best_ms[c];
+      best_c = (int)c;
+    }
   g.shape = best_c < 0 ? saved : cand[best_c].first;
   g.rows = best_c < 0 ? 0 : cand[best_c].second;
   cudaStreamSynchronize(b->stream);
