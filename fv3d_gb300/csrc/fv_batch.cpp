@@ -71,7 +71,7 @@ struct fv_batch {
   std::vector<int> deg_bc;
   std::vector<double> inv_tc, inv_visc;
   std::vector<char> wact, state_set, slot_valid;
-  std::vector<Fields> A, B;
+  std::vector<Fields> A, B, Q;  // Q: primitive copy of A (FP64 2-D RK2), else null
   double* buf = nullptr;
   double* scratch = nullptr;
   long long max_fstride = 0;
@@ -115,6 +115,11 @@ void StorageOrder(int plane, int slot_of[5]) {
 }
 
 const Fields& Current(const fv_batch* b, int i) { return b->flip ? b->B[i] : b->A[i]; }
+
+// FP64 2-D RK2 problems keep a primitive copy of U^n (BatchInst::Q).
+bool WithPrimCopy(const fv_batch* b, int i) {
+  return b->precision == FV_PREC_FP64 && b->ts == FV_TS_RK2 && b->G[i].ndim == 2;
+}
 
 // ---- tile-shape cache --------------------------------------------------
 
@@ -220,6 +225,7 @@ std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, St
     I.G = b->G[i];
     I.A = b->A[i];
     I.B = b->B[i];
+    I.Q = b->Q[i];
     I.ctrl = ctrl_base + i;
     I.tiles_x = (I.G.na + tx - 1) / tx;
     I.tiles_y = (I.G.nb + ty - 1) / ty;
@@ -241,10 +247,12 @@ int SmCount() {
   return sms > 0 ? sms : 1;
 }
 
-// Times the candidate shapes of a group on its own data.  Only the first
-// stage is run (RK2 stage 1 writes U* alone; Euler writes the idle buffer),
-// against a scratch copy of the control blocks, so the problems' state and
-// clocks are untouched.
+// Times the candidate shapes of a group on its own data, one whole step per
+// run (RK2: both stages; Euler: its one stage, which writes the idle
+// buffer), against scratch control blocks.  RK2 stage 2 overwrites U^n, so
+// the group's U^n is copied aside first and put back afterwards; without
+// room for that copy only stage 1 is timed.  The problems' state and clocks
+// are left as they were, and the tuning descriptors carry no primitive copy.
 int Autotune(fv_batch* b, Group& g) {
   if (g.ndim == 3) {  // one shape: the 16 x 16 column kernel
     g.shape = 0;
@@ -305,7 +313,7 @@ int Autotune(fv_batch* b, Group& g) {
   const size_t nm = g.members.size();
   BCUDA(b, cudaMalloc(&tune_ctrl, sizeof(StepCtrl) * b->n));
   BCUDA(b, cudaMalloc(&tune_inst, sizeof(BatchInst) * nm * cand.size()));
-  BCUDA(b, cudaMalloc(&tune_queue, sizeof(unsigned)));
+  BCUDA(b, cudaMalloc(&tune_queue, 2 * sizeof(unsigned)));
   std::vector<StepCtrl> hc(b->n);
   for (int i = 0; i < b->n; ++i) {
     std::memset(&hc[i], 0, sizeof(StepCtrl));
@@ -327,10 +335,35 @@ int Autotune(fv_batch* b, Group& g) {
     const int occ = Occupancy(b, g, s);
     if (occ <= 0) continue;
     descs[c] = Describe(b, g, s, tune_ctrl, &ntiles[c], cand[c].second);
+    for (auto& I : descs[c]) I.Q = Fields{};
     cudaMemcpyAsync(tune_inst + c * nm, descs[c].data(), sizeof(BatchInst) * descs[c].size(),
                     cudaMemcpyHostToDevice, b->stream);
     grid[c] = std::min(occ * SmCount(), ntiles[c]);
   }
+  // U^n of the group aside (RK2), when a quarter of the free memory holds it
+  double* backup = nullptr;
+  std::vector<size_t> a_doubles(nm);
+  size_t backup_doubles = 0;
+  if (b->ts == FV_TS_RK2) {
+    for (size_t m = 0; m < nm; ++m) {
+      a_doubles[m] = (size_t)5 * b->G[g.members[m]].fstride;  // A: 5 fields of fstride 8-byte values
+      backup_doubles += a_doubles[m];
+    }
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && backup_doubles * sizeof(double) <= free_b / 4 &&
+        cudaMalloc(&backup, backup_doubles * sizeof(double)) == cudaSuccess) {
+      size_t at = 0;
+      for (size_t m = 0; m < nm; ++m) {
+        cudaMemcpyAsync(backup + at, b->A[g.members[m]].f[0], a_doubles[m] * sizeof(double),
+                        cudaMemcpyDeviceToDevice, b->stream);
+        at += a_doubles[m];
+      }
+    } else {
+      cudaGetLastError();  // a refused allocation leaves no sticky error
+      backup = nullptr;
+    }
+  }
+  const bool both_stages = backup != nullptr;
   // Rounds over all candidates (so that clock and power drift hits each
   // alike), one warm-up round first; a candidate's time is its fastest run.
   constexpr int kRounds = 5;
@@ -339,9 +372,11 @@ int Autotune(fv_batch* b, Group& g) {
     for (size_t c = 0; c < cand.size(); ++c) {
       if (!grid[c]) continue;
       g.shape = cand[c].first;
-      cudaMemsetAsync(tune_queue, 0, sizeof(unsigned), b->stream);
+      cudaMemsetAsync(tune_queue, 0, 2 * sizeof(unsigned), b->stream);
       cudaEventRecord(e0, b->stream);
       cudaError_t e = LaunchStage(b, g, tune_inst + c * nm, ntiles[c], grid[c], tune_queue, kind, b->flip);
+      if (e == cudaSuccess && both_stages)
+        e = LaunchStage(b, g, tune_inst + c * nm, ntiles[c], grid[c], tune_queue + 1, fv::STAGE_RK_2, 0);
       cudaEventRecord(e1, b->stream);
       if (e != cudaSuccess) {
         grid[c] = 0;  // not launchable: drop it
@@ -355,14 +390,28 @@ int Autotune(fv_batch* b, Group& g) {
   }
   float best = 1e30f;
   int best_c = -1;
-  for (size_t c = 0; c < cand.size(); ++c)
+  const bool log = std::getenv("FV3D_TILE_LOG") != nullptr;
+  for (size_t c = 0; c < cand.size(); ++c) {
+    if (log)
+      std::fprintf(stderr, "fv3d tile candidate %dx%d: %.4f ms (%d items, %d CTAs)\n", shapes[cand[c].first].tx,
+                   cand[c].second, grid[c] ? best_ms[c] : -1.0f, ntiles[c], grid[c]);
     if (grid[c] && best_ms[c] < best) {
       best = best_ms[c];
       best_c = (int)c;
     }
+  }
   g.shape = best_c < 0 ? saved : cand[best_c].first;
   g.rows = best_c < 0 ? 0 : cand[best_c].second;
+  if (backup) {  // U^n back in place
+    size_t at = 0;
+    for (size_t m = 0; m < nm; ++m) {
+      cudaMemcpyAsync(b->A[g.members[m]].f[0], backup + at, a_doubles[m] * sizeof(double), cudaMemcpyDeviceToDevice,
+                      b->stream);
+      at += a_doubles[m];
+    }
+  }
   cudaStreamSynchronize(b->stream);
+  if (backup) cudaFree(backup);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(tune_ctrl);
@@ -524,7 +573,7 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
       return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: the FP32-mixed kernels address fields below 2^32 cells", i);
     b->wact[i] = (params[i].viscosity_active || b->G[i].ndim == 3) ? 1 : 0;
     off[i] = total;
-    total += (size_t)10 * b->G[i].fstride;
+    total += (size_t)(WithPrimCopy(b, i) ? 15 : 10) * b->G[i].fstride;
     b->max_fstride = std::max(b->max_fstride, b->G[i].fstride);
   }
   if (cudaMalloc(&b->buf, total * sizeof(double)) != cudaSuccess ||
@@ -543,10 +592,12 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
   BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned) * 2 * kMaxGroups, b->stream));
   b->A.resize(n);
   b->B.resize(n);
+  b->Q.assign(n, Fields{});
   for (int i = 0; i < n; ++i)
     for (int v = 0; v < 5; ++v) {
       b->A[i].f[v] = b->buf + off[i] + (size_t)v * b->G[i].fstride;
       b->B[i].f[v] = b->buf + off[i] + (size_t)(5 + v) * b->G[i].fstride;
+      if (WithPrimCopy(b, i)) b->Q[i].f[v] = b->buf + off[i] + (size_t)(10 + v) * b->G[i].fstride;
     }
   std::vector<StepCtrl> hc(n);
   for (int i = 0; i < n; ++i) {
@@ -598,6 +649,8 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
   if ((bool)b->wact[inst] != wact) b->prepared = false;
   b->wact[inst] = wact;
   if (!b->prepared) ReleaseGroups(b);
+  if (b->Q[inst].f[0])  // the primitive copy no longer matches the state
+    BCUDA(b, cudaMemsetAsync(&b->d_ctrl[inst].q_valid, 0, sizeof(int), b->stream));
   // FP64 values into the staging buffer (the current state for FP64, scratch
   // for the mixed form), primToCons in place, then split into pairs (mixed)
   Fields stage = b->precision == FV_PREC_FP64 ? Current(b, inst) : Fields();

@@ -72,6 +72,9 @@ batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
       uin = flip ? I.B : I.A; u0 = uin; uout = flip ? I.A : I.B;
     }
     StepCtrl* ctrl = I.ctrl;
+    // the primitive copy: read by stage 1 while valid, written by stage 2
+    const Fields* qi = kind == STAGE_RK_1 && I.Q.f[0] && ctrl->q_valid ? &I.Q : nullptr;
+    const Fields* qo = kind == STAGE_RK_2 && I.Q.f[0] ? &I.Q : nullptr;
     const int x0 = bx * TL::TX, ya = by * I.tz;  // tz: rows per work item
     const int yb = ya + I.tz < I.G.nb ? ya + I.tz : I.G.nb;
     if (!ctrl->active) {
@@ -81,11 +84,13 @@ batch_stage64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
     unsigned long long red = 0ull;
     if (I.G.pow2_all)
       stage_segment64<PLANE, WACT, TL, true>(I.G, uin, u0, uout, ctrl, I.rs, kind, ctrl->dt_cur, x0, ya, yb, smem_raw,
-                                             nullptr, red);
+                                             nullptr, red, nullptr, nullptr, nullptr, qi, qo);
     else
       stage_segment64<PLANE, WACT, TL, false>(I.G, uin, u0, uout, ctrl, I.rs, kind, ctrl->dt_cur, x0, ya, yb,
-                                              smem_raw, nullptr, red);
+                                              smem_raw, nullptr, red, nullptr, nullptr, nullptr, qi, qo);
     if (kind != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[ctrl->parity ^ 1], s_red);
+    // the copy is complete once this launch is (the next reader is a later kernel)
+    if (qo && threadIdx.x == 0) ctrl->q_valid = 1;
   }
 }
 

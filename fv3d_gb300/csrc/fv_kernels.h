@@ -139,10 +139,12 @@ enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
 
 // One problem of a batch as the persistent kernels see it.  FP64: A = U^n,
 // B = U* (Euler: ping-pong).  FP32-mixed: A = U^n as float2 (hi, lo) pairs,
-// B = U* as float (RK2) or the second pair buffer (Euler).
+// B = U* as float (RK2) or the second pair buffer (Euler).  Q (FP64 2-D RK2
+// only, else null): the primitive copy of A (PrimCopy), valid while
+// ctrl->q_valid is set.
 struct BatchInst {
   Grid G;
-  Fields A, B;
+  Fields A, B, Q;
   StepCtrl* ctrl;
   int tiles_x;  // tiles along a
   int tile0;    // first tile of this problem in its group's tile numbering

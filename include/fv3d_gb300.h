@@ -251,7 +251,9 @@ int fvgpu_batch_launch_count(const fv_batch* b, long* count);
  * launch per stage; reports the groups and the work-item shape the autotuner
  * chose for each: cells along x by rows along the second axis (a strip
  * segment; 3-D groups: 16 x 16 columns), tuning first if needed; every
- * problem must have a state.  FV3D_TILE=WxH forces a shape. */
+ * problem must have a state.  The autotuner times one whole step of each
+ * candidate shape (the state is saved and restored around it); FV3D_TILE=WxH
+ * forces a shape, FV3D_TILE_LOG=1 prints each candidate's time to stderr. */
 int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_groups);
 
 #ifdef __cplusplus

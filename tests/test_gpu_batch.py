@@ -90,6 +90,30 @@ def test_fp64_batch_bitwise_equals_single(nsteps):
     assert len(b.tiling()) == 3  # x-y; x-z with conduction/viscosity; x-z without
 
 
+def test_fp64_batch_state_replaced_after_steps():
+    """A problem whose state is set again after some steps restarts from that
+    state (the primitive copy an RK2 stage 2 kept of its old state is not
+    reused) while the other problems carry on."""
+    probs = mixed_set()
+    b = fv.Batch([p.params for p in probs])
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    b.run(3)
+    replaced = 1  # the 96^2 Sedov problem
+    pr = probs[replaced]
+    other = [None if a is None else a.copy() for a in pr.prim]
+    other[0] = other[0] * 1.25
+    other[4] = other[4] * 0.8
+    b.set_prim(replaced, *other)
+    b.run(4)
+    ref, _ = run_singles([problems.Problem(pr.name, pr.ini, other, params=pr.params)], 4)
+    for k, (x, y) in enumerate(zip(b.get_prim(replaced), ref[0])):
+        np.testing.assert_array_equal(x, y, err_msg="field %d" % k)
+    kept, _ = run_singles([probs[0]], 7)
+    for k, (x, y) in enumerate(zip(b.get_prim(0), kept[0])):
+        np.testing.assert_array_equal(x, y, err_msg="kept problem field %d" % k)
+
+
 def _run_forced_tile(tile, nsteps):
     code = (
         "import sys, numpy as np; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
@@ -120,6 +144,24 @@ def test_fp64_batch_independent_of_tile_shape(tile, tmp_path):
                        text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "(%s, %s)" % tuple(tile.split("x")) in r.stdout
+    np.testing.assert_array_equal(np.load(out), want)
+
+
+def test_fp64_batch_fresh_autotune_keeps_state(tmp_path):
+    """With an empty tile cache the autotuner times whole RK2 steps on the
+    problems' own state (stage 2 overwrites U^n) and puts U^n back: the run
+    that follows gives the same bits as each problem advanced alone."""
+    nsteps = 5
+    probs = mixed_set()
+    ref, _ = run_singles(probs, nsteps)
+    want = np.concatenate([np.stack(r).ravel() for r in ref])
+    out = str(tmp_path / "x.npy")
+    env = dict(os.environ, FV3D_TILE_CACHE=str(tmp_path / "tiles.txt"), FV3D_TILE_LOG="1")
+    env.pop("FV3D_TILE", None)
+    r = subprocess.run([sys.executable, "-c", _run_forced_tile(None, nsteps), out], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "fv3d tile candidate" in r.stderr  # the tuning ran
     np.testing.assert_array_equal(np.load(out), want)
 
 
