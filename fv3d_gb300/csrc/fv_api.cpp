@@ -41,7 +41,7 @@ struct fv_sim {
   double* d_kappa_z = nullptr;  // B02 face conductivities per z layer
   double* buf = nullptr;      // 3 (4 with Q) states x 5 fields x fstride doubles
   Fields A{}, B{}, S{};       // A: state, B: U* / ping-pong, S: scratch
-  Fields Q{};                 // 2-D RK2: primitives of A, written by stage 2, read by stage 1
+  Fields Q{};                 // RK2: primitives of A, written by stage 2, read by stage 1
   bool q_dirty = false;       // work that may set ctrl->q_valid was enqueued since it was last cleared
   fv::TmaState tma[3];        // TMA descriptors of A, B and Q (2-D plane kernels)
   bool tma_ok = false;
@@ -564,7 +564,7 @@ int fvgpu_create(const fv_params* params, fv_sim** out) {
     s->buf = nullptr;
     return rc;
   }
-  const bool with_q = s->G.ndim == 2 && s->p.time_stepping == FV_TS_RK2;
+  const bool with_q = s->p.time_stepping == FV_TS_RK2;
   const size_t bytes = (size_t)(with_q ? 4 : 3) * 5 * s->G.fstride * sizeof(double);
   if (cudaMalloc(&s->buf, bytes) != cudaSuccess) {
     *out = s;

@@ -94,13 +94,14 @@ bool encode_tma_state(const Grid& G, const Fields& u, TmaState* tin);
 // marched over z, the (column block, layer) units split evenly over the
 // resident CTAs; always carries w.
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
-                           StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr);
+                           StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
+                           const PrimCopy* prims = nullptr);
 
 // The stage kernel the grid needs (2-D plane kernel or 3-D kernel).
 inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, bool wact, Fields uin, Fields u0,
                                 Fields uout, StepCtrl* ctrl, cudaStream_t stream, const Fields* hout = nullptr,
                                 const TmaState* tin = nullptr, const PrimCopy* prims = nullptr) {
-  if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream, hout);
+  if (G.ndim == 3) return launch_stage3d(G, riemann_solver, kind, uin, u0, uout, ctrl, stream, hout, prims);
   return launch_stage2d(G, riemann_solver, kind, wact, uin, u0, uout, ctrl, stream, hout, tin, prims);
 }
 

@@ -61,7 +61,16 @@ struct Smem3 {
 __device__ __forceinline__ int slot_of(int kg) { return (kg + 4) & 3; }
 
 // consToPrim of one stored cell (x, y, z storage order), RN(1/rho) in y.
-__device__ __forceinline__ void load_prim(const Fields& u, long long o, double gm1, double q[5], double& y) {
+// With qsrc (the primitive copy of u, the same bits) the primitives are read
+// and y is computed only when need_y.
+__device__ __forceinline__ void load_prim(const Fields& u, const Fields* qsrc, long long o, double gm1, double q[5],
+                                          double& y, bool need_y = false) {
+  if (qsrc) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) q[v] = qsrc->f[v][o];
+    y = need_y ? 1.0 / q[0] : 0.0;
+    return;
+  }
   double w[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) w[v] = u.f[v][o];
@@ -72,13 +81,13 @@ __device__ __forceinline__ void load_prim(const Fields& u, long long o, double g
 // (already mapped through the x / y boundaries, with their velocity flips).
 // Note the reference scales the hydrostatic term by params.gravity, the
 // boolean, not by g.
-__device__ __forceinline__ void c91_ghost(const Grid& G, const Fields& u, long long col, bool fa, bool fb, int kg,
-                                          double res[5]) {
+__device__ __forceinline__ void c91_ghost(const Grid& G, const Fields& u, const Fields* qsrc, long long col, bool fa,
+                                          bool fb, int kg, double res[5]) {
   const int kref = kg < 0 ? 0 : G.nc - 1;
   const int ksym = kg < 0 ? -kg - 1 : 2 * G.nc - kg - 1;
   double qref[5], qsym[5], y;
-  load_prim(u, (long long)kref * G.nb * G.pitch + col, G.gm1, qref, y);
-  load_prim(u, (long long)ksym * G.nb * G.pitch + col, G.gm1, qsym, y);
+  load_prim(u, qsrc, (long long)kref * G.nb * G.pitch + col, G.gm1, qref, y);
+  load_prim(u, qsrc, (long long)ksym * G.nb * G.pitch + col, G.gm1, qsym, y);
   if (fa) {
     qref[1] = -qref[1];
     qsym[1] = -qsym[1];
@@ -117,9 +126,10 @@ __device__ __forceinline__ void c91_ghost(const Grid& G, const Fields& u, long l
   }
 }
 
-// Loads z layer kg of the tile at (x0, y0) into ring slot slot_of(kg).
-__device__ __forceinline__ void load_layer(const Grid& G, const Fields& u, int x0, int y0, int kg, const Smem3& S,
-                                           int tid) {
+// Loads z layer kg of the tile at (x0, y0) into ring slot slot_of(kg)
+// (from the primitive copy qsrc of u when given).
+__device__ __forceinline__ void load_layer(const Grid& G, const Fields& u, const Fields* qsrc, int x0, int y0, int kg,
+                                           const Smem3& S, int tid) {
   const int s = slot_of(kg);
   const bool c91 = G.bc_c == DBC_C91 && (kg < 0 || kg >= G.nc);
   bool fz = false;
@@ -135,13 +145,13 @@ __device__ __forceinline__ void load_layer(const Grid& G, const Fields& u, int x
     double T = 0.0;
     if (!c91) {
       double y;
-      load_prim(u, zoff + col, G.gm1, q, y);
+      load_prim(u, qsrc, zoff + col, G.gm1, q, y, G.tc != 0);
       if (fa) q[1] = -q[1];
       if (fb) q[2] = -q[2];
       if (fz) q[3] = -q[3];
       if (G.tc) T = div_by_rcp(q[4], q[0], y);
     } else {
-      c91_ghost(G, u, col, fa, fb, kg, q);
+      c91_ghost(G, u, qsrc, col, fa, fb, kg, q);
       if (G.tc) T = q[4] / q[0];
     }
 #pragma unroll
@@ -316,7 +326,8 @@ template <bool P2, bool CORR>
 __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin, const Fields& u0,
                                                 const Fields& uout, StepCtrl* __restrict__ ctrl, int rs, int kind,
                                                 int bx, int by, int k0, int k1, const Fields& hout, double* smem_raw,
-                                                unsigned long long& red) {
+                                                unsigned long long& red, const Fields* qin = nullptr,
+                                                const Fields* qout = nullptr) {
   const Smem3 S{smem_raw};
   const int tid = threadIdx.x;
   const int x0 = bx * kTX, y0 = by * kTY;
@@ -343,7 +354,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
   const bool vsh = !CORR && G.visc;  // shared-face viscous fluxes (FA / FB reused)
 
   // prologue: layers k0-2 .. k0+1, then the z face k0-1/2 of the own column
-  for (int kg = k0 - 2; kg <= k0 + 1; ++kg) load_layer(G, uin, x0, y0, kg, S, tid);
+  for (int kg = k0 - 2; kg <= k0 + 1; ++kg) load_layer(G, uin, qin, x0, y0, kg, S, tid);
   __syncthreads();
   double fzL[5], poutL = 0.0;
   if (own) {
@@ -359,7 +370,7 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
 #pragma unroll 1
   for (int k = k0; k < k1; ++k) {
     // ---- 1. layer k+2 in, x and y faces of layer k ----
-    load_layer(G, uin, x0, y0, k + 2, S, tid);
+    load_layer(G, uin, qin, x0, y0, k + 2, S, tid);
     const int sk = slot_of(k);
     for (int it = tid; it < kNFA_PAD + kNFB; it += kThreads) {
       double c[4][5], f[5];
@@ -540,6 +551,10 @@ __device__ __forceinline__ void stage3d_segment(const Grid& G, const Fields& uin
           for (int v = 0; v < 5; ++v)
             if (hout.f[v]) hout.f[v][h] = q[v];
         }
+        if (qout) {
+#pragma unroll
+          for (int v = 0; v < 5; ++v) qout->f[v][o] = q[v];
+        }
       }
 #pragma unroll
       for (int v = 0; v < 5; ++v) fzL[v] = fzR[v];
@@ -569,7 +584,8 @@ __device__ __forceinline__ void stage3d_body(const Grid& G, const Fields& uin, c
 template <bool P2, bool CORR, int RS, int KIND>
 __device__ __forceinline__ unsigned long long march3d(const Grid& G, const Fields& uin, const Fields& u0,
                                                       const Fields& uout, StepCtrl* __restrict__ ctrl, long long ub,
-                                                      long long ue, const Fields& hout, double* smem_raw) {
+                                                      long long ue, const Fields& hout, double* smem_raw,
+                                                      const Fields* qin, const Fields* qout) {
   const int tiles_x = (G.na + kTX - 1) / kTX;
   unsigned long long red = 0ull;
   for (long long u = ub; u < ue;) {
@@ -578,7 +594,7 @@ __device__ __forceinline__ unsigned long long march3d(const Grid& G, const Field
     const int k1 = (int)(k0 + (ue - u) < (long long)G.nc ? k0 + (ue - u) : (long long)G.nc);
     u += k1 - k0;
     stage3d_segment<P2, CORR>(G, uin, u0, uout, ctrl, RS, KIND, cb % tiles_x, cb / tiles_x, k0, k1, hout, smem_raw,
-                              red);
+                              red, qin, qout);
   }
   return red;
 }
@@ -589,16 +605,21 @@ __device__ __forceinline__ unsigned long long march3d(const Grid& G, const Field
 template <int RS, int KIND, bool CORR>
 __global__ void __launch_bounds__(kThreads, 2)
 stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
-             long long units, const Fields hout) {
+             long long units, const Fields hout, const Fields qin, const Fields qout) {
   extern __shared__ double smem_raw[];
   __shared__ unsigned long long s_red[kThreads / 32];
   pdl_wait();
   const long long ub = units * blockIdx.x / gridDim.x, ue = units * (blockIdx.x + 1) / gridDim.x;
   const int active = ctrl->active, parity = ctrl->parity;
+  // the primitive copy of uin, when the last stage that wrote uin left one
+  const Fields* qi = qin.f[0] && ctrl->q_valid ? &qin : nullptr;
+  const Fields* qo = qout.f[0] ? &qout : nullptr;
   const unsigned long long red =
-      G.pow2_all ? march3d<true, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw)
-                 : march3d<false, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw);
+      G.pow2_all ? march3d<true, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw, qi, qo)
+                 : march3d<false, CORR, RS, KIND>(G, uin, u0, uout, ctrl, ub, ue, hout, smem_raw, qi, qo);
   if (active && KIND != STAGE_RK_1) block_max_atomic(red, &ctrl->slot[parity ^ 1], s_red);
+  // the copy is complete once this launch is (the next reader is a later kernel)
+  if (active && qo && threadIdx.x == 0) ctrl->q_valid = 1;
   pdl_trigger();
 }
 
@@ -614,7 +635,7 @@ int sm_count3d() {
 
 template <int RS, int KIND, bool CORR>
 cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl, const Fields* hout,
-                       cudaStream_t st) {
+                       const PrimCopy& pc, cudaStream_t st) {
   auto kern = stage3d_fp64<RS, KIND, CORR>;
   static bool attr_set = false;  // per instantiation, once per process
   if (!attr_set) {
@@ -637,25 +658,26 @@ cudaError_t launch_one(const Grid& G, Fields uin, Fields u0, Fields uout, StepCt
   if (ctas < 1) ctas = 1;
   const Fields none{};
   const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kThreads), Smem3::bytes(tc), st, G, uin, u0, uout,
-                                   ctrl, units, hout ? *hout : none);
+                                   ctrl, units, hout ? *hout : none, pc.qin ? *pc.qin : none,
+                                   pc.qout ? *pc.qout : none);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int RS, bool CORR>
 cudaError_t launch_kind(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                        const Fields* hout, cudaStream_t st) {
+                        const Fields* hout, const PrimCopy& pc, cudaStream_t st) {
   switch (kind) {
-    case STAGE_EULER: return launch_one<RS, STAGE_EULER, CORR>(G, uin, u0, uout, ctrl, hout, st);
-    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1, CORR>(G, uin, u0, uout, ctrl, nullptr, st);
-    default: return launch_one<RS, STAGE_RK_2, CORR>(G, uin, u0, uout, ctrl, hout, st);
+    case STAGE_EULER: return launch_one<RS, STAGE_EULER, CORR>(G, uin, u0, uout, ctrl, hout, pc, st);
+    case STAGE_RK_1: return launch_one<RS, STAGE_RK_1, CORR>(G, uin, u0, uout, ctrl, nullptr, pc, st);
+    default: return launch_one<RS, STAGE_RK_2, CORR>(G, uin, u0, uout, ctrl, hout, pc, st);
   }
 }
 
 template <int RS>
 cudaError_t launch_phys(const Grid& G, int kind, Fields uin, Fields u0, Fields uout, StepCtrl* ctrl,
-                        const Fields* hout, cudaStream_t st) {
-  return G.corrected ? launch_kind<RS, true>(G, kind, uin, u0, uout, ctrl, hout, st)
-                     : launch_kind<RS, false>(G, kind, uin, u0, uout, ctrl, hout, st);
+                        const Fields* hout, const PrimCopy& pc, cudaStream_t st) {
+  return G.corrected ? launch_kind<RS, true>(G, kind, uin, u0, uout, ctrl, hout, pc, st)
+                     : launch_kind<RS, false>(G, kind, uin, u0, uout, ctrl, hout, pc, st);
 }
 
 static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
@@ -762,9 +784,11 @@ cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles
 }
 
 cudaError_t launch_stage3d(const Grid& G, int riemann_solver, int kind, Fields uin, Fields u0, Fields uout,
-                           StepCtrl* ctrl, cudaStream_t st, const Fields* hout) {
-  return riemann_solver == 0 ? launch_phys<0>(G, kind, uin, u0, uout, ctrl, hout, st)
-                             : launch_phys<1>(G, kind, uin, u0, uout, ctrl, hout, st);
+                           StepCtrl* ctrl, cudaStream_t st, const Fields* hout, const PrimCopy* prims) {
+  static const PrimCopy no_prims{};
+  const PrimCopy& pc = prims ? *prims : no_prims;
+  return riemann_solver == 0 ? launch_phys<0>(G, kind, uin, u0, uout, ctrl, hout, pc, st)
+                             : launch_phys<1>(G, kind, uin, u0, uout, ctrl, hout, pc, st);
 }
 
 }  // namespace fv

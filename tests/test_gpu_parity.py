@@ -132,13 +132,24 @@ def test_advance_fixed_steps_equals_stepping(name, nsteps):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("builder", ["sedov", "shear_layer"])
+def _random_3d_rk2(n):
+    """Periodic random n^3 state, HLLC, PLM, RK2, conduction + viscosity."""
+    return problems.random_problem(
+        "rk2_3d", problems._mesh(n, n, n),
+        {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "periodic", "boundaries_z": "periodic"},
+        {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2", "CFL": 0.4},
+        {"gamma0": 1.4}, seed=4242, wmag=0.5,
+        extra={"thermal_conduction": {"active": True, "kappa": 1e-4}, "viscosity": {"active": True, "mu": 1e-4}})
+
+
+@pytest.mark.parametrize("builder", ["sedov", "shear_layer", "random_3d"])
 @pytest.mark.parametrize("setter", ["set_prim", "set_cons"])
 def test_state_replaced_after_steps(builder, setter):
     """A state set after some steps is stepped from scratch: the primitive
-    copy the last RK2 stage kept of the old state is not reused (2-D RK2
-    handles; shear_layer carries the third momentum, with viscosity)."""
-    pr = problems.BUILDERS[builder](n=128)
+    copy the last RK2 stage kept of the old state is not reused (RK2
+    handles; shear_layer carries the third momentum, with viscosity; the 3-D
+    case runs the column kernel)."""
+    pr = _random_3d_rk2(40) if builder == "random_3d" else problems.BUILDERS[builder](n=128)
     other = [None if a is None else a.copy() for a in pr.prim]
     other[0] = other[0] * 1.25
     other[4] = other[4] * 0.8
