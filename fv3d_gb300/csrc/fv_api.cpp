@@ -350,16 +350,12 @@ int EnqueueStep(fv_sim* s, int mode, double dt, bool counting = true, const Fiel
   }
   const int rs = s->p.riemann_solver == FV_HLL ? 0 : 1;
   if (s->p.time_stepping == FV_TS_RK2) {
-    // A step that hands its result to the host (step_host) is followed by
-    // a new state, so it leaves no copy.
     fv::PrimCopy read_q, write_q;
     if (s->Q.f[0]) {
       read_q.qin = &s->Q;
       read_q.tq = s->tma_ok ? &s->tma[2] : nullptr;
-      if (!hout) {
-        write_q.qout = &s->Q;
-        s->q_dirty = true;
-      }
+      write_q.qout = &s->Q;
+      s->q_dirty = true;
     }
     {
       Timed t(s, KC_STAGE);
@@ -753,13 +749,16 @@ int fvgpu_step_host(fv_sim* s, const double* const prim_in[5], double dt, double
   s->cur = 0;
   const bool cfl = !(dt > 0.0);
   const int slot = (int)(s->step & 1);
-  int rc0 = DropPrims(s);
-  if (rc0) return rc0;
   if (cfl) CUDA_TRY(s, cudaMemsetAsync(&s->d_ctrl->slot[slot], 0, sizeof(unsigned long long), s->stream));
   {
+    // the conversion also writes the primitive copy of the new state (the
+    // consToPrim its CFL maximum computes) and marks it valid
     Timed t(s, KC_CONV);
+    const bool keep_q = s->Q.f[0] != nullptr;
     cudaError_t e = fv::launch_prim_to_cons_from(s->G, s->wact, src, s->A, cfl ? s->d_ctrl : nullptr, slot,
-                                                 s->stream);
+                                                 s->stream, keep_q ? &s->Q : nullptr,
+                                                 keep_q ? &s->d_ctrl->q_valid : nullptr);
+    if (keep_q) s->q_dirty = true;
     if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "primToCons launch: %s", cudaGetErrorString(e));
     t.done();
   }

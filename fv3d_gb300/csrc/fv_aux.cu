@@ -109,9 +109,11 @@ __global__ void prim_to_cons2d(const Grid G, const Fields u) {
 // primToCons from unpadded primitive arrays the GPU can address (a caller's
 // host arrays), optionally with the CFL maximum of the result.  Same
 // arithmetic as prim_to_cons2d.
+// qout (optional): the primitive copy of dst (consToPrim of the result, the
+// bits the stage kernels' own conversion gives), with *q_valid set after it.
 template <int PLANE, bool WACT, bool REDUCE>
 __global__ void __launch_bounds__(256) prim_to_cons_from(const Grid G, const Fields src, const Fields dst,
-                                                         StepCtrl* ctrl, int slot) {
+                                                         StepCtrl* ctrl, int slot, const Fields qout, int* q_valid) {
   __shared__ unsigned long long s_red[8];
   unsigned long long red = 0ull;
   const long long n = (long long)G.na * G.rows;
@@ -131,15 +133,28 @@ __global__ void __launch_bounds__(256) prim_to_cons_from(const Grid G, const Fie
     dst.f[2][o] = mb;
     if (WACT) dst.f[3][o] = mc;
     dst.f[4][o] = E;
-    if (REDUCE) {
+    if (REDUCE || qout.f[0]) {
       const double u[5] = {r, ma, mb, mc, E};
-      const double inv = inv_dt_hyp64<PLANE, WACT>(u, G);
-      const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
-      red = b > red ? b : red;
-      if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+      double q[5];
+      if (REDUCE) {
+        const double inv = inv_dt_hyp64<PLANE, WACT>(u, G, q);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(inv);
+        red = b > red ? b : red;
+        if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
+      } else {
+        double y;
+        cons_to_prim64<PLANE, WACT>(u, G.gm1, q, y);
+      }
+      if (qout.f[0]) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          if (WACT || v != 3) qout.f[v][o] = q[v];
+      }
     }
   }
   if (REDUCE) block_max_atomic(red, &ctrl->slot[slot], s_red);
+  // the copy is complete once this launch is (the next reader is a later kernel)
+  if (q_valid && threadIdx.x == 0) *q_valid = 1;
 }
 
 // consToPrim (States.h:34-45); src and dst may alias.
@@ -237,22 +252,25 @@ cudaError_t launch_prim_to_cons2d(const Grid& G, Fields u, cudaStream_t st) {
 }
 
 template <int PLANE, bool WACT>
-cudaError_t launch_p2c_from(const Grid& G, Fields src, Fields dst, StepCtrl* ctrl, int slot, cudaStream_t st) {
+cudaError_t launch_p2c_from(const Grid& G, Fields src, Fields dst, StepCtrl* ctrl, int slot, const Fields& qout,
+                            int* q_valid, cudaStream_t st) {
   const int grid = grid_for((long long)G.na * G.rows, 256);
   if (ctrl)
-    prim_to_cons_from<PLANE, WACT, true><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot);
+    prim_to_cons_from<PLANE, WACT, true><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot, qout, q_valid);
   else
-    prim_to_cons_from<PLANE, WACT, false><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot);
+    prim_to_cons_from<PLANE, WACT, false><<<grid, 256, 0, st>>>(G, src, dst, ctrl, slot, qout, q_valid);
   return cudaGetLastError();
 }
 
 cudaError_t launch_prim_to_cons_from(const Grid& G, bool wact, Fields src, Fields dst, StepCtrl* ctrl, int slot,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, const Fields* qout, int* q_valid) {
+  const Fields q = qout ? *qout : Fields{};
+  int* qv = qout ? q_valid : nullptr;
   if (G.plane == PLANE_XY)
-    return wact ? launch_p2c_from<PLANE_XY, true>(G, src, dst, ctrl, slot, st)
-                : launch_p2c_from<PLANE_XY, false>(G, src, dst, ctrl, slot, st);
-  return wact ? launch_p2c_from<PLANE_XZ, true>(G, src, dst, ctrl, slot, st)
-              : launch_p2c_from<PLANE_XZ, false>(G, src, dst, ctrl, slot, st);
+    return wact ? launch_p2c_from<PLANE_XY, true>(G, src, dst, ctrl, slot, q, qv, st)
+                : launch_p2c_from<PLANE_XY, false>(G, src, dst, ctrl, slot, q, qv, st);
+  return wact ? launch_p2c_from<PLANE_XZ, true>(G, src, dst, ctrl, slot, q, qv, st)
+              : launch_p2c_from<PLANE_XZ, false>(G, src, dst, ctrl, slot, q, qv, st);
 }
 
 cudaError_t launch_cons_to_prim2d(const Grid& G, Fields src, Fields dst, cudaStream_t st) {

@@ -109,9 +109,10 @@ inline cudaError_t launch_stage(const Grid& G, int riemann_solver, int kind, boo
 // (unpadded rows of na values, storage order, a null field reads as 0) into
 // the padded conserved state dst; with ctrl, also the CFL maximum of
 // consToPrim of the result into ctrl->slot[slot] (ComputeDt.h:28-54, the
-// reference's dt after its set-up).
+// reference's dt after its set-up).  qout (optional): also the primitive
+// copy of dst (PrimCopy), with *q_valid set once it is written.
 cudaError_t launch_prim_to_cons_from(const Grid& G, bool wact, Fields src, Fields dst, StepCtrl* ctrl, int slot,
-                                     cudaStream_t stream);
+                                     cudaStream_t stream, const Fields* qout = nullptr, int* q_valid = nullptr);
 
 // Reduce max inv_dt_hyp of state u into ctrl->slot[slot] (caller zeroes it).
 cudaError_t launch_reduce2d(const Grid& G, bool wact, Fields u, StepCtrl* ctrl, int slot, cudaStream_t stream);
