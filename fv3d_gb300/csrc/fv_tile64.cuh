@@ -745,6 +745,9 @@ __device__ __forceinline__ void pass_on64(const Grid& G, const Fields& uin, cons
 // tin / mbar (optional, single-problem kernel): TMA descriptors of uin and
 // the CTA's mbarrier; full blocks whose halo lies inside the grid are then
 // staged by tensor copies (stage_rows_tma) and converted in place.
+// qin (optional): the primitive copy of uin; the halo is then read (or
+// staged, tin then describing qin) from it and only the temperature is
+// computed.  qout (optional): receives the primitives of uout (update64).
 template <int PLANE, bool WACT, class TL, bool P2>
 __device__ __forceinline__ void stage_segment64(const Grid& G, const Fields& uin, const Fields& u0,
                                                 const Fields& uout, StepCtrl* ctrl, int rs, int kind, double dt,
