@@ -106,6 +106,26 @@ int Fail(fv_batch* b, int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return Fail((b), FV_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// Device allocations of one scope, freed when it ends (early returns
+// included; cudaFree waits for the work that may still use them).
+struct ScopedDevice {
+  std::vector<void*> ptrs;
+  ScopedDevice() = default;
+  ScopedDevice(const ScopedDevice&) = delete;
+  ScopedDevice& operator=(const ScopedDevice&) = delete;
+  ~ScopedDevice() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t bytes) {
+    void* q = nullptr;
+    const cudaError_t e = cudaMalloc(&q, bytes);
+    *p = e == cudaSuccess ? static_cast<T*>(q) : nullptr;
+    if (e == cudaSuccess) ptrs.push_back(q);
+    return e;
+  }
+};
+
 void StorageOrder(int plane, int slot_of[5]) {
   slot_of[0] = 0;
   slot_of[1] = 1;
@@ -311,9 +331,10 @@ int Autotune(fv_batch* b, Group& g) {
   BatchInst* tune_inst = nullptr;
   unsigned* tune_queue = nullptr;
   const size_t nm = g.members.size();
-  BCUDA(b, cudaMalloc(&tune_ctrl, sizeof(StepCtrl) * b->n));
-  BCUDA(b, cudaMalloc(&tune_inst, sizeof(BatchInst) * nm * cand.size()));
-  BCUDA(b, cudaMalloc(&tune_queue, 2 * sizeof(unsigned)));
+  ScopedDevice scratch;
+  BCUDA(b, scratch.alloc(&tune_ctrl, sizeof(StepCtrl) * b->n));
+  BCUDA(b, scratch.alloc(&tune_inst, sizeof(BatchInst) * nm * cand.size()));
+  BCUDA(b, scratch.alloc(&tune_queue, 2 * sizeof(unsigned)));
   std::vector<StepCtrl> hc(b->n);
   for (int i = 0; i < b->n; ++i) {
     std::memset(&hc[i], 0, sizeof(StepCtrl));
@@ -414,9 +435,6 @@ int Autotune(fv_batch* b, Group& g) {
   if (backup) cudaFree(backup);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(tune_ctrl);
-  cudaFree(tune_inst);
-  cudaFree(tune_queue);
   if (best_c < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
   std::lock_guard<std::mutex> lock(g_cache_mutex);
   g_cache[key] = {shapes[g.shape].tx, g.rows};
