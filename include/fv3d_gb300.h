@@ -124,7 +124,10 @@ typedef struct fv_sim fv_sim;
  * runs the problem in the FP32-mixed form through the batch machinery (a
  * batch of one): every call below works except set_cons / get_cons and
  * per-kernel profiling (FV_ERR_UNSUPPORTED).  FV_ERR_UNSUPPORTED names
- * settings this build does not run (see fvgpu_last_error). */
+ * settings this build does not run (see fvgpu_last_error).  FP64 device
+ * memory: 3 states of 5 fields (U^n, U*, scratch), plus a primitive copy
+ * of U^n with RK2 time stepping; a state is 5 fields of pitch x rows
+ * doubles (pitch: Nx rounded up to 16; each field rounded up to 256 bytes). */
 int fvgpu_create(const fv_params* params, fv_sim** out);
 int fvgpu_destroy(fv_sim* sim);
 /* Message for the last failing call on this handle ("" if none). */
