@@ -64,9 +64,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def problem():
+def problem(parse=None):
     from fv3d_gb300 import problems
-    return problems.rayleigh_taylor(512, 1536)
+    return problems.rayleigh_taylor(512, 1536, parse=parse)
 
 
 def config_dict(pr, l2):
@@ -153,8 +153,9 @@ def run_reference(args):
     world, rank, _ = dist_info()
     if rank != 0:
         return 0
-    pr = problem()
     from oracle import pyoracle
+    # the oracle's own readInifile: this arm loads no library of the GPU path
+    pr = problem(parse=pyoracle.parse_ini)
     threads = os.cpu_count() or 1
     pyoracle.set_threads(threads)
     kind = "port"

@@ -1,5 +1,5 @@
-// fv_noalloc.cu -- fvgpu_step_noalloc: one time step of a 2-D problem on
-// device arrays the caller owns, without allocating any memory.
+// fv_noalloc.cu -- fvgpu_step_noalloc: one time step of a 2-D or 3-D
+// problem on device arrays the caller owns, without allocating any memory.
 //
 // Why it exists: some host codes cannot call cudaMalloc from their time loop.
 // An application whose device memory belongs to another allocator (a memory
@@ -16,16 +16,28 @@
 //     x 8 bytes plus 256 bytes of control block must fit, e.g. 786,432 cells
 //     (512 x 1536) at pitch 512.  Larger problems are rejected with
 //     FV_ERR_PARAM and a message; they need the regular handle.
-//   - The array exists once per device and stays allocated by the CUDA
-//     runtime until the process exits, on every device where this entry point
-//     has been called.
+//   - The array exists once per device and stays allocated until the process
+//     exits.  With lazy module loading (CUDA_MODULE_LOADING=LAZY, the default
+//     since CUDA 12.2) it is reserved on a device when this file's kernels are
+//     first used there; with CUDA_MODULE_LOADING=EAGER every process that
+//     loads the library reserves the 32 MiB on each device where it creates a
+//     context, whether it calls this entry point or not.
 //   - Every call uses the same array and leaves the last call's contents in
 //     it; calls whose work overlaps on the GPU (other streams, other host
 //     threads) race on it.  The control block is rewritten at the start of
-//     every call; U* is fully written by the first stage before it is read.
+//     every call except its error flag; U* is fully written by the first
+//     stage before it is read.
+//   - Errors: the error flag (non-finite state, a bounded wait that gave up)
+//     is sticky across calls and is read -- then cleared -- only by a call
+//     that passes next_dt, which waits for the stream.  A call without
+//     next_dt returns once its work is enqueued and reports launch errors
+//     only.
 //   - The first call on a device looks the array's device address up
 //     (cudaGetSymbolAddress, once per device, with that device current); make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  A call with next_dt
+//     synchronises its stream and is refused while that stream is capturing.
+#include <cmath>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -54,11 +66,16 @@ static __device__ __align__(256) unsigned char g_step_scratch[kScratchBytes];
 
 std::mutex g_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
+bool g_fresh[kMaxDevices] = {};  // the next call on the device is its first
 
-// Writes a fresh control block (all counters, slots and flags zero).
-__global__ void init_ctrl_kernel(fv::StepCtrl* ctrl, double cfl, double inv_tc, double inv_visc, double eps) {
+// Writes a fresh control block (all counters, slots and flags zero), except
+// the sticky error flag, which is kept unless `first` (the device's first
+// call: nothing has written the block yet).
+__global__ void init_ctrl_kernel(fv::StepCtrl* ctrl, double cfl, double inv_tc, double inv_visc, double eps,
+                                 int first) {
   fv::StepCtrl c;
   memset(&c, 0, sizeof(c));
+  c.err = first ? 0 : ctrl->err;
   c.cfl = cfl;
   c.inv_tc = inv_tc;
   c.inv_visc = inv_visc;
@@ -78,8 +95,9 @@ int Message(char* buf, size_t len, int code, const char* fmt, ...) {
 }
 
 // Device address of the scratch array on the current device (set up on the
-// first call per device).
-cudaError_t ScratchAddress(void** out) {
+// first call per device).  *dev_out: the device; *first: no call has yet
+// initialised its control block (MarkInitialised clears it).
+cudaError_t ScratchAddress(void** out, bool* first, int* dev_out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -90,9 +108,17 @@ cudaError_t ScratchAddress(void** out) {
     e = cudaGetSymbolAddress(&ptr, g_step_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = ptr;
+    g_fresh[dev] = true;
   }
   *out = g_scratch_addr[dev];
+  *first = g_fresh[dev];
+  *dev_out = dev;
   return cudaSuccess;
+}
+
+void MarkInitialised(int dev) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  g_fresh[dev] = false;
 }
 
 }  // namespace
@@ -104,6 +130,9 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
   using fv::StepCtrl;
   if (errbuf && errlen) errbuf[0] = '\0';
   if (!params || !fields) return Message(errbuf, errlen, FV_ERR_PARAM, "null params or fields");
+  if (!(dt > 0.0) || !std::isfinite(dt))
+    return Message(errbuf, errlen, FV_ERR_PARAM, "dt must be positive and finite (got %g): this call has no CFL dt",
+                   dt);
   Grid G;
   double inv_tc = 0.0, inv_visc = 0.0;
   int deg_bc = 0;
@@ -111,6 +140,13 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
   int rc = fv::configure_grid(*params, &G, &inv_tc, &inv_visc, &deg_bc, &err);
   if (rc != FV_OK) return Message(errbuf, errlen, rc, "%s", err.c_str());
   if (pitch < G.na) return Message(errbuf, errlen, FV_ERR_PARAM, "pitch %ld < Nx %d", pitch, G.na);
+  // bound pitch before any product with rows can overflow
+  const long max_pitch = (long)((kScratchBytes - kCtrlBytes) / (5 * sizeof(double)) / (size_t)G.rows);
+  if (pitch > INT_MAX || pitch > max_pitch)
+    return Message(errbuf, errlen, FV_ERR_PARAM,
+                   "pitch %ld x %d rows does not fit the fixed %zu-byte step scratch (at most pitch %ld); use "
+                   "fvgpu_create for larger problems",
+                   pitch, G.rows, kScratchBytes, max_pitch);
   const int plane = G.plane;
   // reference order (rho, rho u, rho v, rho w, E) -> storage order (rho, m_a, m_b, m_c, E)
   const int slot_of[5] = {0, 1, plane == fv::PLANE_XY ? 2 : 3, plane == fv::PLANE_XY ? 3 : 2, 4};
@@ -146,19 +182,31 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
                    "rows x 8 B + %zu); use fvgpu_create for larger problems",
                    need, kScratchBytes, pitch, G.rows, kCtrlBytes);
 
+  cudaStream_t st = (cudaStream_t)stream;
+  if (next_dt) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &cs);
+    if (ce != cudaSuccess)
+      return Message(errbuf, errlen, FV_ERR_CUDA, "stream query failed: %s", cudaGetErrorString(ce));
+    if (cs != cudaStreamCaptureStatusNone)
+      return Message(errbuf, errlen, FV_ERR_PARAM, "next_dt must be NULL while the stream is being captured");
+  }
+
   void* base = nullptr;
-  cudaError_t e = ScratchAddress(&base);
+  bool first = false;
+  int dev = 0;
+  cudaError_t e = ScratchAddress(&base, &first, &dev);
   if (e != cudaSuccess)
     return Message(errbuf, errlen, FV_ERR_CUDA, "scratch address lookup failed: %s", cudaGetErrorString(e));
   StepCtrl* ctrl = (StepCtrl*)base;
   double* ustar = (double*)((unsigned char*)base + kCtrlBytes);
   Fields B;
   for (int v = 0; v < 5; ++v) B.f[v] = ustar + (size_t)v * (size_t)G.fstride;
-  cudaStream_t st = (cudaStream_t)stream;
 
-  // control block: fresh every call (nothing of a previous call is reused)
-  init_ctrl_kernel<<<1, 1, 0, st>>>(ctrl, params->CFL, inv_tc, inv_visc, params->epsilon);
+  // control block: fresh every call but for the sticky error flag
+  init_ctrl_kernel<<<1, 1, 0, st>>>(ctrl, params->CFL, inv_tc, inv_visc, params->epsilon, first ? 1 : 0);
   e = cudaGetLastError();
+  if (e == cudaSuccess && first) MarkInitialised(dev);
   if (e == cudaSuccess) e = fv::launch_control(ctrl, 1, 0, dt, st);
   const int rs = params->riemann_solver == FV_HLL ? 0 : 1;
   if (params->time_stepping == FV_TS_RK2) {
@@ -179,6 +227,7 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
     int errflag = 0;
     e = cudaMemcpyAsync(&bits, &ctrl->slot[1], sizeof(bits), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&errflag, &ctrl->err, sizeof(errflag), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&ctrl->err, 0, sizeof(int), st);  // reported: clear
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return Message(errbuf, errlen, FV_ERR_CUDA, "readback failed: %s", cudaGetErrorString(e));
     double inv_hyp;
@@ -187,8 +236,11 @@ extern "C" int fvgpu_step_noalloc(const fv_params* params, double* const fields[
     if (inv_tc > m) m = inv_tc;
     if (inv_visc > m) m = inv_visc;
     *next_dt = params->CFL / m;
+    if (errflag & 2)
+      return Message(errbuf, errlen, FV_ERR_TIMEOUT, "a bounded device wait gave up since the last check");
     if (errflag || !(*next_dt > 0.0 && *next_dt <= 1.0e300))
-      return Message(errbuf, errlen, FV_ERR_NONFINITE, "non-finite state or dt after the step (dt = %g)", *next_dt);
+      return Message(errbuf, errlen, FV_ERR_NONFINITE,
+                     "non-finite state since the last check, or non-finite dt after the step (dt = %g)", *next_dt);
   }
   return FV_OK;
 }

@@ -85,7 +85,11 @@ def ini_text(sections):
     return "\n".join(out)
 
 
-def _parse(ini):
+def _parse(ini, parse=None):
+    """Params of the .ini text: the library's readInifile by default, or
+    the callable `parse` (text -> FvParams) a caller supplies."""
+    if parse is not None:
+        return parse(ini)
     from fv3d_gb300 import parse_ini
     return parse_ini(ini)
 
@@ -127,10 +131,11 @@ def sedov(n=256, gamma=1.4, tend=0.1, cfl=0.8, riemann="hllc", extra=None, name=
 
 
 def rayleigh_taylor(nx=512, nz=1536, g=-0.1, ratio=2.0, tend=5.0, kappa=0.0, mu=0.0, seed=MASTER_SEED,
-                    riemann="hll", name="rayleigh_taylor"):
+                    riemann="hll", name="rayleigh_taylor", parse=None):
     """Two layers in the x-z plane: rho = ratio above z = 0.75, 1 below,
     hydrostatic p = 2.5 + g rho (z - 0.75), w perturbed by
-    0.01 (1 + cos 4 pi x)(1 + cos(3 pi z / 1.5))/4 plus uniform noise 1e-4."""
+    0.01 (1 + cos 4 pi x)(1 + cos(3 pi z / 1.5))/4 plus uniform noise 1e-4.
+    `parse` (optional): the .ini parser to use (see _parse)."""
     sec = {
         "mesh": _mesh(nx, 1, nz, xr=(0.0, 0.5), zr=(0.0, 1.5)),
         "run": {"tend": tend, "boundaries_x": "periodic", "boundaries_y": "periodic",
@@ -143,7 +148,7 @@ def rayleigh_taylor(nx=512, nz=1536, g=-0.1, ratio=2.0, tend=5.0, kappa=0.0, mu=
     if mu:
         sec["viscosity"] = {"active": True, "mu": repr(float(mu))}
     ini = ini_text(sec)
-    p = _parse(ini)
+    p = _parse(ini, parse)
     X, _, Z = _centres(p)
     rho = np.where(Z > 0.75, ratio, 1.0)
     prs = 2.5 + p.g * rho * (Z - 0.75)

@@ -194,7 +194,10 @@ int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
  * reserved the GPU) and latency-critical loops that cannot take the device
  * synchronisation of cudaMalloc/cudaFree.  The stage scratch (U* and the
  * dt/reduction control block) is one fixed 32 MiB array per device, held
- * until the process exits once the call has been used on that device.
+ * until the process exits.  Under lazy module loading (the CUDA default
+ * since 12.2) a device holds it once the call has been used there; with
+ * CUDA_MODULE_LOADING=EAGER every process that loads this library holds it
+ * on each device where it creates a context.
  *   fields  device pointers to rho, rho*u, rho*v, rho*w, E of the interior
  *           cells, rows of Nx cells along x with a stride of `pitch`
  *           doubles, rows following y (Nz == 1), z (Ny == 1) or, for a
@@ -205,9 +208,16 @@ int fvgpu_kernel_times(fv_sim* sim, long counts[3], double ms[3]);
  *   pitch   row stride in doubles (>= Nx).  5 x pitch x rows x 8 bytes
  *           + 256 must fit in 32 MiB (e.g. 512 x 1536 at pitch 512); larger
  *           problems get FV_ERR_PARAM and a message -- use fvgpu_create.
- *   next_dt if non-NULL, receives the CFL dt of the updated state (this
- *           synchronises the stream); otherwise the call returns after
- *           enqueueing its work on `stream` (NULL: the legacy default stream).
+ *   dt      the step, > 0 and finite (FV_ERR_PARAM otherwise): unlike
+ *           fvgpu_step there is no CFL fallback for dt <= 0.
+ *   next_dt if non-NULL, receives the CFL dt of the updated state; the call
+ *           then waits for the stream (so it is refused, FV_ERR_PARAM, while
+ *           the stream is being captured) and reports FV_ERR_NONFINITE /
+ *           FV_ERR_TIMEOUT for this call or any call since the last one that
+ *           passed next_dt (the device-side error flag is sticky until such
+ *           a call reads and clears it).  With next_dt NULL the call returns
+ *           after enqueueing its work on `stream` (NULL: the legacy default
+ *           stream) and reports launch errors only.
  *   errbuf  optional buffer for a message when the status is not FV_OK.
  * All calls share the scratch and leave its last contents there: calls whose
  * work overlaps on the GPU race.  The first call on each device looks up the

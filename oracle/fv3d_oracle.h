@@ -33,6 +33,8 @@ int fvora_advance(fvora_sim* s, double tend, long max_steps, double* t, long* ns
 int fvora_riemann(int solver, double gamma0, long n, const double* qL, const double* qR, double* flux,
                   double* pout);
 int fvora_set_threads(int nthreads);
+/* readInifile (SimInfo.h:169-306) on .ini text: fv3d_ini.c. */
+int fvora_parse_ini(const char* text, fv_params* out);
 
 #ifdef __cplusplus
 }

@@ -46,6 +46,8 @@ def load_oracle():
         lib.fvora_riemann.argtypes = [C.c_int, C.c_double, C.c_long, _dp, _dp, _dp, _dp]
         lib.fvora_set_threads.argtypes = [C.c_int]
         lib.fvora_set_threads.restype = C.c_int
+        lib.fvora_parse_ini.argtypes = [C.c_char_p, C.POINTER(FvParams)]
+        lib.fvora_parse_ini.restype = C.c_int
         _lib_oracle = lib
     return _lib_oracle
 
@@ -198,6 +200,16 @@ class RefOracle(_Base):
         n = C.c_long(0)
         self.lib.fvref_advance(self._h, float(tend), int(max_steps), C.byref(tt), C.byref(n))
         return tt.value, n.value
+
+
+def parse_ini(text):
+    """readInifile (SimInfo.h:169-306) on .ini text, by the oracle's own
+    restatement (fv3d_ini.c): Params without the GPU library."""
+    p = FvParams()
+    rc = load_oracle().fvora_parse_ini(text.encode(), C.byref(p))
+    if rc:
+        raise ValueError("fvora_parse_ini failed: %d" % rc)
+    return p
 
 
 def ref_read_ini(path):

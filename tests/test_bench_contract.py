@@ -32,6 +32,17 @@ def test_reference_arm_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
+def test_reference_arm_loads_no_gpu_library():
+    """The reference arm parses its .ini with the oracle's readInifile and
+    steps the oracle: no library of the GPU path enters its process."""
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3'];"
+            "bench.main(); maps = open('/proc/self/maps').read();"
+            "print('LOADED_GB300' if 'libfv3d_gb300' in maps else 'CLEAN')")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1] == "CLEAN", r.stdout[-2000:]
+
+
 @pytest.mark.gpu
 def test_gb300_arm_line():
     d = _run(["--steps", "3", "--warmup", "3", "--no-variants"], 900)

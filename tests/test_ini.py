@@ -31,6 +31,18 @@ def test_parse_matches_reference_params(name):
         assert got[k] == v, (k, got[k], v)
 
 
+@pytest.mark.parametrize("name", [c["name"] for c in golden_cases()])
+def test_oracle_parse_matches_reference_params(name):
+    """The oracle's own readInifile restatement (what the CPU reference arm of
+    the benchmark parses with) gives the reference's Params too."""
+    case = load_case(name)
+    got = pyoracle.parse_ini(case["ini"]).as_dict()
+    for k, v in case["params"].items():
+        if k.startswith("b02_"):
+            continue
+        assert got[k] == v, (k, got[k], v)
+
+
 EDGE = {
     "defaults": ("", dict(Nx=32, Ny=32, Nz=32, Ng=2, CFL=F32(0.8), gamma0=F32(5.0 / 3.0), tend=1.0,
                           boundary_x=fv._abi.FV_BC_REFLECTING, reconstruction=fv._abi.FV_PCM,
@@ -70,6 +82,17 @@ def test_ini_edge_cases(case):
         assert got[k] == v, (k, got[k], v)
 
 
+@pytest.mark.parametrize("case", sorted(EDGE))
+def test_oracle_ini_edge_cases(case):
+    text, want = EDGE[case]
+    got = pyoracle.parse_ini(text).as_dict()
+    prod = fv.parse_ini(text).as_dict()
+    for k, v in want.items():
+        if v is not None:
+            assert got[k] == v, (k, got[k], v)
+    assert got == prod
+
+
 @pytest.mark.skipif(not pyoracle.reference_available(), reason="reference sources absent")
 @pytest.mark.parametrize("case", sorted(EDGE))
 def test_ini_edge_cases_against_reference(case):
@@ -79,10 +102,12 @@ def test_ini_edge_cases_against_reference(case):
         f.write(text)
     ref = pyoracle.ref_read_ini(path).as_dict()
     got = fv.read_ini(path).as_dict()
+    ora = pyoracle.parse_ini(text).as_dict()
     for k, v in ref.items():
         if k.startswith("b02_") or k == "precision":
             continue
         assert got[k] == v, (k, got[k], v)
+        assert ora[k] == v, (k, ora[k], v)
 
 
 def test_reference_settings_files_parse():

@@ -46,7 +46,24 @@ def _to_host(arrs, shape):
     return [np.zeros(shape) if t is None else t[:, :nx].cpu().numpy().reshape(shape) for t in arrs]
 
 
-@pytest.mark.parametrize("case", ["rt_xz_null_v", "thermal_xy_visc", "blast_3d_euler"])
+def _sod_euler_null_w():
+    pr = problems.sod(96, "y", nx_other=40)
+    text = pr.ini.replace("time_stepping=RK2", "time_stepping=euler")
+    pr.params = fv.parse_ini(text)
+    return pr
+
+
+def _random_3d_rk2():
+    return problems.random_problem(
+        "r3", problems._mesh(20, 18, 16),
+        {"tend": 1.0, "boundaries_x": "periodic", "boundaries_y": "absorbing", "boundaries_z": "reflecting"},
+        {"riemann_solver": "hllc", "reconstruction": "plm", "time_stepping": "RK2", "CFL": 0.5},
+        {"gamma0": 1.4}, seed=4242, wmag=0.7,
+        extra={"thermal_conduction": {"active": True, "kappa": 1e-3}, "viscosity": {"active": True, "mu": 1e-3}})
+
+
+@pytest.mark.parametrize("case", ["rt_xz_null_v", "thermal_xy_visc", "blast_3d_euler", "sod_xy_euler_null_w",
+                                  "random_3d_rk2"])
 def test_noalloc_matches_handle_two_calls(case):
     torch = pytest.importorskip("torch")
     if case == "rt_xz_null_v":
@@ -54,6 +71,12 @@ def test_noalloc_matches_handle_two_calls(case):
         skip = 2          # rho*v: zero in the x-z plane without viscosity
     elif case == "blast_3d_euler":
         pr = problems.blast(24, nz=20)  # 3-D kernel, Euler stepping (copies U* back)
+        skip = -1
+    elif case == "sod_xy_euler_null_w":
+        pr = _sod_euler_null_w()        # 2-D Euler: copy-back without the third momentum
+        skip = 3
+    elif case == "random_3d_rk2":
+        pr = _random_3d_rk2()           # 3-D RK2: stage 2 writes into the caller's arrays
         skip = -1
     else:
         pr = problems.thermal_pulse(96)
@@ -100,3 +123,55 @@ def test_noalloc_rejects_problems_beyond_its_scratch():
     rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs, 2048, 1e-3, None, None, err, 512)
     assert rc == 1
     assert b"scratch" in err.value and b"fvgpu_create" in err.value
+
+
+def test_noalloc_refuses_bad_dt_and_huge_pitch():
+    """dt must be positive and finite (no CFL fallback here), and a pitch
+    whose product with the row count would overflow is refused before any
+    size arithmetic."""
+    lib = fv.load_library()
+    params = fv.parse_ini("[mesh]\nNx=64\nNy=64\nNz=1\n[run]\nboundaries_z=periodic\n"
+                          "[solvers]\ntime_stepping=RK2\nreconstruction=plm\n")
+    ptrs = (C.c_void_p * 5)(1, 1, 1, None, 1)  # never dereferenced: rejected first
+    err = C.create_string_buffer(512)
+    for dt in (0.0, -1e-3, float("nan"), float("inf")):
+        assert lib.fvgpu_step_noalloc(C.byref(params), ptrs, 64, dt, None, None, err, 512) == 1
+        assert b"dt" in err.value
+    for pitch in (1 << 40, (1 << 31) + 5, 200000):
+        assert lib.fvgpu_step_noalloc(C.byref(params), ptrs, pitch, 1e-3, None, None, err, 512) == 1
+        assert b"pitch" in err.value
+
+
+def test_noalloc_error_flag_is_sticky_until_read():
+    """A non-finite state met by a call without next_dt is reported by the
+    next call that passes next_dt, which clears the flag: a clean call after
+    it reports FV_OK and matches the handle bit for bit."""
+    torch = pytest.importorskip("torch")
+    lib = fv.load_library()
+    pr = problems.sedov(48)
+    sim = fv.Simulation(pr.params)
+    sim.set_prim(*pr.prim)
+    dt = sim.compute_dt()
+    good = sim.get_cons()
+    shape = sim.shape
+    params = pr.params.copy()
+    err = C.create_string_buffer(512)
+    next_dt = C.c_double()
+    bad = [a.copy() for a in good]
+    bad[4][0, 5, 7] = -1.0  # negative energy, so negative pressure: NaN sound speed
+    arrs1, ptrs1 = _device_state(torch, bad, shape[2], 3)
+    rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs1, shape[2], dt, None, None, err, 512)
+    assert rc == 0, err.value           # asynchronous: nothing checked yet
+    torch.cuda.synchronize()
+    arrs2, ptrs2 = _device_state(torch, good, shape[2], 3)
+    rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs2, shape[2], dt, C.byref(next_dt), None, err, 512)
+    assert rc == 4, (rc, err.value)     # the earlier call's non-finite state
+    arrs3, ptrs3 = _device_state(torch, good, shape[2], 3)
+    rc = lib.fvgpu_step_noalloc(C.byref(params), ptrs3, shape[2], dt, C.byref(next_dt), None, err, 512)
+    assert rc == 0, (rc, err.value)     # cleared once reported
+    sim.step(dt)
+    want = sim.get_cons()
+    got = _to_host(arrs3, shape)
+    for k in (0, 1, 2, 4):
+        np.testing.assert_array_equal(got[k], want[k])
+    sim.close()
