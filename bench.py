@@ -520,6 +520,75 @@ def run_variants(torch, args, flush):
     return out
 
 
+def _single_pair(pr, nsteps=0):
+    """The FP64 handle and the FP32-mixed handle on one problem: advanced to
+    its tend (the main.cpp loop) or for nsteps fixed CFL steps."""
+    import fv3d_gb300 as fv
+    out = {}
+    for key, params in (("fp64", pr.params), ("mixed", _mixed(pr.params))):
+        sim = fv.Simulation(params)
+        sim.set_prim(*pr.prim)
+        t0 = time.perf_counter()
+        t, n = sim.advance(1.0e30 if nsteps else pr.params.tend, max_steps=nsteps)
+        out[key] = (sim.get_prim(), t, n, time.perf_counter() - t0)
+        sim.close()
+    return out
+
+
+def accuracy_entry(prim0, gamma, runs):
+    """Per-field relative L1 of the mixed result against the FP64 result, and
+    the relative mass / energy drift of both."""
+    (a, ta, na, wa), (m, tm, nm, wm) = runs["fp64"], runs["mixed"]
+    m0, e0 = _mass_energy(prim0, gamma)
+    drift = {}
+    for key, st in (("fp64", a), ("mixed", m)):
+        m1, e1 = _mass_energy(st, gamma)
+        drift[key] = {"mass": abs(m1 - m0) / abs(m0), "energy": abs(e1 - e0) / abs(e0)}
+    l1 = [_rel_l1(x, y) for x, y in zip(m, a)]
+    return {"rel_l1": dict(zip(["rho", "u", "v", "w", "p"], l1)), "steps": {"fp64": na, "mixed": nm},
+            "t_end": {"fp64": ta, "mixed": tm}, "rel_drift": drift, "wall_s": {"fp64": wa, "mixed": wm}}
+
+
+def run_accuracy(args):
+    """The FP32-mixed form against the bit-exact FP64 form at every
+    configuration's stated horizon (not timed): Sedov 256^2 to t = 0.1,
+    Rayleigh-Taylor 512x1536 to t = 5, the thermal pulse 1024^2 for 200 steps,
+    the shear layer 4096^2 to t = 1, the 512-instance batch for 200 steps and
+    the 64-instance Rayleigh-Taylor batch for 500 steps.  Prints one JSON
+    line: per configuration the per-field relative L1 (worst instance for
+    batches) and the mass / energy drift of both forms."""
+    import torch
+    from fv3d_gb300 import problems
+    torch.cuda.set_device(0)
+    only = set(args.accuracy_only.split(",")) if args.accuracy_only else None
+    out = {}
+
+    def want(name):
+        return only is None or name in only
+
+    singles = [("sedov_256_to_t0.1", lambda: problems.sedov(256), 0),
+               ("rayleigh_taylor_512x1536_to_t5", problem, 0),
+               ("thermal_pulse_1024_200_steps", lambda: problems.thermal_pulse(1024), 200),
+               ("shear_layer_4096_to_t1", lambda: problems.shear_layer(4096), 0)]
+    for name, build, nsteps in singles:
+        if not want(name):
+            continue
+        pr = build()
+        out[name] = accuracy_entry(pr.prim, pr.params.gamma0, _single_pair(pr, nsteps))
+        print(name, json.dumps(out[name]), file=sys.stderr, flush=True)
+    for name, build, nsteps in (("batch512_sod_sedov_200_steps", lambda: problems.batch_sod_sedov(512), 200),
+                                ("batch64_rt_500_steps", lambda: problems.batch_rt(64), 500)):
+        if not want(name):
+            continue
+        probs = build()
+        t0 = time.perf_counter()
+        out[name] = l1_vs_fp64(torch, probs, nsteps, [_mixed(p.params) for p in probs])
+        out[name]["wall_s"] = time.perf_counter() - t0
+        print(name, json.dumps(out[name]), file=sys.stderr, flush=True)
+    print(json.dumps({"accuracy": out, "metric": "relative L1 of FP32-mixed vs bit-exact FP64, per field"}))
+    return 0
+
+
 def run_profile_case(args):
     """Only a workload's steps (warm-up + steps), for launch lists and ncu
     captures: no timing, no CPU baseline, no e2e.  Cases: fp64_rt (the bench
@@ -573,11 +642,17 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other configurations (mixed, batched, shear layer)")
     ap.add_argument("--rt-batch-l1-steps", type=int, default=50,
-                    help="steps of the 64-instance Rayleigh-Taylor batch compared with FP64 (the "
-                         "configuration asks for 500)")
+                    help="steps of the 64-instance Rayleigh-Taylor batch compared with FP64 in the timed "
+                         "run's variants (--accuracy runs the configuration's 500)")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="no timing: the mixed form against FP64 at every configuration's stated horizon "
+                         "(about 20 minutes on one GB300)")
+    ap.add_argument("--accuracy-only", default=None, help="comma-separated subset of the --accuracy cases")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.accuracy:
+        return run_accuracy(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -1,7 +1,8 @@
 // fv_batch32.cu -- FP32-mixed persistent stage kernel for batches, plus the
 // mixed form's CFL reduction and its (hi, lo) pair conversions.  Built with
-// fast-math (FP32 division / sqrt approximations, FMA contraction), the pair
-// arithmetic of fv_tile32.cuh being written with adds only.
+// fast-math (FP32 division / sqrt approximations, FMA contraction); the
+// error-free pair arithmetic of fv_tile32.cuh is written with adds and _rn
+// intrinsics, which contraction leaves alone.
 #include "fv_tile32.cuh"
 
 namespace fv {
@@ -148,18 +149,11 @@ __global__ void __launch_bounds__(256) reduce2d_mixed(const Grid G, const Fields
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(c / G.na), x = (int)(c - (long long)y * G.na);
     const long long o = (long long)y * G.pitch + x;
-    float u[5], e_lo = 0.0f;
+    float2 w[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      if (v == 3 && !WACT) {
-        u[v] = 0.0f;
-        continue;
-      }
-      const float2 w = reinterpret_cast<const float2*>(pairs.f[v])[o];
-      u[v] = v == 4 ? w.x : w.x + w.y;
-      if (v == 4) e_lo = w.y;
-    }
-    const float inv = inv_dt_hyp32<PLANE, WACT>(u, e_lo, G);
+    for (int v = 0; v < 5; ++v)
+      w[v] = (v == 3 && !WACT) ? make_float2(0.0f, 0.0f) : reinterpret_cast<const float2*>(pairs.f[v])[o];
+    const float inv = inv_dt_hyp32<PLANE, WACT>(w, G);
     bad |= !(inv <= 3.0e38f);
     red = fmaxf(red, inv);
   }

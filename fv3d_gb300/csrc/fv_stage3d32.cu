@@ -59,31 +59,26 @@ __device__ __forceinline__ void column_of(int tid, int& cx, int& cy) {
 
 __device__ __forceinline__ int slot_of(int kg) { return (kg + 4) & 3; }
 
-// The stage input of one stored cell: pairs (U^n) or U* values.
+// The stage input of one stored cell: pairs (U^n) or U* values (internal
+// energy in the energy slot).
 struct MixedIn {
   const float2* const* pairs;  // src (STAGE_RK_1 / STAGE_EULER)
   const float* const* us;      // U* (STAGE_RK_2)
   bool in_pairs;
-  __device__ __forceinline__ void load(unsigned o, float u[5], float& e_lo) const {
-    if (in_pairs) {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const float2 w = pairs[v][o];
-        u[v] = v == 4 ? w.x : w.x + w.y;
-        if (v == 4) e_lo = w.y;
-      }
-    } else {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) u[v] = us[v][o];
-      e_lo = 0.0f;
-    }
-  }
 };
 
 __device__ __forceinline__ void load_prim32(const MixedIn& in, unsigned o, float gm1, float q[5]) {
-  float u[5], e_lo;
-  in.load(o, u, e_lo);
-  cons_to_prim32<PLANE_XY, true>(u, e_lo, gm1, q);
+  if (in.in_pairs) {
+    float2 w[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) w[v] = in.pairs[v][o];
+    cons_to_prim_pairs<PLANE_XY, true>(w, gm1, q);
+  } else {
+    float u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = in.us[v][o];
+    cons_to_prim_star<true>(u, gm1, q);
+  }
 }
 
 // fillC91 (BoundaryConditions.h:87-134) in FP32, as the FP64 kernel's.
@@ -350,9 +345,18 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         du[3] += dt * rho_c * G.g_f;
         du[4] += dt * 0.5f * (fL[0] + fR[0]) * G.g_f;
       }
-      float2 base[5];
+      float2 base[5];  // the stage input at this cell as pairs (U*: E* rebuilt, fv_tile32.cuh)
+      if (in.in_pairs) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) base[v] = in.in_pairs ? src[v][o] : make_float2(M.us[v][o], 0.0f);
+        for (int v = 0; v < 5; ++v) base[v] = src[v][o];
+      } else {
+        float u[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) u[v] = M.us[v][o];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) base[v] = make_float2(u[v], 0.0f);
+        base[4] = pair_add(kinetic_star<true>(u), u[4]);
+      }
       {  // density floor on the hydro update (Update.h:160)
         const float2 rho = pair_add(base[0], du[0]);
         if (rho.x + rho.y < 1.0e-6f) {
@@ -384,24 +388,27 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         for (int v = 1; v < 5; ++v) du[v] += (vf[0][v] + vf[1][v] + vf[2][v]) * dt;
       }
       if (kind == STAGE_RK_1) {
+        float us[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) M.us[v][o] = base[v].x + (base[v].y + du[v]);
+        for (int v = 0; v < 4; ++v) us[v] = base[v].x + (base[v].y + du[v]);
+        us[4] = internal_energy(pair_add(base[4], du[4]), kinetic_star<true>(us));
+#pragma unroll
+        for (int v = 0; v < 5; ++v) M.us[v][o] = us[v];
       } else {
-        float fin[5], e_lo = 0.0f;
+        float2 fin[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           float2 r;
           if (kind == STAGE_RK_2) {
-            r = pair_add(pair_add(M.un[v][o], base[v].x), du[v]);
+            r = pair_add(pair_add(M.un[v][o], base[v]), du[v]);
             r = make_float2(0.5f * r.x, 0.5f * r.y);
           } else {
             r = pair_add(base[v], du[v]);
           }
           dst[v][o] = r;
-          fin[v] = r.x;
-          if (v == 4) e_lo = r.y;
+          fin[v] = r;
         }
-        const float inv = inv_dt_hyp32<PLANE_XY, true>(fin, e_lo, G);
+        const float inv = inv_dt_hyp32<PLANE_XY, true>(fin, G);
         bad |= !(inv <= 3.0e38f);
         red = fmaxf(red, inv);
       }

@@ -5,15 +5,23 @@
 //   - U^n, the state carried from step to step, is an FP32 (hi, lo) pair per
 //     value (float2, 8 bytes): about 48 significant bits, so accumulating
 //     many small increments loses nothing measurable;
-//   - U*, the RK2 intermediate, is plain FP32 (4 bytes);
+//   - U*, the RK2 intermediate, is plain FP32 (4 bytes): density and momenta
+//     as conserved values, the energy slot holding the internal energy
+//     E* - |m*|^2 / (2 rho*) rather than E* (see below);
 //   - primitives, slopes, face states, the Riemann solvers, gravity, thermal
 //     conduction and viscosity run in FP32 (fast-math division and sqrt);
 //   - the RK2 combination 0.5*(U^n + U* + dU) and every update of U^n are
 //     done on the (hi, lo) pairs with error-free two-sums (Knuth's TwoSum,
 //     Dekker's Fast2Sum);
-//   - the pressure recovery p = (gamma-1)(E - Ek) subtracts Ek from the
-//     (hi, lo) pair of E, so the cancellation at high Mach loses only Ek's own
-//     FP32 rounding;
+//   - the pressure recovery p = (gamma-1)(E - |m|^2 / (2 rho)) (States.h:42-43)
+//     runs in double-float arithmetic: the kinetic energy is formed from the
+//     (hi, lo) pairs of density and momenta as an unevaluated pair (exact
+//     squares by FMA, a corrected quotient) and subtracted from E's pair, so
+//     at high Mach, where E and the kinetic energy nearly cancel, p keeps
+//     about 2^-24 relative accuracy (an FP32 kinetic energy would lose
+//     2^-24 of E, i.e. 2^-24 gamma (gamma-1) M^2 / 2 of p).  U* keeps its
+//     internal energy for the same reason: E* is rebuilt from it and the
+//     stored density and momenta in the same double-float arithmetic;
 //   - the CFL maximum is taken over FP32 cell values and turned into dt in
 //     FP64 by the control kernel; conservation sums run in FP64.
 // Per cell-update the state traffic is 8 (read U^n) + 4 (write U*) + 4 (read
@@ -67,29 +75,98 @@ __device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
   return fast_two_sum(s.x, s.y + (a.y + b.y));
 }
 
-// consToPrim (States.h:34-45) in FP32 from storage order; E carries its low
-// part so that E - Ek cancels exactly when Ek is close to E.
-template <int PLANE, bool WACT>
-__device__ __forceinline__ void cons_to_prim32(const float u[5], float e_lo, float gm1, float q[5]) {
-  const float r = u[0];
-  const float rinv = 1.0f / r;
-  const float va = u[1] * rinv, vb = u[2] * rinv, vc = WACT ? u[3] * rinv : 0.0f;
-  const float vx = va, vy = PLANE == PLANE_XY ? vb : vc, vz = PLANE == PLANE_XY ? vc : vb;
-  const float Ek = 0.5f * r * (vx * vx + vy * vy + vz * vz);
-  q[0] = r;
-  q[1] = va;
-  q[2] = vb;
-  q[3] = vc;
-  q[4] = ((u[4] - Ek) + e_lo) * gm1;
+// ---- double-float kinetic energy and pressure recovery -------------------
+// The products below use the _rn intrinsics, which the compiler never
+// contracts into FMAs: an error-free transformation needs each rounding
+// exactly where it is written (the files are built with FMA contraction).
+
+// Exact square of h as an unevaluated pair (p, e): p = RN(h*h), e = h*h - p.
+__device__ __forceinline__ float2 two_sq(float h) {
+  const float p = __fmul_rn(h, h);
+  return make_float2(p, __fmaf_rn(h, h, -p));
 }
 
+// |m|^2 / (2 rho) as an unevaluated pair, from pairs of the density and the
+// three momenta (storage order; mc ignored unless WACT).  Relative error
+// about 2^-44: sums of the exact squares by TwoSum, the cross terms 2 h l
+// and the product errors folded into the low part, then one quotient
+// corrected by its remainder (computed with FMAs).
+template <bool WACT>
+__device__ __forceinline__ float2 kinetic_pair(float2 r, float2 ma, float2 mb, float2 mc) {
+  const float2 a = two_sq(ma.x), b = two_sq(mb.x);
+  float2 s = two_sum(a.x, b.x);
+  float lo = s.y + (a.y + b.y);
+  lo = __fmaf_rn(2.0f * ma.x, ma.y, lo);
+  lo = __fmaf_rn(2.0f * mb.x, mb.y, lo);
+  if (WACT) {
+    const float2 c = two_sq(mc.x);
+    const float2 t = two_sum(s.x, c.x);
+    s.x = t.x;
+    lo = lo + t.y + c.y;
+    lo = __fmaf_rn(2.0f * mc.x, mc.y, lo);
+  }
+  const float rinv = 1.0f / r.x;  // approximate: the remainder corrects q1
+  const float q1 = __fmul_rn(s.x, rinv);
+  const float rem = __fadd_rn(__fmaf_rn(-q1, r.x, s.x), __fmaf_rn(-q1, r.y, lo));
+  const float q2 = __fmul_rn(rem, rinv);
+  return make_float2(0.5f * q1, 0.5f * q2);
+}
+
+// E - Ek for an energy pair and a kinetic-energy pair: E.x - k.x is exact
+// where they cancel (Sterbenz), so the result keeps 2^-24 of itself.
+__device__ __forceinline__ float internal_energy(float2 E, float2 k) {
+  return __fadd_rn(__fsub_rn(E.x, k.x), __fsub_rn(E.y, k.y));
+}
+
+// consToPrim (States.h:34-45) of a cell held as (hi, lo) pairs (U^n), storage
+// order: velocities in FP32 from the rounded values, p from the double-float
+// internal energy.
 template <int PLANE, bool WACT>
-__device__ __forceinline__ float inv_dt_hyp32(const float u[5], float e_lo, const Grid& G) {
-  float q[5];
-  cons_to_prim32<PLANE, WACT>(u, e_lo, G.gm1_f, q);
+__device__ __forceinline__ void cons_to_prim_pairs(const float2 w[5], float gm1, float q[5]) {
+  const float r = w[0].x + w[0].y;
+  const float rinv = 1.0f / r;
+  q[0] = r;
+  q[1] = (w[1].x + w[1].y) * rinv;
+  q[2] = (w[2].x + w[2].y) * rinv;
+  q[3] = WACT ? (w[3].x + w[3].y) * rinv : 0.0f;
+  const float2 k = kinetic_pair<WACT>(w[0], w[1], w[2], WACT ? w[3] : make_float2(0.0f, 0.0f));
+  q[4] = internal_energy(w[4], k) * gm1;
+}
+
+// consToPrim of a U* cell: conserved density and momenta, internal energy in
+// the energy slot.
+template <bool WACT>
+__device__ __forceinline__ void cons_to_prim_star(const float u[5], float gm1, float q[5]) {
+  const float r = u[0];
+  const float rinv = 1.0f / r;
+  q[0] = r;
+  q[1] = u[1] * rinv;
+  q[2] = u[2] * rinv;
+  q[3] = WACT ? u[3] * rinv : 0.0f;
+  q[4] = u[4] * gm1;
+}
+
+// The kinetic energy of a U* cell (FP32 values, exact as pairs).
+template <bool WACT>
+__device__ __forceinline__ float2 kinetic_star(const float u[5]) {
+  return kinetic_pair<WACT>(make_float2(u[0], 0.0f), make_float2(u[1], 0.0f), make_float2(u[2], 0.0f),
+                            make_float2(WACT ? u[3] : 0.0f, 0.0f));
+}
+
+// The CFL term (ComputeDt.h:28-54) of primitives in storage order.
+template <int PLANE>
+__device__ __forceinline__ float inv_dt_hyp_prim32(const float q[5], const Grid& G) {
   const float cs = sqrtf(q[4] * G.gamma_f / q[0]);
   const float vx = q[1], vy = PLANE == PLANE_XY ? q[2] : q[3], vz = PLANE == PLANE_XY ? q[3] : q[2];
   return (cs + fabsf(vx)) * G.inv_dx_f + (cs + fabsf(vy)) * G.inv_dy_f + (cs + fabsf(vz)) * G.inv_dz_f;
+}
+
+// The CFL term of a cell held as (hi, lo) pairs.
+template <int PLANE, bool WACT>
+__device__ __forceinline__ float inv_dt_hyp32(const float2 w[5], const Grid& G) {
+  float q[5];
+  cons_to_prim_pairs<PLANE, WACT>(w, G.gm1_f, q);
+  return inv_dt_hyp_prim32<PLANE>(q, G);
 }
 
 // minmod (Update.h:73-80) in FP32: 0 when the signs differ, else the argument
@@ -251,10 +328,15 @@ __device__ __forceinline__ void load_prims32(const Grid& G, const MixedFields& M
       const int idx = base + tid + k * kTileThreads;
       const int r = idx / HX, hx = idx - r * HX;
       const int hy = h0 + r;
-      float u[5], q[5];
+      float q[5];
+      if (in_pairs) {
+        cons_to_prim_pairs<PLANE, WACT>(w[k], gm1, q);
+      } else {
+        float u[5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) u[v] = v == 4 ? w[k][v].x : w[k][v].x + w[k][v].y;
-      cons_to_prim32<PLANE, WACT>(u, w[k][4].y, gm1, q);
+        for (int v = 0; v < 5; ++v) u[v] = w[k][v].x;
+        cons_to_prim_star<WACT>(u, gm1, q);
+      }
       if (fa[k]) q[1] = -q[1];
       if (fb[k]) q[2] = -q[2];
 #pragma unroll
@@ -333,12 +415,20 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
       du[2] += dt * V.q(0, cy + 2, cx + 2) * G.g_f;
       du[4] += dt * 0.5f * (V.fb(0, cy, cx) + V.fb(0, cy + 1, cx)) * G.g_f;
     }
-    // stage input at this cell, as a pair
+    // stage input at this cell, as a pair (U*: E* rebuilt from its internal
+    // energy and the kinetic energy of its stored density and momenta)
     float2 base[5];
+    if (in_pairs) {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      if (v == 3 && !WACT) continue;
-      base[v] = in_pairs ? src[v][o] : make_float2(M.us[v][o], 0.0f);
+      for (int v = 0; v < 5; ++v)
+        base[v] = (v == 3 && !WACT) ? make_float2(0.0f, 0.0f) : src[v][o];
+    } else {
+      float u[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) u[v] = (v == 3 && !WACT) ? 0.0f : M.us[v][o];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) base[v] = make_float2(u[v], 0.0f);
+      base[4] = pair_add(kinetic_star<WACT>(u), u[4]);
     }
     // density floor on the hydro update (Update.h:160), before TC / viscosity
     {
@@ -371,33 +461,37 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
         du[sv] += (vf[0][var] + vf[1][var] + vf[2][var]) * dt;
       }
     }
-    float fin[5], e_lo = 0.0f;
     if (kind == STAGE_RK_1) {
+      float us[5];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        if (v == 3 && !WACT) continue;
-        const float us = base[v].x + (base[v].y + du[v]);
-        M.us[v][o] = us;
-      }
+      for (int v = 0; v < 4; ++v) us[v] = (v == 3 && !WACT) ? 0.0f : base[v].x + (base[v].y + du[v]);
+      // U* keeps its internal energy: E* (a pair) minus the kinetic energy of
+      // the stored density and momenta
+      us[4] = internal_energy(pair_add(base[4], du[4]), kinetic_star<WACT>(us));
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        if (WACT || v != 3) M.us[v][o] = us[v];
       continue;
     }
     // RK2 stage 2: U^n+1 = 0.5 * (U^n + U* + dU); Euler: U^n+1 = U^n + dU
+    float2 fin[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      if (v == 3 && !WACT) continue;
+      if (v == 3 && !WACT) {
+        fin[v] = make_float2(0.0f, 0.0f);
+        continue;
+      }
       float2 r;
       if (kind == STAGE_RK_2) {
-        r = pair_add(pair_add(M.un[v][o], base[v].x), du[v]);
+        r = pair_add(pair_add(M.un[v][o], base[v]), du[v]);
         r = make_float2(0.5f * r.x, 0.5f * r.y);
       } else {
         r = pair_add(base[v], du[v]);
       }
       dst[v][o] = r;
-      fin[v] = r.x;
-      if (v == 4) e_lo = r.y;
+      fin[v] = r;
     }
-    if (!WACT) fin[3] = 0.0f;
-    const float inv = inv_dt_hyp32<PLANE, WACT>(fin, e_lo, G);
+    const float inv = inv_dt_hyp32<PLANE, WACT>(fin, G);
     bad |= !(inv <= 3.0e38f);  // NaN / inf: reported through the error flag
     red = fmaxf(red, inv);
   }

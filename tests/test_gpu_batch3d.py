@@ -12,7 +12,7 @@ import pytest
 
 import fv3d_gb300 as fv
 from fv3d_gb300 import problems
-from _helpers import rel_l1_fields
+from _helpers import assert_mixed_l1, rel_l1_fields
 
 pytestmark = pytest.mark.gpu
 
@@ -87,7 +87,7 @@ def test_batch3d_mixed_close_to_fp64(nsteps):
         assert all(np.isfinite(a).all() for a in got)
         want = _fp64_alone(p, nsteps)
         errs = rel_l1_fields(got, want)
-        assert errs[0] <= 1e-5 and errs[4] <= 1e-5, (i, errs)
+        assert_mixed_l1(errs, i)
 
 
 def test_batch3d_rejects_what_it_does_not_run():

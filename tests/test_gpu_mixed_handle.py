@@ -13,7 +13,7 @@ import pytest
 
 import fv3d_gb300 as fv
 from fv3d_gb300 import build, problems
-from _helpers import rel_l1_fields
+from _helpers import assert_mixed_l1, rel_l1_fields
 from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
@@ -52,11 +52,11 @@ def test_mixed_handle_steps_like_fp64(name):
     a.step(dt64)
     m.step(dt64)  # the same given dt
     errs = rel_l1_fields(m.get_prim(), a.get_prim())
-    assert errs[0] <= 1e-5 and errs[4] <= 1e-5, errs
+    assert_mixed_l1(errs)
     a.enqueue_steps(10)
     m.enqueue_steps(10)
     errs = rel_l1_fields(m.get_prim(), a.get_prim())
-    assert errs[0] <= 1e-5 and errs[4] <= 1e-5, errs
+    assert_mixed_l1(errs)
     ta, na = a.advance(0.02)
     tm, nm = m.advance(0.02)
     assert abs(na - nm) <= 1 and abs(ta - tm) <= 1e-4 * ta
@@ -73,7 +73,7 @@ def test_mixed_handle_step_host_and_refusals():
     a.set_prim(*pr.prim)
     a.step(dt)
     errs = rel_l1_fields(out, a.get_prim())
-    assert errs[0] <= 1e-5 and errs[4] <= 1e-5, errs
+    assert_mixed_l1(errs)
     with pytest.raises(fv.FvError) as e:
         m.set_cons(*a.get_cons())
     assert e.value.status == 2
@@ -123,4 +123,4 @@ def test_driver_runs_the_mixed_form(tmp_path):
     snaps = sorted(f for f in os.listdir(tmp_path) if re.fullmatch(r"snap_\d{4}\.bin", f))
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, *shape)
     errs = rel_l1_fields(list(got), ora.get_prim())
-    assert errs[0] <= 1e-5 and errs[4] <= 1e-5, errs
+    assert_mixed_l1(errs)

@@ -88,6 +88,7 @@ def test_golden_bitwise(name):
     ("rayleigh_taylor", dict(nx=512, nz=1536)),   # config 1 (RT), full size
     ("thermal_pulse", dict(n=1024)),              # config 1 (diffusion), full size
     ("shear_layer", dict(n=1024)),                # config 2 at 1/16 of the cells
+    ("shear_layer", dict(n=4096)),                # config 2, full size (16.8 M cells)
 ])
 def test_config_step_parity(builder, kw):
     pr = problems.BUILDERS[builder](**kw)
