@@ -549,14 +549,69 @@ def accuracy_entry(prim0, gamma, runs):
             "t_end": {"fp64": ta, "mixed": tm}, "rel_drift": drift, "wall_s": {"fp64": wa, "mixed": wm}}
 
 
+def checkpointed_pair(pr, fractions, perturb):
+    """The unstable configurations: the FP64 handle, the FP32-mixed handle
+    and (perturb > 0) a second FP64 handle whose initial density carries
+    seeded relative noise of amplitude `perturb`, advanced side by side to
+    each fraction of tend.  At every checkpoint: the per-field relative L1 of
+    mixed vs FP64 and of perturbed FP64 vs FP64 -- the latter measures how
+    much the flow itself amplifies a difference of rounding size."""
+    import fv3d_gb300 as fv
+    from fv3d_gb300 import problems
+    runs = {"fp64": pr.params, "mixed": _mixed(pr.params)}
+    if perturb:
+        runs["fp64_perturbed"] = pr.params
+    sims, clocks = {}, {}
+    for key, params in runs.items():
+        sims[key] = fv.Simulation(params)
+        prim = [a.copy() for a in pr.prim]
+        if key == "fp64_perturbed":
+            noise = problems.uniform(problems.MASTER_SEED, 99, prim[0].size).reshape(prim[0].shape)
+            prim[0] = prim[0] * (1.0 + perturb * (2.0 * noise - 1.0))
+        sims[key].set_prim(*prim)
+        clocks[key] = [0.0, 0, 0.0]  # t, steps, wall
+    out = []
+    states = {}
+    for f in fractions:
+        tend = f * pr.params.tend
+        for key, sim in sims.items():
+            t0 = time.perf_counter()
+            t, n = sim.advance(tend, t=clocks[key][0])
+            clocks[key][0] = t
+            clocks[key][1] += n
+            clocks[key][2] += time.perf_counter() - t0
+            states[key] = sim.get_prim()
+        row = {"t_target": tend, "t": {k: c[0] for k, c in clocks.items()},
+               "steps": {k: c[1] for k, c in clocks.items()},
+               "mixed_vs_fp64": dict(zip(["rho", "u", "v", "w", "p"],
+                                         [_rel_l1(a, b) for a, b in zip(states["mixed"], states["fp64"])]))}
+        if perturb:
+            row["fp64_perturbed_vs_fp64"] = dict(zip(["rho", "u", "v", "w", "p"], [
+                _rel_l1(a, b) for a, b in zip(states["fp64_perturbed"], states["fp64"])]))
+        out.append(row)
+        print(pr.name, json.dumps(row), file=sys.stderr, flush=True)
+    m0, e0 = _mass_energy(pr.prim, pr.params.gamma0)
+    drift = {}
+    for key in ("fp64", "mixed"):
+        m1, e1 = _mass_energy(states[key], pr.params.gamma0)
+        drift[key] = {"mass": abs(m1 - m0) / abs(m0), "energy": abs(e1 - e0) / abs(e0)}
+    for sim in sims.values():
+        sim.close()
+    return {"checkpoints": out, "rel_l1": out[-1]["mixed_vs_fp64"], "rel_drift": drift,
+            "perturbation": perturb, "wall_s": {k: c[2] for k, c in clocks.items()}}
+
+
 def run_accuracy(args):
     """The FP32-mixed form against the bit-exact FP64 form at every
     configuration's stated horizon (not timed): Sedov 256^2 to t = 0.1,
     Rayleigh-Taylor 512x1536 to t = 5, the thermal pulse 1024^2 for 200 steps,
     the shear layer 4096^2 to t = 1, the 512-instance batch for 200 steps and
-    the 64-instance Rayleigh-Taylor batch for 500 steps.  Prints one JSON
-    line: per configuration the per-field relative L1 (worst instance for
-    batches) and the mass / energy drift of both forms."""
+    the 64-instance Rayleigh-Taylor batch for 500 steps.  The Rayleigh-Taylor
+    and shear-layer flows are unstable (the instabilities they are named for
+    grow any difference exponentially): they are compared at checkpoints on
+    the way, next to FP64 runs from an initial state perturbed by 1e-8.
+    Prints one JSON line: per configuration the per-field relative L1 (worst
+    instance for batches) and the mass / energy drift of both forms."""
     import torch
     from fv3d_gb300 import problems
     torch.cuda.set_device(0)
@@ -566,16 +621,18 @@ def run_accuracy(args):
     def want(name):
         return only is None or name in only
 
-    singles = [("sedov_256_to_t0.1", lambda: problems.sedov(256), 0),
-               ("rayleigh_taylor_512x1536_to_t5", problem, 0),
-               ("thermal_pulse_1024_200_steps", lambda: problems.thermal_pulse(1024), 200),
-               ("shear_layer_4096_to_t1", lambda: problems.shear_layer(4096), 0)]
-    for name, build, nsteps in singles:
+    for name, build, nsteps in (("sedov_256_to_t0.1", lambda: problems.sedov(256), 0),
+                                ("thermal_pulse_1024_200_steps", lambda: problems.thermal_pulse(1024), 200)):
         if not want(name):
             continue
         pr = build()
         out[name] = accuracy_entry(pr.prim, pr.params.gamma0, _single_pair(pr, nsteps))
         print(name, json.dumps(out[name]), file=sys.stderr, flush=True)
+    for name, build in (("rayleigh_taylor_512x1536_to_t5", problem),
+                        ("shear_layer_4096_to_t1", lambda: problems.shear_layer(4096))):
+        if not want(name):
+            continue
+        out[name] = checkpointed_pair(build(), (0.1, 0.25, 0.5, 1.0), 1e-8)
     for name, build, nsteps in (("batch512_sod_sedov_200_steps", lambda: problems.batch_sod_sedov(512), 200),
                                 ("batch64_rt_500_steps", lambda: problems.batch_rt(64), 500)):
         if not want(name):
