@@ -100,6 +100,7 @@ def _declare(lib):
         "fvgpu_batch_launch_count": (C.c_int, [vp, C.POINTER(C.c_long)]),
         "fvgpu_probe_fp64_rate": (C.c_int, [_dp]),
         "fvgpu_probe_wait": (C.c_int, [C.c_int, C.c_int]),
+        "fvgpu_probe_grid_wait": (C.c_int, [C.c_int, C.c_int]),
         "fvgpu_step_host": (C.c_int, [vp, C.POINTER(_dp), C.c_double, C.POINTER(_dp), _dp]),
         "fvgpu_batch_tiling": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
     }
@@ -122,6 +123,13 @@ def probe_wait(arrive, max_polls):
     """Status of the bounded mbarrier wait run on its own (fvgpu_probe_wait):
     0 when it completed, FV_ERR_TIMEOUT when it gave up."""
     return load_library().fvgpu_probe_wait(1 if arrive else 0, int(max_polls))
+
+
+def probe_grid_wait(arrive_all, max_polls):
+    """Status of the multi-step kernel's bounded grid-barrier wait run on its
+    own (fvgpu_probe_grid_wait): 0 when it completed, FV_ERR_TIMEOUT when it
+    gave up because a CTA never arrived."""
+    return load_library().fvgpu_probe_grid_wait(1 if arrive_all else 0, int(max_polls))
 
 
 def parse_ini(text):

@@ -2,6 +2,7 @@
 // reduction, the per-step control kernel, primitive <-> conserved
 // conversions and the conservation sums.  Built without FMA contraction, like
 // the stage kernel, so every value rounds as in the reference.
+#include "fv_control.cuh"
 #include "fv_kernels.h"
 #include "fv_plane2d.cuh"
 
@@ -33,41 +34,6 @@ __global__ void __launch_bounds__(256) reduce2d_fp64(const Grid G, const Fields 
     if (!(inv <= 1.0e300)) atomicOr(&ctrl->err, 1);
   }
   block_max_atomic(red, &ctrl->slot[slot], s_red);
-}
-
-// The control step of one problem: dt, active flag, parity, time and step
-// counter, next reduction slot cleared.
-__device__ __forceinline__ void step_control(StepCtrl& c, int mode_override, double dt_given) {
-  const int p = (int)(c.step & 1);
-  const int mode = mode_override >= 0 ? mode_override : c.mode;
-  double dt;
-  int active;
-  if (mode == 0) {
-    dt = mode_override == 0 ? dt_given : c.dt_given;
-    active = 1;
-  } else {
-    // ComputeDt.h:62: CFL / max(inv_hyp, inv_tc, inv_visc); main.cpp:51 loop bound.
-    const double inv_hyp = __longlong_as_double((long long)c.slot[p]);
-    double m = inv_hyp;
-    if (c.inv_tc > m) m = c.inv_tc;
-    if (c.inv_visc > m) m = c.inv_visc;
-    dt = c.cfl / m;
-    // mode 2: fixed step count, no time bound; a previous error stops it
-    active = mode == 2 ? !c.err
-                       : (c.t + c.epsilon < c.tend) && (c.max_steps <= 0 || c.step < c.max_steps);
-    if (active && !(dt > 0.0 && dt <= 1.0e300)) {
-      c.err |= 1;
-      active = 0;
-    }
-  }
-  c.slot[p ^ 1] = 0ull;
-  c.parity = p;
-  c.active = active;
-  c.dt_cur = active ? dt : 0.0;
-  if (active) {
-    c.t = c.t + dt;
-    c.step = c.step + 1;
-  }
 }
 
 __global__ void control_kernel(StepCtrl* ctrl, int n, int mode_override, double dt_given) {

@@ -45,6 +45,11 @@ namespace {
 
 constexpr int kGraphSteps = 8;
 constexpr int kMaxGroups = 8;  // two work-queue counters each
+// Problems of at most this many cells in all run several steps per launch
+// (FP32-mixed RK2, one group of 2-D problems): their steps are bound by
+// launch latency, not by the GPU's throughput.
+constexpr long long kMultiMaxCells = 1LL << 21;
+constexpr int kMultiChunk = 256;  // steps per multi-step launch of a loop with a time bound
 
 struct Group {
   int ndim = 2;     // 3: 3-D problems (one kernel shape, grouped by solver)
@@ -77,13 +82,15 @@ struct fv_batch {
   long long max_fstride = 0;
   StepCtrl* d_ctrl = nullptr;
   StepCtrl* h_ctrl = nullptr;
-  unsigned* d_queue = nullptr;
+  unsigned* d_queue = nullptr;  // 2 per group, then the grid barrier's counter and abort flag
   std::vector<Group> groups;
   bool prepared = false;
   int flip = 0;  // Euler: current states are in B
   cudaStream_t own_stream = nullptr, stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaGraphExec_t graph_loop = nullptr;  // steps in each control block's own mode
+  BatchInst* d_inst_multi = nullptr;     // descriptors of the multi-step launch
+  int ntiles_multi = 0, grid_multi = 0, rows_multi = 0;
   long launches = 0;
   std::string err;
 };
@@ -445,6 +452,8 @@ int Autotune(fv_batch* b, Group& g) {
 void ReleaseGroups(fv_batch* b) {
   for (auto& g : b->groups)
     if (g.d_inst) cudaFree(g.d_inst);
+  if (b->d_inst_multi) cudaFree(b->d_inst_multi);
+  b->d_inst_multi = nullptr;
   b->groups.clear();
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->graph_loop) cudaGraphExecDestroy(b->graph_loop);
@@ -486,6 +495,66 @@ int Prepare(fv_batch* b) {
   }
   BCUDA(b, cudaStreamSynchronize(b->stream));
   b->prepared = true;
+  return FV_OK;
+}
+
+// The error status of a control block's sticky flag: bit 1 a bounded wait
+// that gave up, bit 0 a non-finite state or dt.
+int ErrStatus(int err) { return (err & 2) ? FV_ERR_TIMEOUT : FV_ERR_NONFINITE; }
+
+// Whether run / advance take several steps per launch (batch_multi32): the
+// FP32-mixed RK2 form, one group of 2-D problems, few cells in all.
+// FV3D_MULTISTEP=0 keeps the per-stage launches, =1 takes the multi-step
+// launch whatever the size.
+bool MultiEligible(const fv_batch* b) {
+  if (b->precision != FV_PREC_FP32_MIXED || b->ts != FV_TS_RK2 || b->groups.size() != 1) return false;
+  const Group& g = b->groups[0];
+  if (g.ndim != 2 || (int)g.members.size() > fv::batch_multi_problems32()) return false;
+  const char* env = std::getenv("FV3D_MULTISTEP");
+  if (env && env[0] == '0') return false;
+  long long cells = 0;
+  for (int i : g.members) cells += (long long)b->G[i].na * b->G[i].nb;
+  return cells <= kMultiMaxCells || (env && env[0] == '1');
+}
+
+// Descriptors of the multi-step launch: the group's strip width, rows per
+// work item that give each resident CTA about one item (4 to 64; measured on
+// Sedov 128^2 / 256^2 / 512^2 and 16 Sod tubes of 96^2, this count was the
+// fastest of 4 / 8 / 16 / 32 rows each time; FV3D_MULTI_ROWS forces it).
+int PrepareMulti(fv_batch* b) {
+  if (b->d_inst_multi) return FV_OK;
+  Group& g = b->groups[0];
+  const int occ = fv::batch_multi_occupancy32(g.plane, g.wact, g.shape, g.tc);
+  if (occ <= 0) return Fail(b, FV_ERR_CUDA, "the multi-step kernel cannot be launched");
+  const fv::TileShape* shapes;
+  NumShapes(b->precision, &shapes);
+  const int tx = shapes[g.shape].tx;
+  long long units = 0;
+  for (int i : g.members) units += (long long)((b->G[i].na + tx - 1) / tx) * b->G[i].nb;
+  const long long slots = (long long)occ * SmCount();
+  int rows = (int)std::min(64LL, std::max(4LL, (units + slots - 1) / slots));
+  if (const char* f = std::getenv("FV3D_MULTI_ROWS")) rows = std::max(1, std::atoi(f));
+  std::vector<BatchInst> d = Describe(b, g, g.shape, b->d_ctrl, &b->ntiles_multi, rows);
+  BCUDA(b, cudaMalloc(&b->d_inst_multi, sizeof(BatchInst) * d.size()));
+  BCUDA(b, cudaMemcpyAsync(b->d_inst_multi, d.data(), sizeof(BatchInst) * d.size(), cudaMemcpyHostToDevice,
+                           b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  b->rows_multi = rows;
+  b->grid_multi = (int)std::max(1LL, std::min((long long)b->ntiles_multi, slots));
+  return FV_OK;
+}
+
+// nsteps steps of the (single) group in one cooperative launch.
+int RunMulti(fv_batch* b, int nsteps, int mode_override) {
+  const Group& g = b->groups[0];
+  unsigned* bar = b->d_queue + 2 * kMaxGroups;
+  BCUDA(b, cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), b->stream));
+  const fv::GridBarrier gb{bar, reinterpret_cast<int*>(bar + 1)};
+  const cudaError_t e = fv::launch_batch_multi32(g.plane, g.wact, g.shape, b->d_inst_multi, (int)g.members.size(),
+                                                 b->ntiles_multi, nsteps, mode_override, gb, b->grid_multi, g.tc,
+                                                 b->stream);
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "multi-step launch: %s", cudaGetErrorString(e));
+  b->launches += 1;
   return FV_OK;
 }
 
@@ -598,7 +667,7 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
       cudaMalloc(&b->scratch, (size_t)5 * b->max_fstride * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&b->d_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
       cudaMallocHost(&b->h_ctrl, sizeof(StepCtrl) * n) != cudaSuccess ||
-      cudaMalloc(&b->d_queue, sizeof(unsigned) * 2 * kMaxGroups) != cudaSuccess)
+      cudaMalloc(&b->d_queue, sizeof(unsigned) * (2 * kMaxGroups + 2)) != cudaSuccess)
     return Fail(b, FV_ERR_NOMEM, "batch allocation of %zu bytes failed", total * sizeof(double));
   // Initialisation is ordered on the batch's own non-blocking stream (a
   // legacy-stream cudaMemset would not be ordered with it) and waited for
@@ -607,7 +676,7 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
     return Fail(b, FV_ERR_CUDA, "stream creation failed");
   b->stream = b->own_stream;
   BCUDA(b, cudaMemsetAsync(b->buf, 0, total * sizeof(double), b->stream));
-  BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned) * 2 * kMaxGroups, b->stream));
+  BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned) * (2 * kMaxGroups + 2), b->stream));
   b->A.resize(n);
   b->B.resize(n);
   b->Q.assign(n, Fields{});
@@ -732,6 +801,11 @@ int fvgpu_batch_run(fv_batch* b, long nsteps) {
   if (rc) return rc;
   rc = EnsureSlots(b);
   if (rc) return rc;
+  if (MultiEligible(b)) {  // small problems: every step in one launch
+    rc = PrepareMulti(b);
+    if (rc == FV_OK && nsteps > 0) rc = RunMulti(b, (int)std::min<long>(nsteps, 1L << 30), 2);
+    return rc;
+  }
   long done = 0;
   // Euler ping-pong: graphs are captured for an even start (state in A)
   if (b->ts != FV_TS_RK2 && b->flip && nsteps > 0) {
@@ -781,7 +855,8 @@ int fvgpu_batch_times(fv_batch* b, double* t) {
     t[i] = b->h_ctrl[i].t;
     if (b->h_ctrl[i].err && bad < 0) bad = i;
   }
-  if (bad >= 0) return Fail(b, FV_ERR_NONFINITE, "problem %d met a non-finite state or dt", bad);
+  if (bad >= 0)
+    return Fail(b, ErrStatus(b->h_ctrl[bad].err), "problem %d met a non-finite state or dt, or a wait gave up", bad);
   return FV_OK;
 }
 
@@ -859,7 +934,8 @@ int batch_compute_dt(fv_batch* b, int i, double* dt, double inv[3]) {
     inv[2] = b->inv_visc[i];
   }
   if (dt) *dt = d;
-  if (c.err || !std::isfinite(d)) return Fail(b, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
+  if (c.err) return Fail(b, ErrStatus(c.err), "non-finite state or a wait that gave up (dt = %g)", d);
+  if (!std::isfinite(d)) return Fail(b, FV_ERR_NONFINITE, "non-finite state or dt (dt = %g)", d);
   return FV_OK;
 }
 
@@ -896,7 +972,20 @@ int batch_advance(fv_batch* b, double tend, long max_steps, double* t, long* nst
   c.max_steps = max_steps > 0 ? step0 + max_steps : 0;
   BCUDA(b, cudaMemcpyAsync(b->d_ctrl, &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, b->stream));
   const bool short_run = max_steps > 0 && max_steps < kGraphSteps;
+  const bool multi = MultiEligible(b);
+  if (multi) {
+    rc = PrepareMulti(b);
+    if (rc) return rc;
+  }
   for (;;) {
+    if (multi) {  // the kernel stops by itself at the time bound or max_steps
+      rc = RunMulti(b, kMultiChunk, -1);
+      if (rc) return rc;
+      rc = ReadCtrl(b);
+      if (rc) return rc;
+      if (b->h_ctrl[0].err || !b->h_ctrl[0].active) break;
+      continue;
+    }
     if (short_run) {
       for (long k = 0; k < max_steps; ++k) {
         rc = EnqueueStep(b, -1, 0.0);
@@ -940,7 +1029,7 @@ int batch_advance(fv_batch* b, double tend, long max_steps, double* t, long* nst
   b->slot_valid[0] = 1;
   *t = b->h_ctrl[0].t;
   if (nsteps) *nsteps = (long)(b->h_ctrl[0].step - step0);
-  if (b->h_ctrl[0].err) return Fail(b, FV_ERR_NONFINITE, "non-finite state or dt during advance");
+  if (b->h_ctrl[0].err) return Fail(b, ErrStatus(b->h_ctrl[0].err), "non-finite state or dt, or a wait that gave up, during advance");
   return FV_OK;
 }
 

@@ -3,6 +3,8 @@
 // fast-math (FP32 division / sqrt approximations, FMA contraction); the
 // error-free pair arithmetic of fv_tile32.cuh is written with adds and _rn
 // intrinsics, which contraction leaves alone.
+#include "fv_control.cuh"
+#include "fv_grid.cuh"
 #include "fv_tile32.cuh"
 
 namespace fv {
@@ -18,8 +20,10 @@ constexpr int kBlockRows32[] = {16, 16, 16, 16};
 constexpr int kKernelOf32[] = {0, 1, 0, 1};
 constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
 
-__device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts, int ninst, int t,
-                                             BatchInst* s_inst) {
+// Copies the descriptor of the problem holding work item t to s_inst and
+// returns its index (binary search over the first items).
+__device__ __forceinline__ int fetch_inst32(const BatchInst* __restrict__ insts, int ninst, int t,
+                                            BatchInst* s_inst) {
   int lo = 0, hi = ninst - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -29,6 +33,7 @@ __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts
   const unsigned long long* src = reinterpret_cast<const unsigned long long*>(insts + lo);
   unsigned long long* dst = reinterpret_cast<unsigned long long*>(s_inst);
   for (int w = threadIdx.x; w < (int)(sizeof(BatchInst) / 8); w += blockDim.x) dst[w] = src[w];
+  return lo;
 }
 
 #if FV_MIXED_MIN_CTAS > 0
@@ -36,6 +41,44 @@ __device__ __forceinline__ void fetch_inst32(const BatchInst* __restrict__ insts
 #else
 #define FV_MIXED_BOUNDS __launch_bounds__(kTileThreads)
 #endif
+
+// One work item t (a strip segment of problem I) of one stage.  active / dt:
+// the problem's step in flight; slot_next / err: its CFL maximum slot for the
+// next step and its error flag (stages that end a step).  Every thread of
+// the CTA calls it; s_inst holds I.
+template <int PLANE, bool WACT, class TL>
+__device__ __forceinline__ void stage_item32(const BatchInst& I, int t, int kind, int flip, bool active, double dt_step,
+                                             unsigned long long* slot_next, int* err, float* smem,
+                                             unsigned long long* s_red) {
+  const int lt = t - I.tile0;
+  const int bx = lt % I.tiles_x, by = lt / I.tiles_x;
+  MixedFields M;
+  float2* src[5];
+  float2* dst[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    M.un[v] = reinterpret_cast<float2*>(I.A.f[v]);
+    M.us[v] = reinterpret_cast<float*>(I.B.f[v]);
+    float2* a = reinterpret_cast<float2*>(I.A.f[v]);
+    float2* b = reinterpret_cast<float2*>(I.B.f[v]);
+    src[v] = (kind == STAGE_EULER && flip) ? b : a;
+    dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
+  }
+  const int x0 = bx * TL::TX, ya = by * I.tz;  // tz: rows per work item
+  const int yb = ya + I.tz < I.G.nb ? ya + I.tz : I.G.nb;
+  if (!active) {
+    if (kind == STAGE_EULER) pass_on32<WACT, TL::TX>(I.G, src, dst, x0, ya, yb, threadIdx.x);
+    return;
+  }
+  const float dt = (float)dt_step;  // the one FP64 -> FP32 conversion per item
+  float red = 0.0f;
+  bool bad = false;
+  stage_segment32<PLANE, WACT, TL>(I.G, M, src, dst, I.rs, kind, dt, x0, ya, yb, smem, red, bad);
+  if (kind != STAGE_RK_1) {
+    if (bad) atomicOr(err, 1);
+    block_max_atomic((unsigned long long)__double_as_longlong((double)red), slot_next, s_red);
+  }
+}
 
 template <int PLANE, bool WACT, class TL>
 __global__ void FV_MIXED_BOUNDS
@@ -56,35 +99,107 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
     }
     fetch_inst32(insts, ninst, t, &s_inst);
     __syncthreads();
-    const BatchInst& I = s_inst;
-    const int lt = t - I.tile0;
-    const int bx = lt % I.tiles_x, by = lt / I.tiles_x;
-    MixedFields M;
-    float2* src[5];
-    float2* dst[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      M.un[v] = reinterpret_cast<float2*>(I.A.f[v]);
-      M.us[v] = reinterpret_cast<float*>(I.B.f[v]);
-      float2* a = reinterpret_cast<float2*>(I.A.f[v]);
-      float2* b = reinterpret_cast<float2*>(I.B.f[v]);
-      src[v] = (kind == STAGE_EULER && flip) ? b : a;
-      dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
+    StepCtrl* ctrl = s_inst.ctrl;
+    stage_item32<PLANE, WACT, TL>(s_inst, t, kind, flip, ctrl->active != 0, ctrl->dt_cur,
+                                  &ctrl->slot[ctrl->parity ^ 1], &ctrl->err, smem_f, s_red);
+  }
+}
+
+// Problems a multi-step launch can carry (per-problem step state sits in
+// shared memory).
+constexpr int kMultiMaxProblems = 256;
+
+// Several RK2 steps of a group in one cooperative launch (every CTA
+// resident): per step, each CTA decides every problem's dt and active flag
+// itself (step_decide on the reduced CFL maximum, the same arithmetic as the
+// control kernel, so every CTA reaches the same values), then stage 1 over
+// the work items t = blockIdx.x, blockIdx.x + gridDim.x, ..., a grid
+// barrier, stage 2 (CFL maxima by atomics), a grid barrier.  Each work item
+// runs the per-stage kernel's body, so the result is bit-identical to the
+// per-stage launches.  The time and step counter of each problem are kept in
+// shared memory during the launch and written back to the control blocks at
+// its end by CTA 0; the CFL slot of the next step is zeroed by CTA 0.  A
+// barrier wait that runs out sets bit 1 of every problem's error flag and
+// the kernel returns.
+template <int PLANE, bool WACT, class TL>
+__global__ void FV_MIXED_BOUNDS batch_multi32(const BatchInst* __restrict__ insts, int ninst, int ntiles, int nsteps,
+                                              int mode_override, GridBarrier gb) {
+  extern __shared__ float smem_f[];
+  __shared__ unsigned long long s_red[kTileThreads / 32];
+  __shared__ BatchInst s_inst;
+  __shared__ double s_t[kMultiMaxProblems], s_dt[kMultiMaxProblems];
+  __shared__ long long s_step[kMultiMaxProblems];
+  __shared__ int s_act[kMultiMaxProblems], s_par[kMultiMaxProblems], s_err[kMultiMaxProblems];
+  __shared__ int s_any;
+  auto timed_out = [&]() {
+    if (threadIdx.x == 0)
+      for (int m = 0; m < ninst; ++m) atomicOr(&insts[m].ctrl->err, 2);
+  };
+  for (int m = threadIdx.x; m < ninst; m += blockDim.x) {
+    const StepCtrl* c = insts[m].ctrl;
+    s_t[m] = c->t;
+    s_step[m] = c->step;
+    s_err[m] = 0;
+  }
+  __syncthreads();
+  unsigned bar = 0;
+  // every CTA has read the initial times before CTA 0 may write any control block
+  if (!grid_sync(gb, bar++)) {
+    timed_out();
+    return;
+  }
+  int k = 0;
+  bool decided = false;
+  for (; k < nsteps; ++k) {
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    for (int m = threadIdx.x; m < ninst; m += blockDim.x) {
+      StepCtrl* c = insts[m].ctrl;
+      double dt;
+      int active;
+      bool bad;
+      step_decide(*c, s_t[m], s_step[m], c->err | s_err[m], mode_override, 0.0, dt, active, bad);
+      const int p = (int)(s_step[m] & 1);
+      if (bad) s_err[m] = 1;
+      s_dt[m] = active ? dt : 0.0;
+      s_act[m] = active;
+      s_par[m] = p;
+      if (blockIdx.x == 0) c->slot[p ^ 1] = 0ull;  // read by no CTA in this step
+      if (active) {
+        s_t[m] = __dadd_rn(s_t[m], dt);
+        s_step[m] += 1;
+        s_any = 1;
+      }
     }
-    StepCtrl* ctrl = I.ctrl;
-    const int x0 = bx * TL::TX, ya = by * I.tz;  // tz: rows per work item
-    const int yb = ya + I.tz < I.G.nb ? ya + I.tz : I.G.nb;
-    if (!ctrl->active) {
-      if (kind == STAGE_EULER) pass_on32<WACT, TL::TX>(I.G, src, dst, x0, ya, yb, threadIdx.x);
-      continue;
+    __syncthreads();
+    decided = true;
+    if (!s_any) break;  // every CTA decides alike: no problem steps any more
+    for (int kind = STAGE_RK_1; kind <= STAGE_RK_2; ++kind) {
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        __syncthreads();  // the previous item is finished with s_inst and smem
+        const int m = fetch_inst32(insts, ninst, t, &s_inst);
+        __syncthreads();
+        StepCtrl* ctrl = s_inst.ctrl;
+        stage_item32<PLANE, WACT, TL>(s_inst, t, kind, 0, s_act[m] != 0, s_dt[m], &ctrl->slot[s_par[m] ^ 1],
+                                      &ctrl->err, smem_f, s_red);
+      }
+      if (!grid_sync(gb, bar++)) {
+        timed_out();
+        return;
+      }
     }
-    const float dt = (float)ctrl->dt_cur;  // the one FP64 -> FP32 conversion per item
-    float red = 0.0f;
-    bool bad = false;
-    stage_segment32<PLANE, WACT, TL>(I.G, M, src, dst, I.rs, kind, dt, x0, ya, yb, smem_f, red, bad);
-    if (kind != STAGE_RK_1) {
-      if (bad) atomicOr(&ctrl->err, 1);
-      block_max_atomic((unsigned long long)__double_as_longlong((double)red), &ctrl->slot[ctrl->parity ^ 1], s_red);
+  }
+  if (blockIdx.x == 0) {  // the control blocks as the per-stage launches leave them
+    for (int m = threadIdx.x; m < ninst; m += blockDim.x) {
+      StepCtrl* c = insts[m].ctrl;
+      if (decided) {
+        c->parity = s_par[m];
+        c->active = s_act[m];
+        c->dt_cur = s_dt[m];
+      }
+      c->t = s_t[m];
+      c->step = s_step[m];
+      if (s_err[m]) atomicOr(&c->err, 1);
     }
   }
 }
@@ -103,6 +218,18 @@ size_t smem_for(bool wact, bool tc) {
 }
 
 typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
+
+typedef void (*MultiKernel)(const BatchInst*, int, int, int, int, GridBarrier);
+
+template <int PLANE, bool WACT>
+MultiKernel pick_multi(int shape) {
+  return kKernelOf32[shape] == 0 ? batch_multi32<PLANE, WACT, BlockOf32<0>> : batch_multi32<PLANE, WACT, BlockOf32<1>>;
+}
+
+MultiKernel pick_multi_any(int plane, bool wact, int shape) {
+  if (plane == PLANE_XY) return wact ? pick_multi<PLANE_XY, true>(shape) : pick_multi<PLANE_XY, false>(shape);
+  return wact ? pick_multi<PLANE_XZ, true>(shape) : pick_multi<PLANE_XZ, false>(shape);
+}
 
 template <int PLANE, bool WACT>
 BatchKernel pick(int shape) {
@@ -129,6 +256,16 @@ cudaError_t prepare(int plane, bool wact, int shape) {
   if (flag) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(pick_any(plane, wact, shape), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem_any(shape, wact, true));
+  if (e == cudaSuccess) flag = true;
+  return e;
+}
+
+cudaError_t prepare_multi(int plane, bool wact, int shape) {
+  static bool done[2][2][kNumShapes32] = {};
+  bool& flag = done[plane == PLANE_XY ? 0 : 1][wact ? 1 : 0][shape];
+  if (flag) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(pick_multi_any(plane, wact, shape),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_any(shape, wact, true));
   if (e == cudaSuccess) flag = true;
   return e;
 }
@@ -214,6 +351,37 @@ cudaError_t launch_batch_stage32(int plane, bool wact, int shape, const BatchIns
   if (e != cudaSuccess) return e;
   e = launch_pdl(pick_any(plane, wact, shape), dim3(grid), dim3(kTileThreads), smem_any(shape, wact, tc), st, insts,
                  ninst, ntiles, queue, kind, flip);
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+int batch_multi_problems32() { return kMultiMaxProblems; }
+
+int batch_multi_occupancy32(int plane, bool wact, int shape, bool tc) {
+  if (shape < 0 || shape >= kNumShapes32 || prepare_multi(plane, wact, shape) != cudaSuccess) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pick_multi_any(plane, wact, shape), kTileThreads,
+                                                    smem_any(shape, wact, tc)) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+cudaError_t launch_batch_multi32(int plane, bool wact, int shape, const BatchInst* insts, int ninst, int ntiles,
+                                 int nsteps, int mode_override, GridBarrier gb, int grid, bool tc,
+                                 cudaStream_t st) {
+  if (shape < 0 || shape >= kNumShapes32 || ninst > kMultiMaxProblems) return cudaErrorInvalidValue;
+  cudaError_t e = prepare_multi(plane, wact, shape);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kTileThreads);
+  cfg.dynamicSmemBytes = smem_any(shape, wact, tc);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident: the grid barriers need it
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, pick_multi_any(plane, wact, shape), insts, ninst, ntiles, nsteps, mode_override, gb);
   return e != cudaSuccess ? e : cudaGetLastError();
 }
 

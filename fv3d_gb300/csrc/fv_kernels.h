@@ -6,6 +6,7 @@
 #include <utility>
 
 #include "fv_device.cuh"
+#include "fv_grid.cuh"
 #include "fv_tma.cuh"
 
 namespace fv {
@@ -188,6 +189,19 @@ cudaError_t launch_batch_stage3d32(const BatchInst* insts, int ninst, int ntiles
                                    int rs, int grid, bool tc, cudaStream_t stream);
 int batch_stage3d_occupancy64(bool tc);
 int batch_stage3d_occupancy32(bool tc);
+
+// Several RK2 steps of a group of FP32-mixed 2-D problems in one cooperative
+// launch (fv_batch32.cu, batch_multi32): for small grids, whose steps are
+// bound by launch latency.  At most batch_multi_problems32() problems; grid
+// at most batch_multi_occupancy32() x SMs CTAs (all resident); the barrier
+// counter and abort flag of gb zeroed before the launch; a grid-barrier wait
+// that runs out sets bit 1 of every problem's error flag.  mode_override as
+// launch_control.
+int batch_multi_problems32();
+int batch_multi_occupancy32(int plane, bool wact, int shape, bool tc);
+cudaError_t launch_batch_multi32(int plane, bool wact, int shape, const BatchInst* insts, int ninst, int ntiles,
+                                 int nsteps, int mode_override, GridBarrier gb, int grid, bool tc,
+                                 cudaStream_t stream);
 
 // launch_control for n problems plus a reset of nq work-queue counters.
 cudaError_t launch_batch_control(StepCtrl* ctrl, int n, unsigned* queue, int nq, int mode_override, double dt_given,

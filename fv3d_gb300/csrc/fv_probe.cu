@@ -1,5 +1,6 @@
 // fv_probe.cu -- measures the FP64 FMA throughput of the current GPU, and
-// exercises the bounded mbarrier wait of the TMA staging path.
+// exercises the bounded waits: the mbarrier wait of the TMA staging path and
+// the grid barrier of the multi-step kernel.
 //
 // The bit-exact FP64 stage kernels are bound by the FP64 pipe, not by HBM,
 // so their roofline is the FP64 instruction rate.  fvgpu_probe_fp64_rate
@@ -9,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "fv3d_gb300.h"
+#include "fv_grid.cuh"
 #include "fv_tma.cuh"
 
 namespace {
@@ -46,7 +48,42 @@ __global__ void __launch_bounds__(kThreads) wait_probe(int arrive, int max_polls
   if (threadIdx.x == 0) out[0] = ok ? 1 : 0;
 }
 
+// Two resident CTAs meet at the multi-step kernel's grid barrier; CTA 1
+// arrives only when `arrive_all` is set.  out[0] = 1 when CTA 0's wait
+// completed, 0 when it gave up.
+__global__ void __launch_bounds__(kThreads) grid_wait_probe(fv::GridBarrier gb, int arrive_all, int max_polls,
+                                                            int* out) {
+  if (blockIdx.x == 1 && !arrive_all) return;  // never arrives
+  const bool ok = fv::grid_sync(gb, 0, max_polls);
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = ok ? 1 : 0;
+}
+
 }  // namespace
+
+extern "C" int fvgpu_probe_grid_wait(int arrive_all, int max_polls) {
+  if (max_polls < 1) return FV_ERR_PARAM;
+  unsigned* d = nullptr;  // barrier counter, abort flag, result
+  int h = -1;
+  if (cudaMalloc(&d, 3 * sizeof(unsigned)) != cudaSuccess) return FV_ERR_NOMEM;
+  bool ok = cudaMemset(d, 0, 3 * sizeof(unsigned)) == cudaSuccess;
+  if (ok) {
+    const fv::GridBarrier gb{d, reinterpret_cast<int*>(d + 1)};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(kThreads);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ok = cudaLaunchKernelEx(&cfg, grid_wait_probe, gb, arrive_all ? 1 : 0, max_polls,
+                            reinterpret_cast<int*>(d + 2)) == cudaSuccess &&
+         cudaMemcpy(&h, d + 2, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(d);
+  if (!ok) return FV_ERR_CUDA;
+  return h == 1 ? FV_OK : FV_ERR_TIMEOUT;
+}
 
 extern "C" int fvgpu_probe_wait(int arrive, int max_polls) {
   if (max_polls < 1) return FV_ERR_PARAM;

@@ -237,6 +237,12 @@ int fvgpu_probe_fp64_rate(double* lane_ops_per_s);
  * barrier completes first.  FV_OK when the wait completed, FV_ERR_TIMEOUT when
  * it gave up (the kernel then returns normally and the context stays usable). */
 int fvgpu_probe_wait(int arrive, int max_polls);
+/* The same for the grid barrier of the multi-step batch kernel: two resident
+ * CTAs meet at it, the second only when arrive_all != 0; the first waits at
+ * most max_polls polls.  FV_OK when the wait completed, FV_ERR_TIMEOUT when
+ * it gave up (the kernel returns normally and the context stays usable).
+ * No reference counterpart. */
+int fvgpu_probe_grid_wait(int arrive_all, int max_polls);
 
 /* ---- many independent problems (no reference counterpart) --------------- */
 typedef struct fv_batch fv_batch;

@@ -12,19 +12,29 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # CPU arithmetic: relative L1 per field.
 REL_L1_STEP = 1e-12
 
-# Bounds of the FP32-mixed form against the bit-exact FP64 form, relative L1
-# per field (rho, u, v, w, p): 1e-5 on density (the stated target) and
-# pressure; 1e-4 on the velocities, some of which start at zero and stay
-# small (the rotated or viscosity-driven components), so their relative
-# error is measured against a small norm.
-MIXED_L1 = (1e-5, 1e-4, 1e-4, 1e-4, 1e-5)
+# Bounds of the FP32-mixed form against the bit-exact FP64 form: relative L1
+# <= 1e-5 on density (the stated target) and pressure; on the velocities a
+# mean absolute difference <= 1e-5 of the largest signal speed |u| + c of the
+# FP64 state.  Velocity components can start at zero and stay tiny (the
+# x-velocity of a Rayleigh-Taylor run, the viscosity-driven third
+# component), where a relative L1 would measure FP32 rounding against an
+# almost empty norm; the signal speed is the scale of the rounding of the
+# momentum fluxes.
+MIXED_L1 = 1e-5
+MIXED_VEL = 1e-5
 FIELD_NAMES = ("rho", "u", "v", "w", "p")
 
 
-def assert_mixed_l1(errs, ctx=""):
-    """Every field of the mixed form within MIXED_L1 of the FP64 form."""
-    for k, (e, bound) in enumerate(zip(errs, MIXED_L1)):
-        assert e <= bound, (ctx, FIELD_NAMES[k], e, bound, dict(zip(FIELD_NAMES, errs)))
+def assert_mixed(got, want, gamma, ctx=""):
+    """The mixed-form state got (rho, u, v, w, p) against the FP64 state
+    want, within MIXED_L1 / MIXED_VEL; the message states every field."""
+    errs = rel_l1_fields(got, want)
+    c = np.sqrt(gamma * np.asarray(want[4]) / np.asarray(want[0]))
+    speed = float((np.sqrt(want[1] ** 2 + want[2] ** 2 + want[3] ** 2) + c).max())
+    dv = [float(np.abs(np.asarray(got[k]) - np.asarray(want[k])).mean()) / speed for k in (1, 2, 3)]
+    msg = (ctx, dict(zip(FIELD_NAMES, errs)), {"du": dv[0], "dv": dv[1], "dw": dv[2]})
+    assert errs[0] <= MIXED_L1 and errs[4] <= MIXED_L1, msg
+    assert max(dv) <= MIXED_VEL, msg
 
 
 def golden_cases():

@@ -2,9 +2,9 @@
 
 FP64 batches must reproduce, bit for bit, each problem advanced alone (which
 itself reproduces the reference bit for bit), whatever tile shape the
-autotuner picks.  The FP32-mixed form must stay within MIXED_L1 of the FP64
-result on every field (relative L1: density and pressure 1e-5, velocities
-1e-4).
+autotuner picks.  The FP32-mixed form must stay within the mixed-form
+bounds of the FP64 result on every field (assert_mixed: relative L1 1e-5 on
+density and pressure, velocities within 1e-5 of the signal speed).
 """
 import os
 import subprocess
@@ -15,7 +15,7 @@ import pytest
 
 import fv3d_gb300 as fv
 from fv3d_gb300 import problems
-from _helpers import assert_mixed_l1, rel_l1_fields
+from _helpers import assert_mixed
 
 pytestmark = pytest.mark.gpu
 
@@ -182,8 +182,8 @@ def test_fp64_batch_euler_pingpong():
 
 
 def test_mixed_batch_l1_against_fp64():
-    """FP32-mixed vs FP64 after 200 steps: every field within MIXED_L1
-    (density and pressure 1e-5, velocities 1e-4)."""
+    """FP32-mixed vs FP64 after 200 steps: every field within the mixed-form
+    bounds (assert_mixed)."""
     probs = [problems.sod(128, "x", nx_other=32), problems.sedov(96, tend=1.0e30),
              problems.sod(64, "y", gamma=1.6, nx_other=48), problems.sedov(128, gamma=1.3, tend=1.0e30)]
     nsteps = 200
@@ -199,9 +199,7 @@ def test_mixed_batch_l1_against_fp64():
     b.run(nsteps)
     t = b.times()
     for i in range(len(probs)):
-        got = b.get_prim(i)
-        errs = rel_l1_fields(got, ref[i])
-        assert_mixed_l1(errs, i)
+        assert_mixed(b.get_prim(i), ref[i], probs[i].params.gamma0, i)
         assert abs(t[i] - ref_t[i]) <= 1e-4 * ref_t[i], (i, t[i], ref_t[i])
 
 
@@ -220,7 +218,7 @@ def test_mixed_batch_rt_with_diffusion():
         b.set_prim(i, *pr.prim)
     b.run(nsteps)
     for i in range(len(probs)):
-        assert_mixed_l1(rel_l1_fields(b.get_prim(i), ref[i]), i)
+        assert_mixed(b.get_prim(i), ref[i], probs[i].params.gamma0, i)
 
 
 def test_batch_nonfinite_reported():
