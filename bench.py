@@ -349,6 +349,7 @@ def time_batch(torch, params_list, prims, nsteps, warmup, flush_each=None):
     for i, pr in enumerate(prims):
         b.set_prim(i, *pr)
     tiles = b.tiling()
+    schedule = b.schedule()
     b.run(warmup)
     b.synchronize()
     l0 = b.launch_count()
@@ -373,7 +374,7 @@ def time_batch(torch, params_list, prims, nsteps, warmup, flush_each=None):
             ms += e0.elapsed_time(e1)
     b.times()  # surfaces any error
     return b, {"mcell_updates_per_s": cells * nsteps / (ms / 1e3) / 1e6, "ms_per_step": ms / nsteps,
-               "cells": cells, "instances": len(params_list), "tiles": tiles,
+               "cells": cells, "instances": len(params_list), "tiles": tiles, "schedule": schedule,
                "gpu_launches": b.launch_count() - l0}
 
 

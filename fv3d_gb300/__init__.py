@@ -103,6 +103,7 @@ def _declare(lib):
         "fvgpu_probe_grid_wait": (C.c_int, [C.c_int, C.c_int]),
         "fvgpu_step_host": (C.c_int, [vp, C.POINTER(_dp), C.c_double, C.POINTER(_dp), _dp]),
         "fvgpu_batch_tiling": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]),
+        "fvgpu_batch_schedule": (C.c_int, [vp, C.POINTER(C.c_int)] + [C.POINTER(C.c_int)] * 4 + [C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -366,6 +367,14 @@ class Batch:
         c = C.c_long()
         self._check(self.lib.fvgpu_batch_launch_count(self._h, C.byref(c)), "batch_launch_count")
         return c.value
+
+    def schedule(self):
+        """[{tx, rows, block_rows, split_viscous}] the autotuner chose per group."""
+        ng = C.c_int()
+        arrs = [(C.c_int * 8)() for _ in range(4)]
+        self._check(self.lib.fvgpu_batch_schedule(self._h, C.byref(ng), *arrs, 8), "batch_schedule")
+        keys = ("tx", "rows", "block_rows", "split_viscous")
+        return [{k: a[g] for k, a in zip(keys, arrs)} for g in range(ng.value)]
 
     def tiling(self):
         """[(tx, ty)] tile shape chosen per group."""

@@ -150,8 +150,15 @@ bool WithPrimCopy(const fv_batch* b, int i) {
 
 // ---- tile-shape cache --------------------------------------------------
 
+// A group's schedule: strip width, rows per work item, and for the
+// FP32-mixed kernels the rows per marched block (cells per thread) and the
+// viscous form (1: per-face pass, 0: fused per cell).
+struct Schedule {
+  int tx = 0, rows = 0, block_rows = 16, vface = 0;
+};
+
 std::mutex g_cache_mutex;
-std::map<std::string, std::pair<int, int>> g_cache;
+std::map<std::string, Schedule> g_cache;
 bool g_cache_loaded = false;
 
 std::string CachePath() {
@@ -169,10 +176,24 @@ void LoadCache() {
   std::ifstream in(CachePath());
   std::string key;
   int tx, ty;
-  while (in >> key >> tx >> ty) g_cache[key] = {tx, ty};
+  // lines: key tx rows [block_rows vface]
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    Schedule sc;
+    if (!(ls >> key >> sc.tx >> sc.rows)) continue;
+    int br = 0, vf = 0;
+    if (ls >> br >> vf) {
+      sc.block_rows = br;
+      sc.vface = vf;
+    }
+    g_cache[key] = sc;
+  }
+  (void)tx;
+  (void)ty;
 }
 
-void SaveCacheEntry(const std::string& key, int tx, int ty) {
+void SaveCacheEntry(const std::string& key, const Schedule& sc) {
   const std::string path = CachePath();
   if (path.empty()) return;
   const std::string dir = path.substr(0, path.find_last_of('/'));
@@ -180,7 +201,7 @@ void SaveCacheEntry(const std::string& key, int tx, int ty) {
   mkdir(parent.c_str(), 0755);
   mkdir(dir.c_str(), 0755);
   std::ofstream out(path, std::ios::app);
-  if (out) out << key << " " << tx << " " << ty << "\n";
+  if (out) out << key << " " << sc.tx << " " << sc.rows << " " << sc.block_rows << " " << sc.vface << "\n";
 }
 
 // Key of a group: precision, plane, layout, conduction, solver mix and the
@@ -210,6 +231,24 @@ std::string GroupKey(const fv_batch* b, const Group& g) {
 
 int NumShapes(int precision, const fv::TileShape** shapes) {
   return precision == FV_PREC_FP64 ? fv::batch_tile_shapes64(shapes) : fv::batch_tile_shapes32(shapes);
+}
+
+// The schedule a shape stands for (rows: the shape's own).  FP64 kernels:
+// blocks of 512 cells, viscous fluxes of the face-only branches shared per
+// face (fv_tile64.cuh).
+Schedule ShapeSchedule(const fv_batch* b, int shape) {
+  const fv::TileShape* shapes;
+  NumShapes(b->precision, &shapes);
+  Schedule sc;
+  sc.tx = shapes[shape].tx;
+  sc.rows = shapes[shape].ty;
+  if (b->precision == FV_PREC_FP64) {
+    sc.block_rows = 512 / sc.tx;
+    sc.vface = 1;
+  } else {
+    fv::batch_shape_kernel32(shape, &sc.block_rows, &sc.vface);
+  }
+  return sc;
 }
 
 int Occupancy(const fv_batch* b, const Group& g, int shape) {
@@ -287,21 +326,39 @@ int Autotune(fv_batch* b, Group& g) {
   }
   const fv::TileShape* shapes;
   const int ns = NumShapes(b->precision, &shapes);
-  // the first shape of a strip width (its kernel serves every row count)
-  auto shape_of_tx = [&](int tx) {
-    for (int s = 0; s < ns; ++s)
-      if (shapes[s].tx == tx && Occupancy(b, g, s) > 0) return s;
+  bool visc = false;  // the viscous form matters only with viscosity
+  for (int i : g.members) visc = visc || b->G[i].visc;
+  // the first shape of a kernel (it serves every row count): strip width,
+  // block rows and viscous form
+  auto shape_of = [&](const Schedule& sc) {
+    for (int s = 0; s < ns; ++s) {
+      const Schedule k = ShapeSchedule(b, s);
+      if (k.tx == sc.tx && k.block_rows == sc.block_rows && k.vface == sc.vface && Occupancy(b, g, s) > 0) return s;
+    }
     return -1;
   };
-  if (const char* force = std::getenv("FV3D_TILE")) {
-    int tx = 0, ty = 0;
-    if (std::sscanf(force, "%dx%d", &tx, &ty) == 2 && ty > 0) {
-      const int s = shape_of_tx(tx);
-      if (s >= 0) {
-        g.shape = s;
-        g.rows = ty;
-        return FV_OK;
+  auto take = [&](const Schedule& sc) {
+    const int s = shape_of(sc);
+    if (s < 0) return false;
+    g.shape = s;
+    g.rows = sc.rows;
+    return true;
+  };
+  if (const char* force = std::getenv("FV3D_TILE")) {  // WxH, WxH/B, WxHv, WxH/Bv
+    Schedule sc;
+    char rest[16] = "";
+    const int got = std::sscanf(force, "%dx%d%15s", &sc.tx, &sc.rows, rest);
+    if (got >= 2 && sc.rows > 0) {
+      char* r = rest;
+      if (*r == '/') sc.block_rows = (int)std::strtol(r + 1, &r, 10);
+      sc.vface = *r == 'v' ? 1 : 0;
+      if (b->precision == FV_PREC_FP64) {  // one kernel per strip width
+        const int rows = sc.rows;
+        for (int s = 0; s < ns; ++s)
+          if (shapes[s].tx == sc.tx) sc = ShapeSchedule(b, s);
+        sc.rows = rows;
       }
+      if (take(sc)) return FV_OK;
     }
   }
   const std::string key = GroupKey(b, g);
@@ -309,29 +366,24 @@ int Autotune(fv_batch* b, Group& g) {
     std::lock_guard<std::mutex> lock(g_cache_mutex);
     LoadCache();
     auto it = g_cache.find(key);
-    if (it != g_cache.end() && it->second.second > 0) {
-      const int s = shape_of_tx(it->second.first);
-      if (s >= 0) {
-        g.shape = s;
-        g.rows = it->second.second;
-        return FV_OK;
-      }
-    }
+    if (it != g_cache.end() && it->second.rows > 0 && take(it->second)) return FV_OK;
   }
   // Candidates: every shape with its own rows, and per strip width the rows
   // that give each resident CTA one work item's worth of strip rows (the
   // balanced split for a few large problems).
   std::vector<std::pair<int, int>> cand;
-  for (int s = 0; s < ns; ++s) cand.push_back({s, shapes[s].ty});
+  for (int s = 0; s < ns; ++s)
+    if (visc || !ShapeSchedule(b, s).vface || b->precision == FV_PREC_FP64) cand.push_back({s, shapes[s].ty});
   for (int s = 0; s < ns; ++s) {
-    if (shape_of_tx(shapes[s].tx) != s) continue;
+    const Schedule ks = ShapeSchedule(b, s);
+    if ((ks.vface && !visc && b->precision != FV_PREC_FP64) || shape_of(ks) != s) continue;
     long long units = 0;
     for (int i : g.members) units += (long long)((b->G[i].na + shapes[s].tx - 1) / shapes[s].tx) * b->G[i].nb;
     const long long slots = (long long)Occupancy(b, g, s) * SmCount();
     if (slots <= 0) continue;
     const int rows = (int)std::max(4LL, (units + slots - 1) / slots);
     bool dup = false;
-    for (auto& c : cand) dup = dup || (shapes[c.first].tx == shapes[s].tx && c.second == rows);
+    for (auto& c : cand) dup = dup || (shape_of(ShapeSchedule(b, c.first)) == s && c.second == rows);
     if (!dup) cand.push_back({s, rows});
   }
   StepCtrl* tune_ctrl = nullptr;
@@ -420,9 +472,11 @@ int Autotune(fv_batch* b, Group& g) {
   int best_c = -1;
   const bool log = std::getenv("FV3D_TILE_LOG") != nullptr;
   for (size_t c = 0; c < cand.size(); ++c) {
-    if (log)
-      std::fprintf(stderr, "fv3d tile candidate %dx%d: %.4f ms (%d items, %d CTAs)\n", shapes[cand[c].first].tx,
-                   cand[c].second, grid[c] ? best_ms[c] : -1.0f, ntiles[c], grid[c]);
+    if (log) {
+      const Schedule k = ShapeSchedule(b, cand[c].first);
+      std::fprintf(stderr, "fv3d tile candidate %dx%d/%d%s: %.4f ms (%d items, %d CTAs)\n", k.tx, cand[c].second,
+                   k.block_rows, k.vface ? "v" : "", grid[c] ? best_ms[c] : -1.0f, ntiles[c], grid[c]);
+    }
     if (grid[c] && best_ms[c] < best) {
       best = best_ms[c];
       best_c = (int)c;
@@ -444,8 +498,10 @@ int Autotune(fv_batch* b, Group& g) {
   cudaEventDestroy(e1);
   if (best_c < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
   std::lock_guard<std::mutex> lock(g_cache_mutex);
-  g_cache[key] = {shapes[g.shape].tx, g.rows};
-  SaveCacheEntry(key, shapes[g.shape].tx, g.rows);
+  Schedule chosen = ShapeSchedule(b, g.shape);
+  chosen.rows = g.rows;
+  g_cache[key] = chosen;
+  SaveCacheEntry(key, chosen);
   return FV_OK;
 }
 
@@ -510,6 +566,7 @@ bool MultiEligible(const fv_batch* b) {
   if (b->precision != FV_PREC_FP32_MIXED || b->ts != FV_TS_RK2 || b->groups.size() != 1) return false;
   const Group& g = b->groups[0];
   if (g.ndim != 2 || (int)g.members.size() > fv::batch_multi_problems32()) return false;
+  if (ShapeSchedule(b, g.shape).vface) return false;  // multi-step kernels: the fused viscous form
   const char* env = std::getenv("FV3D_MULTISTEP");
   if (env && env[0] == '0') return false;
   long long cells = 0;
@@ -880,6 +937,33 @@ int fvgpu_batch_synchronize(fv_batch* b) {
 int fvgpu_batch_launch_count(const fv_batch* b, long* count) {
   if (!b || !count) return FV_ERR_PARAM;
   *count = b->launches;
+  return FV_OK;
+}
+
+int fvgpu_batch_schedule(fv_batch* b, int* ngroups, int* tx, int* rows, int* block_rows, int* split_viscous,
+                         int max_groups) {
+  if (!b || !ngroups) return FV_ERR_PARAM;
+  for (int i = 0; i < b->n; ++i)
+    if (!b->state_set[i]) return Fail(b, FV_ERR_STATE, "problem %d has no state", i);
+  int rc = Prepare(b);
+  if (rc) return rc;
+  *ngroups = (int)b->groups.size();
+  for (int gi = 0; gi < *ngroups && gi < max_groups; ++gi) {
+    const Group& g = b->groups[gi];
+    Schedule sc;
+    if (g.ndim == 3) {  // column blocks of 16 x 16 marched over z chunks
+      sc.tx = sc.rows = fv::batch3d_columns();
+      sc.block_rows = 0;
+      sc.vface = b->precision == FV_PREC_FP64 ? 1 : 0;
+    } else {
+      sc = ShapeSchedule(b, g.shape);
+      if (g.rows > 0) sc.rows = g.rows;
+    }
+    if (tx) tx[gi] = sc.tx;
+    if (rows) rows[gi] = sc.rows;
+    if (block_rows) block_rows[gi] = sc.block_rows;
+    if (split_viscous) split_viscous[gi] = sc.vface;
+  }
   return FV_OK;
 }
 

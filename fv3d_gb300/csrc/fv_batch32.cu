@@ -11,13 +11,19 @@ namespace fv {
 
 namespace {
 
-// Work-item shapes (cells along a x rows along b) the autotuner starts from:
-// strip segments marched in blocks of 16 rows (32x16 or 64x16 cells); the
-// rows of an item are a run-time value (BatchInst::tz), so shapes of one
-// strip width share a kernel (kKernelOf32).
-constexpr TileShape kShapes32[] = {{32, 32}, {64, 16}, {32, 16}, {64, 32}};
-constexpr int kBlockRows32[] = {16, 16, 16, 16};
-constexpr int kKernelOf32[] = {0, 1, 0, 1};
+// Work-item shapes (cells along a x rows along b) the autotuner starts
+// from, each with the kernel that marches it: strip segments marched in
+// blocks of 16 or 8 rows (cells per thread in the update: 32x16 -> 2,
+// 64x16 -> 4, 32x8 -> 1, 64x8 -> 2), with the viscous fluxes fused per cell
+// or split into a per-face pass (VF).  The rows of an item are a run-time
+// value (BatchInst::tz), so shapes of one kernel differ only in their
+// starting rows.
+struct MixedKernel {
+  int tx, block_rows, vface;
+};
+constexpr MixedKernel kKernels32[] = {{32, 16, 0}, {64, 16, 0}, {32, 8, 0}, {64, 8, 0}, {32, 16, 1}, {64, 16, 1}};
+constexpr TileShape kShapes32[] = {{32, 32}, {64, 16}, {32, 16}, {64, 32}, {32, 16}, {64, 8}, {32, 32}, {64, 16}};
+constexpr int kKernelOf32[] = {0, 1, 0, 1, 2, 3, 4, 5};
 constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
 
 // Copies the descriptor of the problem holding work item t to s_inst and
@@ -46,7 +52,7 @@ __device__ __forceinline__ int fetch_inst32(const BatchInst* __restrict__ insts,
 // the problem's step in flight; slot_next / err: its CFL maximum slot for the
 // next step and its error flag (stages that end a step).  Every thread of
 // the CTA calls it; s_inst holds I.
-template <int PLANE, bool WACT, class TL>
+template <int PLANE, bool WACT, class TL, bool VF>
 __device__ __forceinline__ void stage_item32(const BatchInst& I, int t, int kind, int flip, bool active, double dt_step,
                                              unsigned long long* slot_next, int* err, float* smem,
                                              unsigned long long* s_red) {
@@ -73,14 +79,14 @@ __device__ __forceinline__ void stage_item32(const BatchInst& I, int t, int kind
   const float dt = (float)dt_step;  // the one FP64 -> FP32 conversion per item
   float red = 0.0f;
   bool bad = false;
-  stage_segment32<PLANE, WACT, TL>(I.G, M, src, dst, I.rs, kind, dt, x0, ya, yb, smem, red, bad);
+  stage_segment32<PLANE, WACT, TL, VF>(I.G, M, src, dst, I.rs, kind, dt, x0, ya, yb, smem, red, bad);
   if (kind != STAGE_RK_1) {
     if (bad) atomicOr(err, 1);
     block_max_atomic((unsigned long long)__double_as_longlong((double)red), slot_next, s_red);
   }
 }
 
-template <int PLANE, bool WACT, class TL>
+template <int PLANE, bool WACT, class TL, bool VF>
 __global__ void FV_MIXED_BOUNDS
 batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ float smem_f[];
@@ -100,7 +106,7 @@ batch_stage32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsign
     fetch_inst32(insts, ninst, t, &s_inst);
     __syncthreads();
     StepCtrl* ctrl = s_inst.ctrl;
-    stage_item32<PLANE, WACT, TL>(s_inst, t, kind, flip, ctrl->active != 0, ctrl->dt_cur,
+    stage_item32<PLANE, WACT, TL, VF>(s_inst, t, kind, flip, ctrl->active != 0, ctrl->dt_cur,
                                   &ctrl->slot[ctrl->parity ^ 1], &ctrl->err, smem_f, s_red);
   }
 }
@@ -180,7 +186,7 @@ __global__ void FV_MIXED_BOUNDS batch_multi32(const BatchInst* __restrict__ inst
         const int m = fetch_inst32(insts, ninst, t, &s_inst);
         __syncthreads();
         StepCtrl* ctrl = s_inst.ctrl;
-        stage_item32<PLANE, WACT, TL>(s_inst, t, kind, 0, s_act[m] != 0, s_dt[m], &ctrl->slot[s_par[m] ^ 1],
+        stage_item32<PLANE, WACT, TL, false>(s_inst, t, kind, 0, s_act[m] != 0, s_dt[m], &ctrl->slot[s_par[m] ^ 1],
                                       &ctrl->err, smem_f, s_red);
       }
       if (!grid_sync(gb, bar++)) {
@@ -204,17 +210,18 @@ __global__ void FV_MIXED_BOUNDS batch_multi32(const BatchInst* __restrict__ inst
   }
 }
 
-template <int S>
-using BlockOf32 = Tile<kShapes32[S].tx, kBlockRows32[S]>;
+template <int K>
+using BlockOf32 = Tile<kKernels32[K].tx, kKernels32[K].block_rows>;
 
-template <int PLANE, bool WACT, int S>
+template <int PLANE, bool WACT, int K>
 auto kernel_for() {
-  return batch_stage32<PLANE, WACT, BlockOf32<S>>;
+  return batch_stage32<PLANE, WACT, BlockOf32<K>, kKernels32[K].vface != 0>;
 }
 
-template <int S>
+template <int K>
 size_t smem_for(bool wact, bool tc) {
-  return wact ? TileSmem<float, 5, BlockOf32<S>>::bytes(tc) : TileSmem<float, 4, BlockOf32<S>>::bytes(tc);
+  if (kKernels32[K].vface && wact) return TileSmem<float, 5, BlockOf32<K>>::bytes_vface();
+  return wact ? TileSmem<float, 5, BlockOf32<K>>::bytes(tc) : TileSmem<float, 4, BlockOf32<K>>::bytes(tc);
 }
 
 typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
@@ -222,8 +229,13 @@ typedef void (*BatchKernel)(const BatchInst*, int, int, unsigned*, int, int);
 typedef void (*MultiKernel)(const BatchInst*, int, int, int, int, GridBarrier);
 
 template <int PLANE, bool WACT>
-MultiKernel pick_multi(int shape) {
-  return kKernelOf32[shape] == 0 ? batch_multi32<PLANE, WACT, BlockOf32<0>> : batch_multi32<PLANE, WACT, BlockOf32<1>>;
+MultiKernel pick_multi(int shape) {  // fused viscous form only (shapes of kernels 0-3)
+  switch (kKernelOf32[shape]) {
+    case 0: return batch_multi32<PLANE, WACT, BlockOf32<0>>;
+    case 1: return batch_multi32<PLANE, WACT, BlockOf32<1>>;
+    case 2: return batch_multi32<PLANE, WACT, BlockOf32<2>>;
+    default: return batch_multi32<PLANE, WACT, BlockOf32<3>>;
+  }
 }
 
 MultiKernel pick_multi_any(int plane, bool wact, int shape) {
@@ -233,7 +245,14 @@ MultiKernel pick_multi_any(int plane, bool wact, int shape) {
 
 template <int PLANE, bool WACT>
 BatchKernel pick(int shape) {
-  return kKernelOf32[shape] == 0 ? kernel_for<PLANE, WACT, 0>() : kernel_for<PLANE, WACT, 1>();
+  switch (kKernelOf32[shape]) {
+    case 0: return kernel_for<PLANE, WACT, 0>();
+    case 1: return kernel_for<PLANE, WACT, 1>();
+    case 2: return kernel_for<PLANE, WACT, 2>();
+    case 3: return kernel_for<PLANE, WACT, 3>();
+    case 4: return kernel_for<PLANE, WACT, 4>();
+    default: return kernel_for<PLANE, WACT, 5>();
+  }
 }
 
 BatchKernel pick_any(int plane, bool wact, int shape) {
@@ -242,11 +261,13 @@ BatchKernel pick_any(int plane, bool wact, int shape) {
 }
 
 size_t smem_any(int shape, bool wact, bool tc) {
-  switch (shape) {
+  switch (kKernelOf32[shape]) {
     case 0: return smem_for<0>(wact, tc);
     case 1: return smem_for<1>(wact, tc);
     case 2: return smem_for<2>(wact, tc);
-    default: return smem_for<3>(wact, tc);
+    case 3: return smem_for<3>(wact, tc);
+    case 4: return smem_for<4>(wact, tc);
+    default: return smem_for<5>(wact, tc);
   }
 }
 
@@ -333,6 +354,14 @@ __global__ void double_from_pairs(const Grid G, const Fields src, const Fields d
 int batch_tile_shapes32(const TileShape** shapes) {
   *shapes = kShapes32;
   return kNumShapes32;
+}
+
+int batch_shape_kernel32(int shape, int* block_rows, int* vface) {
+  if (shape < 0 || shape >= kNumShapes32) return -1;
+  const MixedKernel& k = kKernels32[kKernelOf32[shape]];
+  if (block_rows) *block_rows = k.block_rows;
+  if (vface) *vface = k.vface;
+  return kKernelOf32[shape];
 }
 
 int batch_stage_occupancy32(int plane, bool wact, int shape, bool tc) {

@@ -163,6 +163,10 @@ struct TileShape {
 };
 int batch_tile_shapes64(const TileShape** shapes);
 int batch_tile_shapes32(const TileShape** shapes);
+// The kernel of FP32-mixed shape `shape`: its index (shapes of one kernel
+// differ only in their starting rows), its block rows (8 or 16) and whether
+// it computes the viscous fluxes in a per-face pass (1) or per cell (0).
+int batch_shape_kernel32(int shape, int* block_rows, int* vface);
 
 // Persistent stage kernel over a group of problems sharing plane and third
 // momentum: `grid` CTAs pull tiles from the work-queue counter *queue (reset

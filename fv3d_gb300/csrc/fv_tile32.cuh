@@ -391,7 +391,10 @@ __device__ __forceinline__ void faces32(const Grid& G, const PV& V, int rs, int 
 //   STAGE_RK_1 : read U^n (pairs) -> write U* (FP32)
 //   STAGE_RK_2 : read U* (FP32) and U^n (pairs) -> write U^n+1 (pairs, over U^n)
 //   STAGE_EULER: read U^n (pairs in `src`) -> write U^n+1 (pairs in `dst`)
-template <int PLANE, bool WACT, class TL, class PV>
+// VF: the viscous fluxes of the face-only branches come from the shared face
+// arrays visc_faces filled (the split form), else every cell evaluates its
+// stencil (the fused form).
+template <int PLANE, bool WACT, class TL, bool VF, class PV>
 __device__ __forceinline__ void update32(const Grid& G, const PV& V, const MixedFields& M, float2* const src[5],
                                          float2* const dst[5], int kind, float dt, int x0, int y0, int nr, int tid,
                                          float& red, bool& bad) {
@@ -449,12 +452,16 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
       du[4] += dtdx * (FR - FL) + dtdb * (FD - FU);
     }
     if (WACT && G.visc) {
-      // per cell: the shared-face form (viscous_face) needs 17 KB more shared
-      // memory per CTA, which costs this issue-bound kernel a resident CTA
-      // per SM and measured 5-14 % slower
-      PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
+      // fused: every cell evaluates its stencil; split: the face-only
+      // branches once per face (17 KB more shared memory per CTA, so fewer
+      // resident CTAs: the autotuner chooses per group)
       float vf[3][5];
-      viscous_plane<PLANE, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
+      if (VF) {
+        visc_cell_shared<PLANE>(V, cy, cx, G.inv_dx_f, G.inv_dz_f, G.mu_f, vf);
+      } else {
+        PlaneVel<PLANE, PV> P{V, cy + 2, cx + 2};
+        viscous_plane<PLANE, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
+      }
 #pragma unroll
       for (int var = 1; var < 5; ++var) {
         const int sv = var == 4 ? 4 : phys_slot<PLANE>(var);
@@ -522,8 +529,9 @@ __device__ __forceinline__ void carry_rows32(const Grid& G, const SM& S, int tid
 // boundary are reused), the arithmetic of every face and cell that of the
 // tile form.  Every thread of the CTA calls it; the CFL maximum and the
 // non-finite flag are folded into red / bad; smem holds
-// TileSmem<float, NV, TL>::bytes(G.tc) bytes.
-template <int PLANE, bool WACT, class TL>
+// TileSmem<float, NV, TL>::bytes(G.tc) bytes, or bytes_vface() for the split
+// viscous form (VF, update32).
+template <int PLANE, bool WACT, class TL, bool VF>
 __device__ __forceinline__ void stage_segment32(const Grid& G, const MixedFields& M, float2* const src[5],
                                                 float2* const dst[5], int rs, int kind, float dt, int x0, int ya,
                                                 int yb, float* smem, float& red, bool& bad) {
@@ -543,13 +551,20 @@ __device__ __forceinline__ void stage_segment32(const Grid& G, const MixedFields
         const int sv = NV == 5 ? v : (v == 3 ? 4 : v);
         S.fb(sv, 0, fx) = S.fb(sv, TY, fx);
       }
+      if (VF && WACT && G.visc && PLANE == PLANE_XY)  // and their viscous fluxes
+        for (int i = tid; i < 4 * TX; i += kTileThreads) {
+          const int k = i / TX, fx = i - k * TX;
+          S.vb(k, 0, fx) = S.vb(k, TY, fx);
+        }
       carry_rows32<WACT, TL>(G, S, tid);
     }
     load_prims32<PLANE, WACT, TL>(G, M, src, in_pairs, V, x0, y0, first ? 0 : 4, nr + 4, tid);
     __syncthreads();
     faces32<PLANE, WACT, TL>(G, V, rs, nr, first ? 0 : 1, tid);
+    if (VF && WACT && G.visc)
+      visc_faces<PLANE, TL>(V, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, nr, first ? 0 : 1, tid);
     __syncthreads();
-    update32<PLANE, WACT, TL>(G, V, M, src, dst, kind, dt, x0, y0, nr, tid, red, bad);
+    update32<PLANE, WACT, TL, VF>(G, V, M, src, dst, kind, dt, x0, y0, nr, tid, red, bad);
     __syncthreads();
   }
 }

@@ -274,6 +274,18 @@ int fvgpu_batch_launch_count(const fv_batch* b, long* count);
  * candidate shape (the state is saved and restored around it); FV3D_TILE=WxH
  * forces a shape, FV3D_TILE_LOG=1 prints each candidate's time to stderr. */
 int fvgpu_batch_tiling(fv_batch* b, int* ngroups, int* tx, int* ty, int max_groups);
+/* The full schedule the autotuner chose per group (arrays of max_groups,
+ * any may be NULL): strip width tx and rows per work item (as
+ * fvgpu_batch_tiling), the rows of one marched block (cells per thread in
+ * the update: tx x block_rows / 256; 3-D groups: 0) and whether the viscous
+ * fluxes of the face-only branches are computed once per face in a separate
+ * pass (1) or fused into each cell's update (0).  The FP32-mixed kernels
+ * offer 8- and 16-row blocks and both viscous forms, tuned per (grid sizes,
+ * precision, group) and remembered in the tile cache; FV3D_TILE=WxH/Bv
+ * forces width W, rows H, block rows B and (suffix v) the per-face form.
+ * No reference counterpart. */
+int fvgpu_batch_schedule(fv_batch* b, int* ngroups, int* tx, int* rows, int* block_rows, int* split_viscous,
+                         int max_groups);
 
 #ifdef __cplusplus
 }

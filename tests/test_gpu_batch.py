@@ -15,7 +15,7 @@ import pytest
 
 import fv3d_gb300 as fv
 from fv3d_gb300 import problems
-from _helpers import assert_mixed
+from _helpers import assert_mixed, rel_l1_fields
 
 pytestmark = pytest.mark.gpu
 
@@ -241,3 +241,90 @@ def test_batch_rejects_mixed_settings():
     with pytest.raises(fv.FvError) as e:
         fv.Batch([a, c])
     assert e.value.status == 2
+
+
+def _schedule_set():
+    """Both planes, with and without viscosity (three groups)."""
+    return [problems.rayleigh_taylor(48, 144, kappa=1e-3, mu=1e-3, tend=1.0e30),
+            problems.thermal_pulse(80),
+            problems.sod(70, "x", gamma=1.3, nx_other=45)]
+
+
+def _run_forced(probs, tile, nsteps, monkeypatch):
+    monkeypatch.setenv("FV3D_TILE", tile)
+    params = []
+    for pr in probs:
+        q = pr.params.copy()
+        q.precision = fv._abi.FV_PREC_FP32_MIXED
+        params.append(q)
+    b = fv.Batch(params)
+    for i, pr in enumerate(probs):
+        b.set_prim(i, *pr.prim)
+    sched = b.schedule()
+    b.run(nsteps)
+    out = [b.get_prim(i) for i in range(len(probs))], b.times()
+    b.close()
+    return sched, out
+
+
+@pytest.mark.parametrize("tile,block,split", [("32x16/8", 8, 0), ("64x24/8", 8, 0), ("32x40/16", 16, 0),
+                                              ("32x16v", 16, 1), ("64x20v", 16, 1)])
+def test_mixed_schedules(tile, block, split, monkeypatch):
+    """Every mixed schedule -- blocks of 8 or 16 rows (one to four cells per
+    thread in the update), viscous fluxes fused per cell or computed once per
+    face -- is reported by fvgpu_batch_schedule and gives the same flow:
+    bit for bit across block sizes of one viscous form, to FP32 rounding
+    across the two forms (relative L1 <= 1e-6 on density and pressure,
+    velocities within 1e-6 of the signal speed)."""
+    probs = _schedule_set()
+    nsteps = 12
+    sched, (got, t) = _run_forced(probs, tile, nsteps, monkeypatch)
+    tx, rows = (int(x) for x in tile.rstrip("v").split("/")[0].split("x"))
+    assert len(sched) == 3
+    for s in sched:
+        assert (s["tx"], s["rows"], s["block_rows"], s["split_viscous"]) == (tx, rows, block, split)
+    base_sched, (ref, t_ref) = _run_forced(probs, "32x16", nsteps, monkeypatch)
+    assert all(s["block_rows"] == 16 and s["split_viscous"] == 0 for s in base_sched)
+    for i, pr in enumerate(probs):
+        if split == 0 or not pr.params.viscosity_active:
+            np.testing.assert_array_equal(t[i], t_ref[i])
+            for k in range(5):
+                np.testing.assert_array_equal(got[i][k], ref[i][k], err_msg="%s %d" % (pr.name, k))
+        else:
+            errs = rel_l1_fields(got[i], ref[i])
+            assert errs[0] <= 1e-6 and errs[4] <= 1e-6, (pr.name, errs)
+            c = np.sqrt(pr.params.gamma0 * ref[i][4] / ref[i][0])
+            speed = float((np.sqrt(ref[i][1] ** 2 + ref[i][2] ** 2 + ref[i][3] ** 2) + c).max())
+            for k in (1, 2, 3):
+                assert float(np.abs(got[i][k] - ref[i][k]).mean()) <= 1e-6 * speed, (pr.name, k)
+
+
+def test_autotuned_schedule_is_cached(tmp_path, monkeypatch):
+    """A fresh tuning records width, rows, block rows and viscous form per
+    group in the tile cache, and a new batch of the same problems takes the
+    recorded schedule."""
+    cache = tmp_path / "tiles.txt"
+    monkeypatch.delenv("FV3D_TILE", raising=False)
+    code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "import fv3d_gb300 as fv\n"
+            "from test_gpu_batch import _schedule_set\n"
+            "probs = _schedule_set()\n"
+            "ps = []\n"
+            "for p in probs:\n"
+            "    q = p.params.copy(); q.precision = 1; ps.append(q)\n"
+            "b = fv.Batch(ps)\n"
+            "[b.set_prim(i, *p.prim) for i, p in enumerate(probs)]\n"
+            "print([tuple(s.values()) for s in b.schedule()])\n") % (
+        os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FV3D_TILE_CACHE=str(cache))
+    env.pop("FV3D_TILE", None)
+    first = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert first.returncode == 0, first.stderr[-2000:]
+    lines = [l.split() for l in cache.read_text().splitlines() if l.strip()]
+    assert len(lines) == 3 and all(len(l) == 5 for l in lines)
+    recorded = sorted(tuple(int(x) for x in l[1:]) for l in lines)
+    again = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert again.returncode == 0, again.stderr[-2000:]
+    assert again.stdout == first.stdout
+    assert sorted(eval(first.stdout.strip().splitlines()[-1])) == recorded
+    assert len(cache.read_text().splitlines()) == 3  # nothing tuned the second time
