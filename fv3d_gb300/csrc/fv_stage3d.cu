@@ -36,6 +36,11 @@ constexpr int kMinLayersPerCta = 8;              // the prologue loads 4 layers 
 constexpr int kThreads = kTX * kTY;              // one thread per column
 constexpr int kHX = kTX + 4, kHY = kTY + 4;      // layer with halo
 constexpr int kLayer = kHX * kHY;
+// Resident CTAs per SM the register allocation of the 3-D FP64 kernels
+// targets.
+#ifndef FV_3D64_MIN_CTAS
+#define FV_3D64_MIN_CTAS 2
+#endif
 constexpr int kRing = 4;                         // z layers held
 constexpr int kNFA = (kTX + 1) * kTY;            // x faces per layer
 constexpr int kNFA_PAD = (kNFA + 31) / 32 * 32;  // keeps each warp on one face kind
@@ -603,7 +608,7 @@ __device__ __forceinline__ unsigned long long march3d(const Grid& G, const Field
 // block by column block, are split evenly over the CTAs that fit on the GPU
 // at once; a CTA marches each column block of its range over its layers.
 template <int RS, int KIND, bool CORR>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, FV_3D64_MIN_CTAS)
 stage3d_fp64(const Grid G, const Fields uin, const Fields u0, const Fields uout, StepCtrl* __restrict__ ctrl,
              long long units, const Fields hout, const Fields qin, const Fields qout) {
   extern __shared__ double smem_raw[];
@@ -687,7 +692,7 @@ static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
 // their problem by binary search over the first item numbers, and run the
 // same body as the one-problem kernel.
 template <int KIND, int RS>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, FV_3D64_MIN_CTAS)
 batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int flip) {
   const int kind = KIND;
   extern __shared__ double smem_raw[];
