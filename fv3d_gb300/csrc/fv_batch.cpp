@@ -211,7 +211,7 @@ std::string GroupKey(const fv_batch* b, const Group& g) {
   int rs_mask = 0;
   bool visc = false;
   for (int i : g.members) {
-    sizes.push_back({b->G[i].na, b->G[i].nb});
+    sizes.push_back({b->G[i].na, b->G[i].nb * b->G[i].nc});
     rs_mask |= 1 << (b->p[i].riemann_solver == FV_HLL ? 0 : 1);
     visc = visc || b->G[i].visc;
   }
@@ -224,7 +224,7 @@ std::string GroupKey(const fv_batch* b, const Group& g) {
     cells += (long long)s.first * s.second;
   }
   std::ostringstream k;
-  k << "p" << b->precision << "_pl" << g.plane << "_w" << g.wact << "_tc" << g.tc << "_v" << visc << "_rs"
+  k << "p" << b->precision << "_d" << g.ndim << "_pl" << g.plane << "_w" << g.wact << "_tc" << g.tc << "_v" << visc << "_rs"
     << rs_mask << "_ts" << b->ts << "_n" << g.members.size() << "_c" << cells << "_h" << std::hex << h;
   return k.str();
 }
@@ -248,6 +248,17 @@ Schedule ShapeSchedule(const fv_batch* b, int shape) {
   } else {
     fv::batch_shape_kernel32(shape, &sc.block_rows, &sc.vface);
   }
+  return sc;
+}
+
+// The schedule of a 3-D group: 16 x 16 column blocks, z layers per work item;
+// the FP64 kernel shares the x / y faces' viscous fluxes.
+Schedule Schedule3d(const fv_batch* b, int layers) {
+  Schedule sc;
+  sc.tx = fv::batch3d_columns();
+  sc.rows = layers > 0 ? layers : 16;
+  sc.block_rows = 0;
+  sc.vface = b->precision == FV_PREC_FP64 ? 1 : 0;
   return sc;
 }
 
@@ -295,7 +306,7 @@ std::vector<BatchInst> Describe(const fv_batch* b, const Group& g, int shape, St
     I.ctrl = ctrl_base + i;
     I.tiles_x = (I.G.na + tx - 1) / tx;
     I.tiles_y = (I.G.nb + ty - 1) / ty;
-    I.tz = g.ndim == 3 ? std::min(I.G.nc, 16) : ty;
+    I.tz = g.ndim == 3 ? std::min(I.G.nc, rows > 0 ? rows : 16) : ty;  // 3-D: z layers per item
     const int chunks = g.ndim == 3 ? (I.G.nc + I.tz - 1) / I.tz : 1;
     I.tile0 = t0;
     I.rs = b->p[i].riemann_solver == FV_HLL ? 0 : 1;
@@ -320,17 +331,16 @@ int SmCount() {
 // room for that copy only stage 1 is timed.  The problems' state and clocks
 // are left as they were, and the tuning descriptors carry no primitive copy.
 int Autotune(fv_batch* b, Group& g) {
-  if (g.ndim == 3) {  // one shape: the 16 x 16 column kernel
-    g.shape = 0;
-    return Occupancy(b, g, 0) > 0 ? FV_OK : Fail(b, FV_ERR_CUDA, "the 3-D batch kernel cannot be launched");
-  }
+  const bool d3 = g.ndim == 3;  // one kernel: 16 x 16 column blocks; tuned: z layers per item
+  if (d3 && Occupancy(b, g, 0) <= 0) return Fail(b, FV_ERR_CUDA, "the 3-D batch kernel cannot be launched");
   const fv::TileShape* shapes;
-  const int ns = NumShapes(b->precision, &shapes);
+  const int ns = d3 ? 1 : NumShapes(b->precision, &shapes);
   bool visc = false;  // the viscous form matters only with viscosity
   for (int i : g.members) visc = visc || b->G[i].visc;
   // the first shape of a kernel (it serves every row count): strip width,
   // block rows and viscous form
   auto shape_of = [&](const Schedule& sc) {
+    if (d3) return sc.tx == fv::batch3d_columns() ? 0 : -1;
     for (int s = 0; s < ns; ++s) {
       const Schedule k = ShapeSchedule(b, s);
       if (k.tx == sc.tx && k.block_rows == sc.block_rows && k.vface == sc.vface && Occupancy(b, g, s) > 0) return s;
@@ -352,7 +362,9 @@ int Autotune(fv_batch* b, Group& g) {
       char* r = rest;
       if (*r == '/') sc.block_rows = (int)std::strtol(r + 1, &r, 10);
       sc.vface = *r == 'v' ? 1 : 0;
-      if (b->precision == FV_PREC_FP64) {  // one kernel per strip width
+      if (d3) {
+        sc = Schedule3d(b, sc.rows);
+      } else if (b->precision == FV_PREC_FP64) {  // one kernel per strip width
         const int rows = sc.rows;
         for (int s = 0; s < ns; ++s)
           if (shapes[s].tx == sc.tx) sc = ShapeSchedule(b, s);
@@ -372,9 +384,14 @@ int Autotune(fv_batch* b, Group& g) {
   // that give each resident CTA one work item's worth of strip rows (the
   // balanced split for a few large problems).
   std::vector<std::pair<int, int>> cand;
-  for (int s = 0; s < ns; ++s)
+  int max_nc = 1;
+  for (int i : g.members) max_nc = std::max(max_nc, b->G[i].nc);
+  if (d3)  // z layers per work item; a 4-layer prologue is converted per item
+    for (int z : {8, 16, 32, 64})
+      if (z == 8 || z <= max_nc) cand.push_back({0, z});
+  for (int s = 0; s < ns && !d3; ++s)
     if (visc || !ShapeSchedule(b, s).vface || b->precision == FV_PREC_FP64) cand.push_back({s, shapes[s].ty});
-  for (int s = 0; s < ns; ++s) {
+  for (int s = 0; s < ns && !d3; ++s) {
     const Schedule ks = ShapeSchedule(b, s);
     if ((ks.vface && !visc && b->precision != FV_PREC_FP64) || shape_of(ks) != s) continue;
     long long units = 0;
@@ -473,7 +490,7 @@ int Autotune(fv_batch* b, Group& g) {
   const bool log = std::getenv("FV3D_TILE_LOG") != nullptr;
   for (size_t c = 0; c < cand.size(); ++c) {
     if (log) {
-      const Schedule k = ShapeSchedule(b, cand[c].first);
+      const Schedule k = d3 ? Schedule3d(b, cand[c].second) : ShapeSchedule(b, cand[c].first);
       std::fprintf(stderr, "fv3d tile candidate %dx%d/%d%s: %.4f ms (%d items, %d CTAs)\n", k.tx, cand[c].second,
                    k.block_rows, k.vface ? "v" : "", grid[c] ? best_ms[c] : -1.0f, ntiles[c], grid[c]);
     }
@@ -498,7 +515,7 @@ int Autotune(fv_batch* b, Group& g) {
   cudaEventDestroy(e1);
   if (best_c < 0) return Fail(b, FV_ERR_CUDA, "no tile shape could be launched for a batch group");
   std::lock_guard<std::mutex> lock(g_cache_mutex);
-  Schedule chosen = ShapeSchedule(b, g.shape);
+  Schedule chosen = d3 ? Schedule3d(b, g.rows) : ShapeSchedule(b, g.shape);
   chosen.rows = g.rows;
   g_cache[key] = chosen;
   SaveCacheEntry(key, chosen);
@@ -951,10 +968,8 @@ int fvgpu_batch_schedule(fv_batch* b, int* ngroups, int* tx, int* rows, int* blo
   for (int gi = 0; gi < *ngroups && gi < max_groups; ++gi) {
     const Group& g = b->groups[gi];
     Schedule sc;
-    if (g.ndim == 3) {  // column blocks of 16 x 16 marched over z chunks
-      sc.tx = sc.rows = fv::batch3d_columns();
-      sc.block_rows = 0;
-      sc.vface = b->precision == FV_PREC_FP64 ? 1 : 0;
+    if (g.ndim == 3) {  // column blocks of 16 x 16 marched over chunks of `rows` z layers
+      sc = Schedule3d(b, g.rows);
     } else {
       sc = ShapeSchedule(b, g.shape);
       if (g.rows > 0) sc.rows = g.rows;

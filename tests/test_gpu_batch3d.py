@@ -66,6 +66,24 @@ def test_batch3d_fp64_equals_one_problem():
             np.testing.assert_array_equal(a, w)
 
 
+@pytest.mark.parametrize("layers", [8, 32, 64])
+def test_batch3d_z_chunks_fp64_equal_one_problem(layers, monkeypatch):
+    """Every z-chunk length the autotuner may pick (layers per work item,
+    forced through FV3D_TILE) gives the bits of each problem advanced alone,
+    and the schedule reports it."""
+    monkeypatch.setenv("FV3D_TILE", "16x%d" % layers)
+    probs = _problems()[:3]
+    b = fv.Batch([p.params for p in probs])
+    for i, p in enumerate(probs):
+        b.set_prim(i, *p.prim)
+    sched = b.schedule()
+    assert all((s["tx"], s["rows"], s["block_rows"]) == (16, layers, 0) for s in sched), sched
+    b.run(4)
+    for i, p in enumerate(probs):
+        for a, w in zip(b.get_prim(i), _fp64_alone(p, 4)):
+            np.testing.assert_array_equal(a, w)
+
+
 def test_batch3d_euler_fp64_equals_one_problem():
     pr = problems.blast(24, nz=20)  # Euler stepping (ping-pong buffers)
     b = fv.Batch([pr.params])
