@@ -651,6 +651,7 @@ def run_profile_case(args):
     """Only a workload's steps (warm-up + steps), for launch lists and ncu
     captures: no timing, no CPU baseline, no e2e.  Cases: fp64_rt (the bench
     workload), mixed_rt (the same in the FP32-mixed form, a batch of one),
+    sedov_mixed (Sedov 256^2 mixed: the multi-step launch),
     batch_sod_sedov_mixed / batch_sod_sedov_fp64 (64 instances of the
     512-instance set, to keep captures small), shear_mixed / shear_fp64 (the
     4096^2 shear layer, a state larger than L2; FP64 through fvgpu_create as
@@ -671,6 +672,8 @@ def run_profile_case(args):
     else:
         if case == "mixed_rt":
             probs = [problem()]
+        elif case == "sedov_mixed":
+            probs = [problems.sedov(256)]
         elif case.startswith("shear"):
             probs = [problems.shear_layer(4096)]
         elif case == "mixed_3d":
@@ -694,7 +697,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-case", nargs="?", const="fp64_rt", default=None,
-                    choices=["fp64_rt", "fp64_3d", "mixed_3d", "mixed_rt", "batch_sod_sedov_mixed",
+                    choices=["fp64_rt", "fp64_3d", "mixed_3d", "mixed_rt", "sedov_mixed", "batch_sod_sedov_mixed",
                              "batch_sod_sedov_fp64", "shear_mixed", "shear_fp64"],
                     help="run only a workload's steps (for ncu); prints no JSON")
     ap.add_argument("--no-variants", action="store_true",
