@@ -76,6 +76,8 @@ def _declare(lib):
         "fvgpu_get_prim": (C.c_int, [vp] + [_dp] * 5),
         "fvgpu_set_cons": (C.c_int, [vp] + [_dp] * 5),
         "fvgpu_get_cons": (C.c_int, [vp] + [_dp] * 5),
+        "fvgpu_init_problem": (C.c_int, [vp]),
+        "fvgpu_generate": (C.c_int, [P] + [_dp] * 5),
         "fvgpu_compute_dt": (C.c_int, [vp, _dp, _dp]),
         "fvgpu_step": (C.c_int, [vp, C.c_double]),
         "fvgpu_advance": (C.c_int, [vp, C.c_double, C.c_long, _dp, C.POINTER(C.c_long)]),
@@ -93,6 +95,7 @@ def _declare(lib):
         "fvgpu_batch_last_error": (C.c_char_p, [vp]),
         "fvgpu_batch_set_prim": (C.c_int, [vp, C.c_int] + [_dp] * 5),
         "fvgpu_batch_get_prim": (C.c_int, [vp, C.c_int] + [_dp] * 5),
+        "fvgpu_batch_init_problem": (C.c_int, [vp, C.c_int]),
         "fvgpu_batch_run": (C.c_int, [vp, C.c_long]),
         "fvgpu_batch_times": (C.c_int, [vp, _dp]),
         "fvgpu_batch_set_stream": (C.c_int, [vp, vp]),
@@ -131,6 +134,17 @@ def probe_grid_wait(arrive_all, max_polls):
     own (fvgpu_probe_grid_wait): 0 when it completed, FV_ERR_TIMEOUT when it
     gave up because a CTA never arrived."""
     return load_library().fvgpu_probe_grid_wait(1 if arrive_all else 0, int(max_polls))
+
+
+def generate(params):
+    """The reference's generator for params.problem (Init.h:18-209) run on the
+    GPU (fvgpu_generate): the primitives (rho, u, v, w, p), each [Nz][Ny][Nx]."""
+    shape = (params.Nz, params.Ny, params.Nx)
+    arrs = [np.empty(shape, np.float64) for _ in range(5)]
+    rc = load_library().fvgpu_generate(C.byref(params), *[_ptr(a) for a in arrs])
+    if rc:
+        raise FvError(rc, "fvgpu_generate(%r)" % params.problem)
+    return arrs
 
 
 def parse_ini(text):
@@ -219,6 +233,11 @@ class Simulation:
     def set_prim(self, rho, u=None, v=None, w=None, p=None):
         arrs = [_as_field(a, self.shape) for a in (rho, u, v, w, p)]
         self._check(self.lib.fvgpu_set_prim(self._h, *[_ptr(a) for a in arrs]), "set_prim")
+
+    def init_problem(self):
+        """InitFunctor::init + primToCons on the GPU (fvgpu_init_problem): the
+        generator named by params.problem sets the state."""
+        self._check(self.lib.fvgpu_init_problem(self._h), "init_problem")
 
     def set_cons(self, rho, mx=None, my=None, mz=None, E=None):
         arrs = [_as_field(a, self.shape) for a in (rho, mx, my, mz, E)]
@@ -343,6 +362,10 @@ class Batch:
     def set_prim(self, i, rho, u=None, v=None, w=None, p=None):
         arrs = [_as_field(a, self.shape(i)) for a in (rho, u, v, w, p)]
         self._check(self.lib.fvgpu_batch_set_prim(self._h, int(i), *[_ptr(a) for a in arrs]), "batch_set_prim")
+
+    def init_problem(self, i):
+        """The generator of problem i's params.problem on the GPU."""
+        self._check(self.lib.fvgpu_batch_init_problem(self._h, int(i)), "batch_init_problem")
 
     def get_prim(self, i):
         arrs = [np.empty(self.shape(i), np.float64) for _ in range(5)]

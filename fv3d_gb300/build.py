@@ -29,9 +29,9 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["fv_stage2d.cu", "fv_stage3d.cu", "fv_stage3d32.cu", "fv_batch64.cu", "fv_batch32.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp",
-               "fv_batch.cpp", "fv_noalloc.cu", "fv_probe.cu"]
+               "fv_batch.cpp", "fv_noalloc.cu", "fv_probe.cu", "fv_init.cu"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
-FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_stage3d.cu", "fv_batch64.cu", "fv_aux.cu"}
+FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_stage3d.cu", "fv_batch64.cu", "fv_aux.cu", "fv_init.cu"}
 # the FP32-mixed kernels: approximate FP32 division/sqrt, FMA contraction
 FAST_MATH_SOURCES = {"fv_batch32.cu", "fv_stage3d32.cu"}
 

@@ -7,15 +7,18 @@
 // Reads the same .ini file (readInifile semantics), sets the initial state,
 // and runs the reference's time loop: while (t + epsilon < tend) { dt =
 // computeDt; log every log_frequency steps; save when due; update; t += dt }.
-// Every problem generator of Init.h is provided (sod_x, sod_y, sod_z, blast,
-// diffusion, rayleigh-taylor, H84, C91).  H84 and C91 draw their
-// perturbations from Kokkos' XorShift64 pool in the reference, whose
-// sequence depends on the thread schedule; here each cell draws from a
+// Every problem generator of Init.h runs on the GPU (sod_x, sod_y, sod_z,
+// blast, diffusion, rayleigh-taylor, H84, C91: fvgpu_init_problem, the
+// state written in place as init.init(Q); primToCons(Q, U) do).  H84 and C91
+// draw their perturbations from Kokkos' XorShift64 pool in the reference,
+// whose sequence depends on the thread schedule; here each cell draws from a
 // counter-based splitmix64 stream of [misc] seed instead (the same stream as
 // fv3d_gb300.problems.uniform), so the runs are reproducible but not
 // bit-identical to a reference run.  Any other initial state is read with --ic
 // from a raw file of 5 float64 arrays (rho, u, v, w, p), each Nz*Ny*Nx in C
-// order; --write-ic writes the generated state in that format.  Snapshots
+// order; --write-ic writes the generated state in that format (generated
+// into host arrays with fvgpu_generate, then set with fvgpu_set_prim: the
+// same state).  Snapshots
 // are written as the same raw format (<prefix>_<ite>.bin) instead of HDF5,
 // with the vertex coordinates in <prefix>_grid.bin and an XDMF index
 // (<prefix>.xdmf) shaped like the reference's, so XDMF readers (ParaView,
@@ -47,83 +50,6 @@ namespace {
 struct Fields {
   std::vector<double> f[5];
 };
-
-double PosX(const fv_params& p, int i) { return p.xmin + (i + 0.5) * p.dx; }
-double PosY(const fv_params& p, int j) { return p.ymin + (j + 0.5) * p.dy; }
-double PosZ(const fv_params& p, int k) { return p.zmin + (k + 0.5) * p.dz; }
-
-uint64_t Mix64(uint64_t z) {
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-// Uniform [0, 1) number `c` of stream `stream` of `seed` (counter-based
-// splitmix64, top 53 bits).
-double Uniform(uint64_t seed, uint64_t stream, uint64_t c) {
-  const uint64_t golden = 0x9E3779B97F4A7C15ull;
-  const uint64_t key = Mix64(seed + golden * (stream + 1));
-  return (double)(Mix64(key + golden * (c + 1)) >> 11) * (1.0 / 9007199254740992.0);
-}
-
-constexpr uint64_t kStreamH84 = 31, kStreamC91 = 32;
-
-// Init.h:18-209 on the interior cells.
-bool Generate(const fv_params& p, Fields& q) {
-  const std::string prob = p.problem;
-  const size_t n = (size_t)p.Nx * p.Ny * p.Nz;
-  for (auto& a : q.f) a.assign(n, 0.0);
-  for (int k = 0; k < p.Nz; ++k)
-    for (int j = 0; j < p.Ny; ++j)
-      for (int i = 0; i < p.Nx; ++i) {
-        const size_t c = ((size_t)k * p.Ny + j) * p.Nx + i;
-        const double x = PosX(p, i), y = PosY(p, j), z = PosZ(p, k);
-        double r = 0, u = 0, v = 0, w = 0, pr = 0;
-        if (prob == "sod_x" || prob == "sod_y" || prob == "sod_z") {
-          const double s = prob == "sod_x" ? x : prob == "sod_y" ? y : z;
-          r = s <= 0.5 ? 1.0 : 0.125;
-          pr = s <= 0.5 ? 1.0 : 0.1;
-        } else if (prob == "blast") {
-          const double xr = 0.5 * (p.xmin + p.xmax) - x, yr = 0.5 * (p.ymin + p.ymax) - y,
-                       zr = 0.5 * (p.zmin + p.zmax) - z;
-          const double rr = std::sqrt(xr * xr + yr * yr + zr * zr);
-          r = rr < 0.2 ? 1.0 : 1.2;
-          pr = rr < 0.2 ? 10.0 : 0.1;
-        } else if (prob == "diffusion") {
-          const double x0 = x - 0.5 * (p.xmin + p.xmax), y0 = y - 0.5 * (p.ymin + p.ymax),
-                       z0 = z - 0.5 * (p.zmin + p.zmax);
-          const double rr = std::sqrt(x0 * x0 + y0 * y0 + z0 * z0);
-          r = rr < 0.2 ? 1.0 : 0.1;
-          pr = 1.0;
-          u = v = w = 1.0;
-        } else if (prob == "rayleigh-taylor") {
-          const double zmid = 0.5 * (p.zmin + p.zmax);
-          r = z < zmid ? 1.0 : 2.0;
-          pr = 2.5 + 0.1 * p.g * z;
-          if (z > -1.0 / 3.0 && z < 1.0 / 3.0)
-            w = 0.01 * (1.0 + std::cos(4 * M_PI * x)) * (1.0 + std::cos(4.0 * M_PI * y)) *
-                (1 + std::cos(3.0 * M_PI * z)) / 4.0;
-        } else if (prob == "H84") {  // Init.h:104-121
-          r = std::pow(z, p.m1);
-          pr = std::pow(z, p.m1 + 1.0);
-          w = p.h84_pert * (Uniform((uint64_t)p.seed, kStreamH84, c) - 0.5);
-        } else if (prob == "C91") {  // Init.h:127-148
-          const double T = 1.0 + p.theta1 * z;
-          r = std::pow(T, p.m1);
-          pr = std::pow(T, p.m1 + 1.0);
-          const double pert = p.c91_pert * (Uniform((uint64_t)p.seed, kStreamC91, c) - 0.5);
-          pr = pr * (1.0 + pert);
-        } else {
-          return false;
-        }
-        q.f[0][c] = r;
-        q.f[1][c] = u;
-        q.f[2][c] = v;
-        q.f[3][c] = w;
-        q.f[4][c] = pr;
-      }
-  return true;
-}
 
 bool ReadRaw(const std::string& path, size_t n, Fields& q) {
   FILE* f = std::fopen(path.c_str(), "rb");
@@ -306,10 +232,14 @@ int main(int argc, char** argv) {
       std::fprintf(stderr, "cannot read %zu cells from %s\n", n, ic.c_str());
       return 1;
     }
-  } else if (!Generate(p, q)) {
-    std::fprintf(stderr, "Error unknown problem %s (give --ic)\n", p.problem);
-    return 1;
+  } else if (!write_ic.empty()) {  // generated on the GPU into host arrays, written, then set
+    for (auto& a : q.f) a.resize(n);
+    if (fvgpu_generate(&p, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data()) != FV_OK) {
+      std::fprintf(stderr, "Error unknown problem %s (give --ic)\n", p.problem);
+      return 1;
+    }
   }
+  const bool on_device = !restart && ic.empty() && write_ic.empty();  // fvgpu_init_problem
   if (!write_ic.empty() && !WriteRaw(write_ic, q)) {
     std::fprintf(stderr, "cannot write %s\n", write_ic.c_str());
     return 1;
@@ -317,7 +247,9 @@ int main(int argc, char** argv) {
   fv_sim* s = nullptr;
   if (Check(s, fvgpu_create(&p, &s), "fvgpu_create")) return 1;
   const double* qs[5] = {q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data()};
-  if (restart && ck.conserved) {
+  if (on_device) {
+    if (Check(s, fvgpu_init_problem(s), "init_problem")) return 1;
+  } else if (restart && ck.conserved) {
     if (Check(s, fvgpu_set_cons(s, qs[0], qs[1], qs[2], qs[3], qs[4]), "set_cons")) return 1;
   } else if (Check(s, fvgpu_set_prim(s, qs[0], qs[1], qs[2], qs[3], qs[4]), "set_prim")) {
     return 1;

@@ -647,6 +647,85 @@ int fvgpu_set_prim(fv_sim* s, const double* rho, const double* u, const double* 
   return SetState(s, f, true);
 }
 
+int fvgpu_init_problem(fv_sim* s) {
+  if (s && s->mixed) return Mixed(s, fvgpu_batch_init_problem(s->mixed, 0));
+  if (!s || !s->buf) return s ? Fail(s, FV_ERR_STATE, "handle not configured") : FV_ERR_PARAM;
+  fv::InitSpec spec;
+  if (fv::make_init_spec(s->p, &spec) != FV_OK)
+    return Fail(s, FV_ERR_PARAM, "unknown problem '%.63s' (Init.h: sod_x, sod_y, sod_z, blast, rayleigh-taylor, "
+                "diffusion, H84, C91)", s->p.problem);
+  int slot_of[5];
+  StorageOrder(s->G.plane, slot_of);
+  Fields out;
+  for (int v = 0; v < 5; ++v) out.f[v] = s->A.f[slot_of[v]];
+  ResetGraph(s);
+  s->cur = 0;
+  s->state_set = false;
+  int rc = DropPrims(s);
+  if (rc) return rc;
+  int* d_flags = reinterpret_cast<int*>(s->d_partial);
+  int* h_flags = reinterpret_cast<int*>(s->h_partial);
+  CUDA_TRY(s, cudaMemsetAsync(d_flags, 0, sizeof(int), s->stream));
+  cudaError_t e = fv::launch_generate(spec, out, s->G.pitch, d_flags, s->stream);
+  if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "generator launch: %s", cudaGetErrorString(e));
+  CUDA_TRY(s, cudaMemcpyAsync(h_flags, d_flags, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  const int flags = *h_flags;
+  // the checks set_prim makes on the velocities, from the generator's flags
+  if (s->G.ndim == 3) {
+    s->wact = true;
+    for (int a = 0; a < 3; ++a)
+      if ((s->refl_deg >> a & 1) && (flags >> (1 + a) & 1))
+        return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting one-cell axis is not built");
+  } else {
+    const int out_of_plane = s->G.plane == fv::PLANE_XY ? 3 : 2;  // w, or v of an x-z run
+    s->wact = s->p.viscosity_active || (flags >> out_of_plane & 1);
+    if (s->wact && s->deg_bc == FV_BC_REFLECTING)
+      return Fail(s, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  }
+  {
+    Timed t(s, KC_CONV);
+    e = fv::launch_prim_to_cons2d(s->G, s->A, s->stream);
+    if (e != cudaSuccess) return Fail(s, FV_ERR_CUDA, "primToCons launch: %s", cudaGetErrorString(e));
+    t.done();
+  }
+  s->launches += 1;  // the generator
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  s->slot_valid = false;
+  s->state_set = true;
+  return FV_OK;
+}
+
+int fvgpu_generate(const fv_params* p, double* rho, double* u, double* v, double* w, double* pr) {
+  if (!p || p->Nx < 1 || p->Ny < 1 || p->Nz < 1) return FV_ERR_PARAM;
+  fv::InitSpec spec;
+  if (fv::make_init_spec(*p, &spec) != FV_OK) return FV_ERR_PARAM;
+  const size_t n = (size_t)p->Nx * p->Ny * p->Nz;
+  double* dst[5] = {rho, u, v, w, pr};
+  double* d = nullptr;
+  cudaStream_t st = nullptr;
+  int rc = FV_OK;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return FV_ERR_CUDA;
+  if (cudaMallocAsync(&d, 5 * n * sizeof(double) + 256, st) != cudaSuccess) {
+    cudaStreamDestroy(st);
+    return FV_ERR_NOMEM;
+  }
+  Fields out;
+  for (int k = 0; k < 5; ++k) out.f[k] = d + (size_t)k * n;
+  int* flags = reinterpret_cast<int*>(d + 5 * n);
+  // the caller's arrays: any memory (device, pinned or pageable host)
+  if (cudaMemsetAsync(flags, 0, sizeof(int), st) != cudaSuccess ||
+      fv::launch_generate(spec, out, p->Nx, flags, st) != cudaSuccess)
+    rc = FV_ERR_CUDA;
+  for (int k = 0; k < 5 && rc == FV_OK; ++k)
+    if (dst[k] && cudaMemcpyAsync(dst[k], out.f[k], n * sizeof(double), cudaMemcpyDefault, st) != cudaSuccess)
+      rc = FV_ERR_CUDA;
+  if (cudaFreeAsync(d, st) != cudaSuccess) rc = FV_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) rc = FV_ERR_CUDA;
+  cudaStreamDestroy(st);
+  return rc;
+}
+
 int fvgpu_set_cons(fv_sim* s, const double* rho, const double* mx, const double* my, const double* mz,
                    const double* E) {
   if (s && s->mixed)

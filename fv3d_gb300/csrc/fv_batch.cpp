@@ -836,6 +836,52 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
   return FV_OK;
 }
 
+int fvgpu_batch_init_problem(fv_batch* b, int inst) {
+  if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
+  if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);
+  fv::InitSpec spec;
+  if (fv::make_init_spec(b->p[inst], &spec) != FV_OK)
+    return Fail(b, FV_ERR_PARAM, "problem %d: unknown problem '%.63s'", inst, b->p[inst].problem);
+  const Grid& G = b->G[inst];
+  int slot_of[5];
+  StorageOrder(G.plane, slot_of);
+  // the generator writes FP64 primitives where set_prim's copies land
+  Fields stage = b->precision == FV_PREC_FP64 ? Current(b, inst) : Fields();
+  if (b->precision != FV_PREC_FP64)
+    for (int k = 0; k < 5; ++k) stage.f[k] = b->scratch + (size_t)k * G.fstride;
+  Fields out;
+  for (int v = 0; v < 5; ++v) out.f[v] = stage.f[slot_of[v]];
+  b->state_set[inst] = 0;
+  int* d_flags = nullptr;
+  int flags = 0;
+  BCUDA(b, cudaMallocAsync(&d_flags, sizeof(int), b->stream));
+  cudaError_t e = cudaMemsetAsync(d_flags, 0, sizeof(int), b->stream);
+  if (e == cudaSuccess) e = fv::launch_generate(spec, out, G.pitch, d_flags, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, d_flags, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
+  cudaFreeAsync(d_flags, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "generator: %s", cudaGetErrorString(e));
+  b->launches += 1;
+  // the velocity checks of set_prim, from the generator's flags
+  const int out_of_plane = G.plane == fv::PLANE_XY ? 3 : 2;  // w, or v of an x-z run
+  const bool wact = b->p[inst].viscosity_active || (G.ndim == 2 && (flags >> out_of_plane & 1)) || G.ndim == 3;
+  if (G.ndim == 2 && wact && b->deg_bc[inst] == FV_BC_REFLECTING)
+    return Fail(b, FV_ERR_UNSUPPORTED, "a non-zero velocity along a reflecting degenerate axis is not built");
+  if ((bool)b->wact[inst] != wact) b->prepared = false;
+  b->wact[inst] = wact;
+  if (!b->prepared) ReleaseGroups(b);
+  if (b->Q[inst].f[0]) BCUDA(b, cudaMemsetAsync(&b->d_ctrl[inst].q_valid, 0, sizeof(int), b->stream));
+  e = fv::launch_prim_to_cons2d(G, stage, b->stream);
+  if (e == cudaSuccess && b->precision != FV_PREC_FP64)
+    e = fv::launch_pairs_from_double(G, stage, Current(b, inst), b->stream);
+  if (e != cudaSuccess) return Fail(b, FV_ERR_CUDA, "init_problem: %s", cudaGetErrorString(e));
+  b->launches += b->precision == FV_PREC_FP64 ? 1 : 2;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  b->state_set[inst] = 1;
+  b->slot_valid[inst] = 0;
+  return FV_OK;
+}
+
 int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* v, double* w, double* pr) {
   if (!b || !b->buf) return b ? Fail(b, FV_ERR_STATE, "batch not configured") : FV_ERR_PARAM;
   if (inst < 0 || inst >= b->n) return Fail(b, FV_ERR_PARAM, "problem index %d out of range", inst);

@@ -5,6 +5,7 @@
 
 #include <utility>
 
+#include "fv3d_gb300.h"
 #include "fv_device.cuh"
 #include "fv_grid.cuh"
 #include "fv_tma.cuh"
@@ -216,5 +217,27 @@ cudaError_t launch_reduce2d_mixed(const Grid& G, bool wact, Fields pairs, StepCt
                                   cudaStream_t stream);
 cudaError_t launch_pairs_from_double(const Grid& G, Fields src, Fields dst_pairs, cudaStream_t stream);
 cudaError_t launch_double_from_pairs(const Grid& G, Fields src_pairs, Fields dst, cudaStream_t stream);
+
+// The reference's problem generators (Init.h:18-209) on the GPU (fv_init.cu).
+enum InitKind : int {
+  INIT_SOD_X, INIT_SOD_Y, INIT_SOD_Z, INIT_BLAST, INIT_RT, INIT_DIFFUSION, INIT_H84, INIT_C91
+};
+struct InitSpec {
+  int kind;                  // InitKind
+  int nx, ny, rows;          // Nx, Ny and rows = Ny * Nz
+  double xmin, ymin, zmin, dx, dy, dz;
+  double xmid, ymid, zmid;   // 0.5 * (min + max) per axis
+  double m1;                 // polytropic index (H84, C91)
+  double c0;                 // 0.1 g (rayleigh-taylor), theta1 (C91)
+  double c1, c2;             // 4 pi and 3 pi (rayleigh-taylor)
+  double pert;               // perturbation amplitude (H84, C91)
+  unsigned long long key;    // perturbation stream key
+};
+// FV_OK, or FV_ERR_PARAM for a problem name Init.h does not know.
+int make_init_spec(const fv_params& p, InitSpec* spec);
+// Writes the primitives of every interior cell to out (reference variable
+// order rho, u, v, w, p; element (k * Ny + j) * pitch + i) and ORs bit v of
+// *flags when field v has a non-zero value.
+cudaError_t launch_generate(const InitSpec& spec, const Fields& out, int pitch, int* flags, cudaStream_t stream);
 
 }  // namespace fv

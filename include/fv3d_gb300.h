@@ -6,6 +6,8 @@
  *
  *   fv_read_ini / fv_parse_ini   <- fv3d::readInifile            (SimInfo.h:169-306)
  *   fvgpu_set_prim / get_prim    <- fv3d::primToCons/consToPrim  (SimInfo.h:313-331)
+ *   fvgpu_init_problem           <- InitFunctor::init(Q) + primToCons (Init.h:247-279,
+ *                                   main.cpp:42-44); fvgpu_generate fills caller arrays
  *   fvgpu_compute_dt             <- ComputeDtFunctor::computeDt  (ComputeDt.h:17-63)
  *   fvgpu_step                   <- UpdateFunctor::update        (Update.h:180-206),
  *                                   which runs BoundaryManager::fillBoundaries
@@ -142,6 +144,21 @@ int fvgpu_set_cons(fv_sim* sim, const double* rho, const double* mx, const doubl
                    const double* mz, const double* E);
 int fvgpu_get_cons(fv_sim* sim, double* rho, double* mx, double* my, double* mz, double* E);
 
+/* InitFunctor(params).init(Q) followed by primToCons (Init.h:228-279,
+ * main.cpp:42-44), on the GPU: the generator named by params.problem
+ * (sod_x, sod_y, sod_z, blast, rayleigh-taylor, diffusion, H84, C91) writes
+ * the state directly.  Positions and operation order are the reference's
+ * (sod / blast / diffusion bit for bit; cos and pow may differ in the last
+ * place).  H84 / C91 perturbations come from a counter-based splitmix64
+ * stream of params.seed (cell (k*Ny + j)*Nx + i, stream 31 / 32) in place of
+ * Kokkos' XorShift64 pool, whose draws depend on the thread schedule.
+ * FV_ERR_PARAM for an unknown problem (where Init.h:241-242 throws). */
+int fvgpu_init_problem(fv_sim* sim);
+/* The same generator into caller arrays of primitives (rho, u, v, w, p;
+ * [Nz][Ny][Nx]; any memory, NULL skips a field), without a handle: the
+ * state init.init(Q) leaves in Q's interior. */
+int fvgpu_generate(const fv_params* params, double* rho, double* u, double* v, double* w, double* p);
+
 /* ComputeDtFunctor::computeDt on the current state: *dt = CFL/max(inv[0..2]);
  * inv (may be NULL) receives {inv_dt_hyp, inv_dt_tc, inv_dt_visc}. */
 int fvgpu_compute_dt(fv_sim* sim, double* dt, double inv[3]);
@@ -257,6 +274,8 @@ int fvgpu_batch_set_prim(fv_batch* b, int inst, const double* rho, const double*
                          const double* v, const double* w, const double* p);
 int fvgpu_batch_get_prim(fv_batch* b, int inst, double* rho, double* u, double* v,
                          double* w, double* p);
+/* fvgpu_init_problem for problem inst of a batch (its params.problem). */
+int fvgpu_batch_init_problem(fv_batch* b, int inst);
 /* Advance every problem by nsteps steps, each with its own CFL dt (the
  * fixed-step form of the main.cpp loop).  Steps are replayed from a captured
  * CUDA graph. */

@@ -18,9 +18,14 @@
 #include "fv3d_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #include <omp.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846 /* <cmath>'s value, which the reference uses */
+#endif
 
 enum { IR = 0, IU = 1, IV = 2, IW = 3, IP = 4, IE = 4 };
 enum { IX = 0, IY = 1, IZ = 2 };
@@ -738,6 +743,92 @@ int fvora_set_prim(fvora_sim* s, const double* r, const double* u, const double*
     double* q = AT(s, s->Q, i_ + s->ibeg, j_ + s->jbeg, k_ + s->kbeg);
     for (int var = 0; var < 5; ++var) q[var] = f[var] ? f[var][INTERIOR_N(s)] : 0.0;
   }
+  fill_boundaries(s, s->Q);
+  array_prim_to_cons(s, s->Q, s->U);
+  return FV_OK;
+}
+
+/* ---------------- Init.h ---------------- */
+
+/* Counter-based uniform in [0, 1): splitmix64 finaliser of key + golden *
+ * (c + 1), top 53 bits, with key = splitmix64(seed + golden * (stream + 1)).
+ * The H84 / C91 perturbations draw cell c = (k * Ny + j) * Nx + i of stream
+ * 31 / 32 from it in place of Kokkos' XorShift64 pool (Init.h:13), whose
+ * draws depend on which thread visits which cell; the product's generator
+ * uses the same stream. */
+static uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double stream_uniform(uint64_t seed, uint64_t stream, uint64_t c) {
+  const uint64_t golden = 0x9E3779B97F4A7C15ull;
+  const uint64_t key = mix64(seed + golden * (stream + 1));
+  return (double)(mix64(key + golden * (c + 1)) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* One cell of the generator `problem` (Init.h:18-209); q in IR..IP order.
+ * Returns 0 for an unknown problem (Init.h:241-242 throws). */
+static int generate_cell(const fvora_sim* s, const char* problem, int i, int j, int k, uint64_t c, double* q) {
+  const fv_params* P = &s->p;
+  double pos[3];
+  get_pos(s, i, j, k, pos);
+  const double x = pos[IX], y = pos[IY], z = pos[IZ];
+  q[IR] = q[IU] = q[IV] = q[IW] = q[IP] = 0.0;
+  if (!strcmp(problem, "sod_x") || !strcmp(problem, "sod_y") || !strcmp(problem, "sod_z")) { /* Init.h:18-64 */
+    const double d = problem[4] == 'x' ? x : problem[4] == 'y' ? y : z;
+    q[IR] = d <= 0.5 ? 1.0 : 0.125;
+    q[IP] = d <= 0.5 ? 1.0 : 0.1;
+  } else if (!strcmp(problem, "blast")) { /* Init.h:69-98 */
+    const double xr = 0.5 * (P->xmin + P->xmax) - x;
+    const double yr = 0.5 * (P->ymin + P->ymax) - y;
+    const double zr = 0.5 * (P->zmin + P->zmax) - z;
+    const double r = sqrt(xr * xr + yr * yr + zr * zr);
+    q[IR] = r < 0.2 ? 1.0 : 1.2;
+    q[IP] = r < 0.2 ? 10.0 : 0.1;
+  } else if (!strcmp(problem, "diffusion")) { /* Init.h:153-177 */
+    const double x0 = x - 0.5 * (P->xmin + P->xmax);
+    const double y0 = y - 0.5 * (P->ymin + P->ymax);
+    const double z0 = z - 0.5 * (P->zmin + P->zmax);
+    const double r = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+    q[IR] = r < 0.2 ? 1.0 : 0.1;
+    q[IP] = 1.0;
+    q[IU] = q[IV] = q[IW] = 1.0;
+  } else if (!strcmp(problem, "rayleigh-taylor")) { /* Init.h:182-206 */
+    const double zmid = 0.5 * (P->zmin + P->zmax);
+    q[IR] = z < zmid ? 1.0 : 2.0;
+    q[IP] = 2.5 + 0.1 * P->g * z;
+    if (z > -1.0 / 3.0 && z < 1.0 / 3.0)
+      q[IW] = 0.01 * (1.0 + cos(4 * M_PI * x)) * (1.0 + cos(4.0 * M_PI * y)) * (1 + cos(3.0 * M_PI * z)) / 4.0;
+  } else if (!strcmp(problem, "H84")) { /* Init.h:103-122 */
+    q[IR] = pow(z, P->m1);
+    q[IP] = pow(z, P->m1 + 1.0);
+    q[IW] = P->h84_pert * (stream_uniform((uint64_t)(int64_t)P->seed, 31, c) - 0.5);
+  } else if (!strcmp(problem, "C91")) { /* Init.h:127-148 */
+    const double T = 1.0 + P->theta1 * z;
+    q[IR] = pow(T, P->m1);
+    const double prs = pow(T, P->m1 + 1.0);
+    const double pert = P->c91_pert * (stream_uniform((uint64_t)(int64_t)P->seed, 32, c) - 0.5);
+    q[IP] = prs * (1.0 + pert);
+  } else {
+    return 0;
+  }
+  return 1;
+}
+
+/* InitFunctor::init(Q) then primToCons (Init.h:247-279, main.cpp:42-44): Q's
+ * interior from the generator, ghosts by the BC fill, U = primToCons(Q).
+ * The generated interior primitives are returned when the arrays are given. */
+int fvora_generate(fvora_sim* s, double* r, double* u, double* v, double* w, double* p) {
+  double* f[5] = {r, u, v, w, p};
+  int ok = 1;
+  FOR_INTERIOR(s) {
+    double* q = AT(s, s->Q, i_ + s->ibeg, j_ + s->jbeg, k_ + s->kbeg);
+    ok &= generate_cell(s, s->p.problem, i_ + s->ibeg, j_ + s->jbeg, k_ + s->kbeg, (uint64_t)INTERIOR_N(s), q);
+    for (int var = 0; var < 5; ++var)
+      if (f[var]) f[var][INTERIOR_N(s)] = q[var];
+  }
+  if (!ok) return FV_ERR_PARAM;
   fill_boundaries(s, s->Q);
   array_prim_to_cons(s, s->Q, s->U);
   return FV_OK;

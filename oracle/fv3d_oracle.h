@@ -25,6 +25,8 @@ int fvora_set_prim(fvora_sim* s, const double* r, const double* u, const double*
                    const double* p);
 int fvora_set_cons(fvora_sim* s, const double* r, const double* mx, const double* my, const double* mz,
                    const double* E);
+/* The generators of Init.h (InitFunctor::init then primToCons). */
+int fvora_generate(fvora_sim* s, double* r, double* u, double* v, double* w, double* p);
 int fvora_get_prim(fvora_sim* s, double* r, double* u, double* v, double* w, double* p);
 int fvora_get_cons(fvora_sim* s, double* r, double* mx, double* my, double* mz, double* E);
 double fvora_compute_dt(fvora_sim* s, double inv[3]);

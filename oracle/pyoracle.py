@@ -36,7 +36,7 @@ def load_oracle():
         lib.fvora_create.restype = C.c_void_p
         lib.fvora_create.argtypes = [C.POINTER(FvParams)]
         lib.fvora_destroy.argtypes = [C.c_void_p]
-        for n in ("fvora_set_prim", "fvora_set_cons", "fvora_get_prim", "fvora_get_cons"):
+        for n in ("fvora_set_prim", "fvora_set_cons", "fvora_get_prim", "fvora_get_cons", "fvora_generate"):
             getattr(lib, n).argtypes = [C.c_void_p] + [_dp] * 5
             getattr(lib, n).restype = C.c_int
         lib.fvora_compute_dt.restype = C.c_double
@@ -71,7 +71,7 @@ def load_ref():
         lib.fvref_create_b02.restype = C.c_void_p
         lib.fvref_create_b02.argtypes = [C.c_char_p] + [C.c_double] * 4
         lib.fvref_destroy.argtypes = [C.c_void_p]
-        for n in ("fvref_set_prim", "fvref_get_prim", "fvref_get_cons"):
+        for n in ("fvref_set_prim", "fvref_get_prim", "fvref_get_cons", "fvref_generate"):
             getattr(lib, n).argtypes = [C.c_void_p] + [_dp] * 5
         lib.fvref_compute_dt.restype = C.c_double
         lib.fvref_compute_dt.argtypes = [C.c_void_p]
@@ -139,6 +139,15 @@ class Oracle(_Base):
     def get_prim(self):
         return self._get(self.lib.fvora_get_prim)
 
+    def generate(self):
+        """The generator named by params.problem (Init.h:18-209): sets the
+        state and returns the generated primitives (rho, u, v, w, p)."""
+        shape = _shape(self.params)
+        arrs = [np.empty(shape, np.float64) for _ in range(5)]
+        if self.lib.fvora_generate(self._h, *[_ptr(a) for a in arrs]) != 0:
+            raise ValueError("unknown problem %r" % self.params.problem)
+        return arrs
+
     def get_cons(self):
         return self._get(self.lib.fvora_get_cons)
 
@@ -185,6 +194,11 @@ class RefOracle(_Base):
 
     def get_prim(self):
         return self._get(self.lib.fvref_get_prim)
+
+    def generate(self):
+        """The reference's InitFunctor::init (its random pool replaced by
+        the shim's: H84 / C91 perturbations are not the reference's)."""
+        return self._get(self.lib.fvref_generate)
 
     def get_cons(self):
         return self._get(self.lib.fvref_get_cons)

@@ -2,14 +2,16 @@
 //
 // Compiles the reference's own FP64 hot-path headers, unmodified, from the
 // reference tree (SimInfo.h, States.h, Update.h, RiemannSolvers.h,
-// BoundaryConditions.h, ThermalConduction.h, Viscosity.h, ComputeDt.h)
-// against the Kokkos/INIReader shims in oracle/shim/, and exposes them through
+// BoundaryConditions.h, ThermalConduction.h, Viscosity.h, ComputeDt.h and
+// the generators of Init.h) against the Kokkos/INIReader shims in oracle/shim/, and exposes them through
 // a small C ABI (fvref_*) that mirrors the product's fvgpu_* calls so tests can
 // run both on identical inputs.  Built by oracle/build.py into oracle/_ref/.
 //
 // Departures from main.cpp, each forced by the reference itself:
-//   - Init.h / IOManager.h are not included (HDF5/HighFive and the Kokkos
-//     random pool are absent); the caller injects the primitive state Q.
+//   - IOManager.h is not included (HDF5/HighFive are absent); the caller
+//     injects the primitive state Q, or runs the reference's own generators
+//     (Init.h, fvref_generate) with the random pool of oracle/shim, whose
+//     draws are not Kokkos' (the H84 / C91 perturbations differ).
 //   - RK2: UpdateFunctor::update (Update.h:180-206) allocates U0/Ustar with 3
 //     extents for a rank-4 View (Update.h:184-185) and cannot run, so
 //     fvref_step performs the same sequence (Update.h:187-204) with correctly
@@ -22,6 +24,7 @@
 #include "SimInfo.h"
 #include "ComputeDt.h"
 #include "Update.h"
+#include "Init.h"
 
 #include "fv3d_gb300.h"
 
@@ -182,6 +185,23 @@ double fvref_compute_dt(void* h) {
   RefSim* s = (RefSim*)h;
   consToPrim(s->U, s->Q, s->params);
   return s->cdt->computeDt(s->Q, s->params.save_freq, 0.0, false);
+}
+
+// init.init(Q); primToCons(Q, U) (main.cpp:42-44, Init.h:247-279): the
+// reference's generator named by params.problem fills Q, the interior
+// primitives are returned as generated.
+int fvref_generate(void* h, double* r, double* u, double* v, double* w, double* pr) {
+  RefSim* s = (RefSim*)h;
+  InitFunctor init(s->params);
+  init.init(s->Q);
+  primToCons(s->Q, s->U, s->params);
+  double* f[5] = {r, u, v, w, pr};
+  Array Q = s->Q;
+  ForInterior(s->params, [&](int i, int j, int k, size_t n) {
+    for (int var = 0; var < 5; ++var)
+      if (f[var]) f[var][n] = Q(k, j, i, var);
+  });
+  return FV_OK;
 }
 
 // One pass of the main.cpp:51-74 loop body with a given dt (no I/O).

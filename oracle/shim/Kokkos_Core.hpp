@@ -3,8 +3,9 @@
 // Kokkos itself (an empty, unpinned git submodule of the reference) is not
 // available.  This header provides exactly the API subset that the
 // reference's hot-path headers use, so that SimInfo.h, States.h, Update.h,
-// RiemannSolvers.h, BoundaryConditions.h, ThermalConduction.h, Viscosity.h and
-// ComputeDt.h compile UNMODIFIED with g++ -fopenmp into oracle/_ref/:
+// RiemannSolvers.h, BoundaryConditions.h, ThermalConduction.h, Viscosity.h,
+// ComputeDt.h and (with Kokkos_Random.hpp) Init.h compile UNMODIFIED with
+// g++ -fopenmp into oracle/_ref/:
 //
 //   View<double****>   host LayoutRight (k,j,i,var), zero-initialised,
 //                      reference counted only outside parallel regions

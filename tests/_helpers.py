@@ -77,3 +77,36 @@ def rel_l1(a, b):
 
 def rel_l1_fields(A, B):
     return [rel_l1(a, b) for a, b in zip(A, B)]
+
+
+# Generator fixtures (tests/golden/generators.npz, InitFunctor::init of the
+# reference): per case, the fields computed through cos / pow (compared to
+# within a few units in the last place: libm and CUDA round those
+# differently) and the random ones (the fixture holds the test shim's draws,
+# not the reference's: checked by their range only).
+GEN_LIBM = {"rt_xz": (3,), "rt_3d": (3,), "h84_3d": (0, 4), "c91_3d": (0,)}
+GEN_RANDOM = {"h84_3d": (3,), "c91_3d": (4,)}
+GEN_MAX_ULP = 4
+
+
+def generator_cases():
+    with np.load(os.path.join(GOLDEN, "generators.npz")) as g:
+        return sorted(k for k in g.files if not k.endswith("__ini"))
+
+
+def load_generator(name):
+    """(ini text, q) of a generator fixture; q has shape (5, Nz, Ny, Nx)."""
+    with np.load(os.path.join(GOLDEN, "generators.npz")) as g:
+        return str(g[name + "__ini"]), g[name]
+
+
+def assert_generated(got, want, name):
+    """got (5 fields) against the fixture `want` of generator case `name`:
+    bit for bit, cos / pow fields within GEN_MAX_ULP, random fields skipped."""
+    for v in range(5):
+        if v in GEN_RANDOM.get(name, ()):
+            continue
+        if v in GEN_LIBM.get(name, ()):
+            np.testing.assert_array_max_ulp(np.asarray(got[v]), want[v], maxulp=GEN_MAX_ULP)
+        else:
+            np.testing.assert_array_equal(np.asarray(got[v]), want[v], err_msg="%s field %d" % (name, v))

@@ -11,7 +11,12 @@ seeded problems and records, per case:
   q1        primitive state after one step
   qN        primitive state after all steps
 and Riemann-solver known answers (hll / hllc) on seeded state pairs that
-cover every wave-speed branch.
+cover every wave-speed branch, and (generators.npz) the state each problem
+generator of Init.h writes (InitFunctor::init) on small grids shaped like the
+reference's settings files: key <case> is the primitive state (5, Nz, Ny,
+Nx), <case>__ini its .ini text.  The random pool of the shim is not Kokkos':
+the H84 w and C91 p fields of those two cases hold the shim's draws and are
+not compared.
 
 Needs the reference sources (only present where the fixtures are made):
     python tests/golden/make_golden.py [case names]
@@ -158,6 +163,60 @@ def cases_z_physics():
     return out
 
 
+def _gen_ini(problem, mesh, bcs=("periodic", "periodic", "periodic"), physics=None, extra=None):
+    sec = {"mesh": dict(mesh),
+           "run": {"tend": 0.1, "boundaries_x": bcs[0], "boundaries_y": bcs[1], "boundaries_z": bcs[2]},
+           "solvers": {"riemann_solver": "hllc", "reconstruction": "plm", "CFL": 0.1},
+           "physics": dict({"gamma0": 1.4, "problem": problem}, **(physics or {}))}
+    sec.update(extra or {})
+    return problems.ini_text(sec)
+
+
+def generator_cases():
+    """(name, ini text): every generator of Init.h, on 2-D planes and 3-D
+    grids, with the parameter ranges of the reference's settings files."""
+    unit3 = {"xmin": 0.0, "xmax": 1.0, "ymin": 0.0, "ymax": 1.0, "zmin": 0.0, "zmax": 1.0}
+    refl = ("reflecting",) * 3
+    out = [
+        ("sod_x_3d", _gen_ini("sod_x", dict(unit3, Nx=32, Ny=4, Nz=4), refl, {"gamma0": 1.666666667})),
+        ("sod_y_xy", _gen_ini("sod_y", dict(unit3, Nx=8, Ny=32, Nz=1), refl, {"gamma0": 1.666666667})),
+        ("sod_z_xz", _gen_ini("sod_z", dict(unit3, Nx=8, Ny=1, Nz=33), refl)),
+        ("blast_3d", _gen_ini("blast", dict(unit3, Nx=16, Ny=16, Nz=16))),
+        ("blast_xy", _gen_ini("blast", dict(unit3, Nx=40, Ny=24, Nz=1))),
+        ("diffusion_xy", _gen_ini("diffusion", dict(unit3, Nx=32, Ny=32, Nz=1),
+                                  extra={"viscosity": {"active": True, "mu": 0.01}})),
+        ("diffusion_3d", _gen_ini("diffusion", dict(unit3, Nx=12, Ny=10, Nz=14))),
+        ("rt_xz", _gen_ini("rayleigh-taylor", {"Nx": 16, "Ny": 1, "Nz": 48, "xmin": -0.25, "xmax": 0.25,
+                                               "zmin": -0.75, "zmax": 0.75}, refl,
+                           {"gravity": True, "g": -0.1})),
+        ("rt_3d", _gen_ini("rayleigh-taylor", {"Nx": 10, "Ny": 6, "Nz": 30, "xmin": -0.25, "xmax": 0.25,
+                                               "ymin": -0.25, "ymax": 0.25, "zmin": -0.75, "zmax": 0.75},
+                           ("periodic", "periodic", "reflecting"), {"gravity": True, "g": -0.1})),
+        ("h84_3d", _gen_ini("H84", {"Nx": 16, "Ny": 8, "xmin": 0.0, "xmax": 4.0, "ymin": 2.0, "ymax": 3.0},
+                            ("periodic", "reflecting", "periodic"), {"gamma0": 1.66666667, "gravity": True, "g": 2.0},
+                            {"H84": {"perturbation": 1.0e-4}, "polytrope": {"m1": 1.5}})),
+        ("c91_3d", _gen_ini("C91", {"Nx": 16, "Ny": 16, "Nz": 8, "xmin": 0.0, "xmax": 4.0, "ymin": 0.0, "ymax": 4.0,
+                                    "zmin": 0.0, "zmax": 1.0}, ("periodic", "periodic", "C91"),
+                            {"gamma0": 1.66666667, "gravity": True, "g": 40.0},
+                            {"C91": {"perturbation": 1.0e-3}, "polytrope": {"theta1": 20.0, "m1": 1.0}})),
+    ]
+    return out
+
+
+def generators():
+    tmp = tempfile.mkdtemp()
+    out = {}
+    for name, ini in generator_cases():
+        path = os.path.join(tmp, name + ".ini")
+        with open(path, "w") as f:
+            f.write(ini)
+        ref = pyoracle.RefOracle(path)
+        out[name] = np.stack(ref.generate())
+        out[name + "__ini"] = np.array(ini)
+        print(name, out[name].shape)
+    return out
+
+
 def riemann_kats(seed=2024, n=600):
     """State pairs over every branch: subsonic, supersonic left/right moving,
     strong contrasts, and exact ties."""
@@ -206,6 +265,8 @@ def main(only=None):
         print(pr.name, q0.shape, dts[:2])
     if not only:
         np.savez_compressed(os.path.join(HERE, "riemann_kats.npz"), **riemann_kats())
+    if not only or "generators" in only:
+        np.savez_compressed(os.path.join(HERE, "generators.npz"), **generators())
     with open(os.path.join(HERE, "index.json"), "w") as f:
         json.dump(index, f, indent=1)
 

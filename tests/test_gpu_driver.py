@@ -1,9 +1,10 @@
 """The fv3d driver binary: the main.cpp:51-74 loop on the GPU, from a .ini.
 
 Runs fv3d_gb300/_lib/fv3d on a Sod tube settings file (the reference's own
-`sod_x` generator, Init.h:19-31) and checks the final snapshot against the
-oracle's loop over the same settings: same number of saves, bit-identical
-final primitive state.  Both the host loop (one compute_dt/step round trip
+`sod_x` generator, Init.h:19-31, run on the GPU by fvgpu_init_problem) and
+checks the final snapshot against the oracle's loop over the same settings
+from the oracle's own generator: same number of saves, bit-identical final
+primitive state.  Both the host loop (one compute_dt/step round trip
 per step, like main.cpp) and --device-loop are run.  Two 3-D settings files
 shaped like the reference's settings/sod_x.ini (64 x 16 x 16, reflecting,
 PCM, Euler) and settings/blast.ini (periodic cube, PCM, HLLC, CFL 0.1),
@@ -102,9 +103,9 @@ def test_driver_matches_oracle(tmp_path, mode):
     assert len(snaps) == r.stdout.count("Saving at time") + 1
 
     p = fv.parse_ini(INI)
-    pr = problems.sod(64, "x", nx_other=8)
     ora = pyoracle.Oracle(p)
-    ora.set_prim(*pr.prim)
+    q0 = ora.generate()
+    np.testing.assert_array_equal(np.stack(q0), np.stack(problems.sod(64, "x", nx_other=8).prim))
     t_o, n_o = ora.advance(p.tend)
     assert (steps, t_end) == (n_o, t_o)
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, 1, 8, 64)
@@ -175,7 +176,7 @@ def test_driver_3d_matches_oracle(tmp_path, problem):
     snaps = sorted(f for f in os.listdir(tmp_path) if re.fullmatch(r"snap_\d{4}\.bin", f))
     p = fv.parse_ini(text)
     ora = pyoracle.Oracle(p)
-    ora.set_prim(*_ic_3d(p, problem))
+    np.testing.assert_array_equal(np.stack(ora.generate()), np.stack(_ic_3d(p, problem)))
     t_o, n_o = ora.advance(p.tend)
     assert (steps, t_end) == (n_o, t_o)
     got = np.fromfile(str(tmp_path / snaps[-1]), dtype=np.float64).reshape(5, p.Nz, p.Ny, p.Nx)
