@@ -78,6 +78,7 @@ def _declare(lib):
         "fvgpu_get_cons": (C.c_int, [vp] + [_dp] * 5),
         "fvgpu_init_problem": (C.c_int, [vp]),
         "fvgpu_generate": (C.c_int, [P] + [_dp] * 5),
+        "fv_h5_save": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double] + [_dp] * 5),
         "fvgpu_compute_dt": (C.c_int, [vp, _dp, _dp]),
         "fvgpu_step": (C.c_int, [vp, C.c_double]),
         "fvgpu_advance": (C.c_int, [vp, C.c_double, C.c_long, _dp, C.POINTER(C.c_long)]),
@@ -145,6 +146,18 @@ def generate(params):
     if rc:
         raise FvError(rc, "fvgpu_generate(%r)" % params.problem)
     return arrs
+
+
+def save_solution(params, path, iteration, t, prim):
+    """IOManager::saveSolution (IOManager.h:88-192) through fv_h5_save: the
+    primitives (rho, u, v, w, p; each [Nz][Ny][Nx]) as group ite_<iteration>
+    of the HDF5 file `path` (iteration 0 creates it)."""
+    shape = (params.Nz, params.Ny, params.Nx)
+    arrs = [_as_field(a, shape) for a in prim]
+    rc = load_library().fv_h5_save(C.byref(params), os.fspath(path).encode(), int(iteration), float(t),
+                                   *[_ptr(a) for a in arrs])
+    if rc:
+        raise FvError(rc, "fv_h5_save(%s)" % os.fspath(path))
 
 
 def parse_ini(text):

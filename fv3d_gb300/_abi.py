@@ -15,6 +15,9 @@ FV_VSC_CONSTANT = 0
 FV_PREC_FP64, FV_PREC_FP32_MIXED = 0, 1
 FV_PHYS_REFERENCE, FV_PHYS_CORRECTED = 0, 1
 
+FV_OK, FV_ERR_PARAM, FV_ERR_UNSUPPORTED, FV_ERR_CUDA, FV_ERR_NONFINITE = 0, 1, 2, 3, 4
+FV_ERR_NOMEM, FV_ERR_IO, FV_ERR_TIMEOUT, FV_ERR_STATE = 5, 6, 7, 8
+
 STATUS_NAMES = {
     0: "FV_OK",
     1: "FV_ERR_PARAM",

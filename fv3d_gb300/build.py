@@ -29,7 +29,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["fv_stage2d.cu", "fv_stage3d.cu", "fv_stage3d32.cu", "fv_batch64.cu", "fv_batch32.cu", "fv_aux.cu", "fv_api.cpp", "fv_ini.cpp",
-               "fv_batch.cpp", "fv_noalloc.cu", "fv_probe.cu", "fv_init.cu"]
+               "fv_batch.cpp", "fv_noalloc.cu", "fv_probe.cu", "fv_init.cu", "fv_h5.cpp"]
 DRIVER_SOURCES = ["fv3d_main.cpp"]
 FP64_EXACT_SOURCES = {"fv_stage2d.cu", "fv_stage3d.cu", "fv_batch64.cu", "fv_aux.cu", "fv_init.cu"}
 # the FP32-mixed kernels: approximate FP32 division/sqrt, FMA contraction

@@ -2,7 +2,7 @@
 // main.cpp (main.cpp:12-89) on the GB300 path.
 //
 //   fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop]
-//                     [--write-ic state.bin] [--restart]
+//                     [--write-ic state.bin] [--restart] [--format h5|raw]
 //
 // Reads the same .ini file (readInifile semantics), sets the initial state,
 // and runs the reference's time loop: while (t + epsilon < tend) { dt =
@@ -18,11 +18,11 @@
 // from a raw file of 5 float64 arrays (rho, u, v, w, p), each Nz*Ny*Nx in C
 // order; --write-ic writes the generated state in that format (generated
 // into host arrays with fvgpu_generate, then set with fvgpu_set_prim: the
-// same state).  Snapshots
-// are written as the same raw format (<prefix>_<ite>.bin) instead of HDF5,
-// with the vertex coordinates in <prefix>_grid.bin and an XDMF index
-// (<prefix>.xdmf) shaped like the reference's, so XDMF readers (ParaView,
-// VisIt) open the series.
+// same state).  Snapshots go, as the reference's IOManager writes them, to
+// <prefix>.h5 (fv_h5_save: group ite_<n> per save) with an XDMF index
+// <prefix>.xdmf naming its datasets; --format raw writes them as the raw
+// format above instead (<prefix>_<ite>.bin, vertex coordinates in
+// <prefix>_grid.bin) with the XDMF index pointing into those files.
 //
 // --device-loop runs the steps between two saves with fvgpu_advance (dt stays
 // on the GPU) instead of one compute_dt/step round trip per step.
@@ -100,16 +100,28 @@ bool WriteGrid(const std::string& path, const fv_params& p) {
 
 // The XDMF index of the snapshots, laid out like the reference's
 // (IOManager.h:16-77: a temporal collection over one 3DSMesh / X_Y_Z
-// geometry; per save rho, a velocity vector joined from u, v, w, and prs),
-// with its data items pointing into the raw files (Format="Binary", Seek =
-// byte offset of the field) instead of HDF5 datasets.
-bool WriteXdmf(const std::string& path, const fv_params& p, const std::string& grid,
+// geometry; per save rho, a velocity vector joined from u, v, w, and prs).
+// Its data items name the HDF5 datasets of `h5` (Format="HDF",
+// file:/ite_<n>/rho, as the reference's) or, with `h5` empty, point into the
+// raw files (Format="Binary", Seek = byte offset of the field; `grid` holds
+// the vertex coordinates).
+bool WriteXdmf(const std::string& path, const fv_params& p, const std::string& grid, const std::string& h5,
                const std::vector<std::pair<std::string, double>>& snaps) {
   FILE* f = std::fopen(path.c_str(), "w");
   if (!f) return false;
   const int nx = p.Nx, ny = p.Ny, nz = p.Nz;
   const size_t nv = (size_t)(nx + 1) * (ny + 1) * (nz + 1), nc = (size_t)nx * ny * nz;
-  auto item = [&](const std::string& file, size_t seek, int a, int b, int c) {
+  static const char* kField[5] = {"rho", "u", "v", "w", "prs"};
+  // field v (0-4: rho, u, v, w, prs of save n; 5-7: x, y, z) with extents a x b x c
+  auto item = [&](size_t n, int v, int a, int b, int c) {
+    if (!h5.empty()) {
+      const std::string ds = v >= 5 ? std::string(1, "xyz"[v - 5]) : "ite_" + std::to_string(n) + "/" + kField[v];
+      std::fprintf(f, "<DataItem Dimensions=\"%d %d %d\" NumberType=\"Float\" Precision=\"8\" Format=\"HDF\">%s:/%s"
+                      "</DataItem>", a, b, c, h5.c_str(), ds.c_str());
+      return;
+    }
+    const std::string& file = v >= 5 ? grid : snaps[n].first;
+    const size_t seek = v >= 5 ? (size_t)(v - 5) * nv * sizeof(double) : (size_t)v * nc * sizeof(double);
     std::fprintf(f,
                  "<DataItem Dimensions=\"%d %d %d\" NumberType=\"Float\" Precision=\"8\" Format=\"Binary\" "
                  "Endian=\"Little\" Seek=\"%zu\">%s</DataItem>",
@@ -123,30 +135,31 @@ bool WriteXdmf(const std::string& path, const fv_params& p, const std::string& g
                nz + 1, ny + 1, nx + 1);
   for (int a = 0; a < 3; ++a) {
     std::fprintf(f, "      ");
-    item(grid, a * nv * sizeof(double), nz + 1, ny + 1, nx + 1);
+    item(0, 5 + a, nz + 1, ny + 1, nx + 1);
     std::fprintf(f, "\n");
   }
   std::fprintf(f, "    </Geometry>\n");
-  for (const auto& sn : snaps) {
+  for (size_t n = 0; n < snaps.size(); ++n) {
+    const auto& sn = snaps[n];
     std::fprintf(f,
                  "    <Grid Name=\"Cells\" GridType=\"Uniform\">\n      <Time TimeType=\"Single\" Value=\"%.17g\" />\n"
                  "      <Topology Reference=\"//Topology[@Name='Main Topology']\" />\n"
                  "      <Geometry Reference=\"//Geometry[@Name='Main Geometry']\" />\n",
                  sn.second);
     std::fprintf(f, "      <Attribute Name=\"rho\" AttributeType=\"Scalar\" Center=\"Cell\">\n        ");
-    item(sn.first, 0, nz, ny, nx);
+    item(n, 0, nz, ny, nx);
     std::fprintf(f, "\n      </Attribute>\n");
     std::fprintf(f, "      <Attribute Name=\"velocity\" AttributeType=\"Vector\" Center=\"Cell\">\n"
                     "        <DataItem Dimensions=\"%d %d %d 3\" ItemType=\"Function\" Function=\"JOIN($0, $1, $2)\">\n",
                  nz, ny, nx);
     for (int v = 1; v <= 3; ++v) {
       std::fprintf(f, "          ");
-      item(sn.first, v * nc * sizeof(double), nz, ny, nx);
+      item(n, v, nz, ny, nx);
       std::fprintf(f, "\n");
     }
     std::fprintf(f, "        </DataItem>\n      </Attribute>\n");
     std::fprintf(f, "      <Attribute Name=\"prs\" AttributeType=\"Scalar\" Center=\"Cell\">\n        ");
-    item(sn.first, 4 * nc * sizeof(double), nz, ny, nx);
+    item(n, 4, nz, ny, nx);
     std::fprintf(f, "\n      </Attribute>\n    </Grid>\n");
   }
   std::fprintf(f, "  </Grid>\n</Domain>\n</Xdmf>\n");
@@ -200,17 +213,20 @@ int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr,
                  "usage: fv3d settings.ini [--ic state.bin] [--out prefix] [--device-loop] [--write-ic state.bin] "
-                 "[--restart]\n");
+                 "[--restart] [--format h5|raw]\n");
     return 2;
   }
   std::string ini = argv[1], ic, out, write_ic;
-  bool device_loop = false, restart = false;
+  bool device_loop = false, restart = false, raw = false;
   for (int a = 2; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--ic") && a + 1 < argc) ic = argv[++a];
     else if (!std::strcmp(argv[a], "--restart")) restart = true;
     else if (!std::strcmp(argv[a], "--out") && a + 1 < argc) out = argv[++a];
     else if (!std::strcmp(argv[a], "--device-loop")) device_loop = true;
     else if (!std::strcmp(argv[a], "--write-ic") && a + 1 < argc) write_ic = argv[++a];
+    else if (!std::strcmp(argv[a], "--format") && a + 1 < argc && (!std::strcmp(argv[a + 1], "h5") ||
+                                                                   !std::strcmp(argv[a + 1], "raw")))
+      raw = !std::strcmp(argv[++a], "raw");
     else {
       std::fprintf(stderr, "unknown argument %s\n", argv[a]);
       return 2;
@@ -266,12 +282,20 @@ int main(int argc, char** argv) {
   auto save = [&](double tt, bool announce, double next) {
     fvgpu_get_prim(s, q.f[0].data(), q.f[1].data(), q.f[2].data(), q.f[3].data(), q.f[4].data());
     char name[512];
-    std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite++);
+    std::snprintf(name, sizeof(name), "%s_%04d.bin", out.c_str(), ite);
     if (announce) std::printf(" - Saving at time %g\n", tt);
-    if (snaps.empty()) WriteGrid(grid, p);
-    WriteRaw(name, q);
     snaps.emplace_back(BaseName(name), tt);
-    WriteXdmf(out + ".xdmf", p, BaseName(grid), snaps);
+    if (raw) {
+      if (snaps.size() == 1) WriteGrid(grid, p);
+      WriteRaw(name, q);
+      WriteXdmf(out + ".xdmf", p, BaseName(grid), "", snaps);
+    } else {  // IOManager::saveSolution: <out>.h5, group ite_<n>
+      const int rc = fv_h5_save(&p, (out + ".h5").c_str(), ite, tt, q.f[0].data(), q.f[1].data(), q.f[2].data(),
+                                q.f[3].data(), q.f[4].data());
+      if (rc != FV_OK) std::fprintf(stderr, "cannot write %s.h5 (%s)\n", out.c_str(), fv_status_string(rc));
+      WriteXdmf(out + ".xdmf", p, "", BaseName(out) + ".h5", snaps);
+    }
+    ++ite;
     Checkpoint c;
     c.t = tt;
     c.next_save = next;

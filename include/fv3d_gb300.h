@@ -118,6 +118,17 @@ const char* fv_status_string(int status);
 int fv_read_ini(const char* path, fv_params* out);
 int fv_parse_ini(const char* text, fv_params* out);
 
+/* IOManager::saveSolution (IOManager.h:88-192) for interior primitive arrays
+ * ([Nz][Ny][Nx]): the reference's HDF5 snapshot file at `path` -- root
+ * attributes Ntx..kend (int) and problem (string), vertex datasets x, y, z,
+ * and a group ite_<iteration> with datasets rho, u, v, w, prs and a time
+ * attribute.  iteration 0 creates (truncates) the file, later iterations
+ * add their group to it.  Written without an HDF5 library, in the original
+ * HDF5 format (superblock 0, symbol-table groups, contiguous datasets).
+ * FV_ERR_IO when the file cannot be written or is not one this call made. */
+int fv_h5_save(const fv_params* params, const char* path, int iteration, double t, const double* rho,
+               const double* u, const double* v, const double* w, const double* prs);
+
 /* ---- single problem --------------------------------------------------- */
 typedef struct fv_sim fv_sim;
 

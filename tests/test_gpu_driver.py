@@ -93,7 +93,7 @@ def test_driver_matches_oracle(tmp_path, mode):
     ini = tmp_path / "sod.ini"
     ini.write_text(INI)
     prefix = str(tmp_path / "snap")
-    args = [exe, str(ini), "--out", prefix] + (["--device-loop"] if mode == "device" else [])
+    args = [exe, str(ini), "--out", prefix, "--format", "raw"] + (["--device-loop"] if mode == "device" else [])
     r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "Computing dts at (t=0)" in r.stdout
@@ -168,8 +168,8 @@ def test_driver_3d_matches_oracle(tmp_path, problem):
     ini = tmp_path / "run.ini"
     ini.write_text(text)
     prefix = str(tmp_path / "snap")
-    r = subprocess.run([exe, str(ini), "--out", prefix, "--device-loop"], capture_output=True, text=True,
-                       timeout=300)
+    r = subprocess.run([exe, str(ini), "--out", prefix, "--device-loop", "--format", "raw"], capture_output=True,
+                       text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
@@ -277,8 +277,8 @@ def test_driver_random_generators_match_oracle(tmp_path, problem):
     ini.write_text(text)
     prefix = str(tmp_path / "snap")
     ic = str(tmp_path / "ic.bin")
-    r = subprocess.run([exe, str(ini), "--out", prefix, "--write-ic", ic, "--device-loop"], capture_output=True,
-                       text=True, timeout=300)
+    r = subprocess.run([exe, str(ini), "--out", prefix, "--write-ic", ic, "--device-loop", "--format", "raw"],
+                       capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps, t_end = int(m.group(1)), float(m.group(2))
@@ -308,13 +308,15 @@ def test_driver_rejects_unknown_problem(tmp_path):
     assert "unknown problem" in r.stderr
 
 
+@pytest.mark.parametrize("fmt", ["raw", "h5"])
 @pytest.mark.parametrize("mode", ["host", "device"])
-def test_driver_restart_continues_bit_for_bit(tmp_path, mode):
+def test_driver_restart_continues_bit_for_bit(tmp_path, mode, fmt):
     """A run stopped at tend/2 and resumed with --restart ends in the same
     state, bit for bit, as the uninterrupted run (the checkpoint holds the
-    conserved state), and the XDMF index keeps every snapshot."""
+    conserved state), and the XDMF index (raw) or the HDF5 file keeps every
+    snapshot."""
     exe = os.path.join(build.lib_dir(), "fv3d")
-    extra = ["--device-loop"] if mode == "device" else []
+    extra = (["--device-loop"] if mode == "device" else []) + ["--format", fmt]
     full = tmp_path / "full"
     part = tmp_path / "part"
     full.mkdir()
@@ -335,12 +337,59 @@ def test_driver_restart_continues_bit_for_bit(tmp_path, mode):
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     assert int(m.group(1)) == n_full > n_half
+    if fmt == "h5":
+        from fv3d_gb300 import snapshots
+        a, b = snapshots.File(str(full / "snap.h5")), snapshots.File(str(part / "snap.h5"))
+        assert sorted(a.keys()) == sorted(b.keys())
+        for k in a.keys():
+            if not k.startswith("ite_"):
+                continue
+            assert a[k].attrs["time"] == b[k].attrs["time"]
+            for field in ("rho", "u", "v", "w", "prs"):
+                np.testing.assert_array_equal(a[k + "/" + field], b[k + "/" + field])
+        return
     last = lambda d: sorted(f for f in os.listdir(d) if re.fullmatch(r"snap_\d{4}\.bin", f))[-1]
     a = np.fromfile(str(full / last(full)), dtype=np.float64)
     b = np.fromfile(str(part / last(part)), dtype=np.float64)
     np.testing.assert_array_equal(a, b)
     nsnaps = len([f for f in os.listdir(part) if re.fullmatch(r"snap_\d{4}\.bin", f)])
     _check_xdmf(part, (1, 8, 64), nsnaps)
+
+
+def test_driver_hdf5_snapshots_equal_raw(tmp_path):
+    """The default output, <out>.h5 in the reference's layout (root
+    attributes, x / y / z, ite_<n>/{rho,u,v,w,prs} with a time attribute)
+    with an XDMF index naming its datasets, holds what --format raw writes."""
+    exe = os.path.join(build.lib_dir(), "fv3d")
+    ini = tmp_path / "sod.ini"
+    ini.write_text(INI)
+    for fmt, d in (("raw", "raw"), ("h5", "h5")):
+        (tmp_path / d).mkdir()
+        r = subprocess.run([exe, str(ini), "--out", str(tmp_path / d / "snap")] + (["--format", fmt] if fmt == "raw"
+                                                                                   else []),
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+    assert not any(f.endswith(".bin") and f.startswith("snap_") for f in os.listdir(tmp_path / "h5"))
+    from fv3d_gb300 import snapshots
+    h5 = snapshots.File(str(tmp_path / "h5" / "snap"))
+    raw = snapshots.File(str(tmp_path / "raw" / "snap"))
+    assert isinstance(raw, snapshots.File) and not isinstance(h5, snapshots.File)
+    assert sorted(h5.keys()) == sorted(raw.keys())
+    p = fv.parse_ini(INI)
+    for k in ("Nx", "Ny", "Nz", "Ntx", "Nty", "Ntz", "ibeg", "iend", "jbeg", "jend", "kbeg", "kend"):
+        assert h5.attrs[k] == raw.attrs[k]
+    assert h5.attrs["problem"] == b"sod_x" and p.Nx == h5.attrs["Nx"]
+    for k in ("x", "y", "z"):
+        np.testing.assert_array_equal(h5[k], raw[k])
+    for k in raw.keys():
+        if k.startswith("ite_"):
+            assert h5[k].attrs["time"] == raw[k].attrs["time"]
+            for field in ("rho", "u", "v", "w", "prs"):
+                np.testing.assert_array_equal(h5[k + "/" + field], raw[k + "/" + field])
+    import xml.etree.ElementTree as ET
+    items = [d.text for d in ET.parse(str(tmp_path / "h5" / "snap.xdmf")).getroot().iter("DataItem")
+             if d.get("Format") == "HDF"]
+    assert items[:3] == ["snap.h5:/x", "snap.h5:/y", "snap.h5:/z"] and "snap.h5:/ite_0/rho" in items
 
 
 def test_driver_restart_needs_a_checkpoint(tmp_path):

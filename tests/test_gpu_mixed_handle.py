@@ -105,8 +105,8 @@ def test_driver_runs_the_mixed_form(tmp_path):
     ini.write_text(SOD_MIXED)
     prefix = str(tmp_path / "snap")
     ic = str(tmp_path / "ic.bin")
-    r = subprocess.run([exe, str(ini), "--out", prefix, "--write-ic", ic, "--device-loop"], capture_output=True,
-                       text=True, timeout=300)
+    r = subprocess.run([exe, str(ini), "--out", prefix, "--write-ic", ic, "--device-loop", "--format", "raw"],
+                       capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     steps = int(m.group(1))
