@@ -271,6 +271,7 @@ int main(int argc, char** argv) {
     return 1;
   }
   const bool fp64 = p.precision == FV_PREC_FP64;
+  for (auto& a : q.f) a.resize(n);  // host copy of the state for the saves (empty after an on-device start)
 
   double t = ck.t, dt = 0.0, next_save = ck.next_save;
   int ite = ck.ite, next_log = ck.next_log;
