@@ -338,15 +338,18 @@ def test_driver_restart_continues_bit_for_bit(tmp_path, mode, fmt):
     m = re.search(r"done: (\d+) steps, t = (\S+)", r.stdout)
     assert int(m.group(1)) == n_full > n_half
     if fmt == "h5":
+        # the final saves hold the same state; the resumed file keeps every
+        # save of both legs (the first leg's final save included), in order
         from fv3d_gb300 import snapshots
         a, b = snapshots.File(str(full / "snap.h5")), snapshots.File(str(part / "snap.h5"))
-        assert sorted(a.keys()) == sorted(b.keys())
-        for k in a.keys():
-            if not k.startswith("ite_"):
-                continue
-            assert a[k].attrs["time"] == b[k].attrs["time"]
-            for field in ("rho", "u", "v", "w", "prs"):
-                np.testing.assert_array_equal(a[k + "/" + field], b[k + "/" + field])
+        ka = sorted((k for k in a.keys() if k.startswith("ite_")), key=lambda k: int(k[4:]))
+        kb = sorted((k for k in b.keys() if k.startswith("ite_")), key=lambda k: int(k[4:]))
+        assert kb == ["ite_%d" % i for i in range(len(kb))] and len(kb) == len(ka) + 1
+        assert a[ka[-1]].attrs["time"] == b[kb[-1]].attrs["time"]
+        for field in ("rho", "u", "v", "w", "prs"):
+            np.testing.assert_array_equal(a[ka[-1] + "/" + field], b[kb[-1] + "/" + field])
+        times = [b[k].attrs["time"] for k in kb]
+        assert times == sorted(times)
         return
     last = lambda d: sorted(f for f in os.listdir(d) if re.fullmatch(r"snap_\d{4}\.bin", f))[-1]
     a = np.fromfile(str(full / last(full)), dtype=np.float64)
@@ -369,7 +372,7 @@ def test_driver_hdf5_snapshots_equal_raw(tmp_path):
                                                                                    else []),
                            capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
-    assert not any(f.endswith(".bin") and f.startswith("snap_") for f in os.listdir(tmp_path / "h5"))
+    assert not any(re.fullmatch(r"snap_\d{4}\.bin", f) for f in os.listdir(tmp_path / "h5"))
     from fv3d_gb300 import snapshots
     h5 = snapshots.File(str(tmp_path / "h5" / "snap"))
     raw = snapshots.File(str(tmp_path / "raw" / "snap"))
