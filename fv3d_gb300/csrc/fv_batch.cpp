@@ -53,7 +53,7 @@ constexpr int kMultiChunk = 256;  // steps per multi-step launch of a loop with 
 
 struct Group {
   int ndim = 2;     // 3: 3-D problems (one kernel shape, grouped by solver)
-  int rs = -1;      // 3-D groups: the shared Riemann solver
+  int rs = -1;      // 3-D groups: the shared Riemann solver (bit 0) and corrected physics (bit 1)
   int plane = 0;
   bool wact = false;
   bool tc = false;
@@ -224,7 +224,7 @@ std::string GroupKey(const fv_batch* b, const Group& g) {
     cells += (long long)s.first * s.second;
   }
   std::ostringstream k;
-  k << "p" << b->precision << "_d" << g.ndim << "_pl" << g.plane << "_w" << g.wact << "_tc" << g.tc << "_v" << visc << "_rs"
+  k << "p" << b->precision << "_d" << g.ndim << "_co" << (g.rs >= 2) << "_pl" << g.plane << "_w" << g.wact << "_tc" << g.tc << "_v" << visc << "_rs"
     << rs_mask << "_ts" << b->ts << "_n" << g.members.size() << "_c" << cells << "_h" << std::hex << h;
   return k.str();
 }
@@ -264,7 +264,8 @@ Schedule Schedule3d(const fv_batch* b, int layers) {
 
 int Occupancy(const fv_batch* b, const Group& g, int shape) {
   if (g.ndim == 3)
-    return b->precision == FV_PREC_FP64 ? fv::batch_stage3d_occupancy64(g.tc) : fv::batch_stage3d_occupancy32(g.tc);
+    return b->precision == FV_PREC_FP64 ? fv::batch_stage3d_occupancy64(g.rs, g.tc)
+                                        : fv::batch_stage3d_occupancy32(g.rs, g.tc);
   return b->precision == FV_PREC_FP64 ? fv::batch_stage_occupancy64(g.plane, g.wact, shape, g.tc)
                                       : fv::batch_stage_occupancy32(g.plane, g.wact, shape, g.tc);
 }
@@ -542,7 +543,7 @@ int Prepare(fv_batch* b) {
   ReleaseGroups(b);
   for (int i = 0; i < b->n; ++i) {
     const int ndim = b->G[i].ndim;
-    const int rs = ndim == 3 ? (b->p[i].riemann_solver == FV_HLL ? 0 : 1) : -1;
+    const int rs = ndim == 3 ? (b->p[i].riemann_solver == FV_HLL ? 0 : 1) + (b->G[i].corrected ? 2 : 0) : -1;
     Group* g = nullptr;
     for (auto& h : b->groups)
       if (h.ndim == ndim && h.rs == rs && h.plane == b->G[i].plane && h.wact == (bool)b->wact[i]) g = &h;
@@ -720,8 +721,6 @@ int fvgpu_batch_create(const fv_params* params, int n, fv_batch** out) {
     int rc = fv::configure_grid(q, &b->G[i], &b->inv_tc[i], &b->inv_visc[i], &b->deg_bc[i], &err);
     if (rc) return Fail(b, rc, "problem %d: %s", i, err.c_str());
     if (b->G[i].ndim == 3) {
-      if (b->G[i].corrected)
-        return Fail(b, FV_ERR_UNSUPPORTED, "problem %d: corrected physics runs with fvgpu_create", i);
       const int n_ax[3] = {params[i].Nx, params[i].Ny, params[i].Nz};
       const int bc_ax[3] = {params[i].boundary_x, params[i].boundary_y, params[i].boundary_z};
       for (int a = 0; a < 3; ++a)

@@ -192,8 +192,9 @@ cudaError_t launch_batch_stage3d64(const BatchInst* insts, int ninst, int ntiles
                                    int rs, int grid, bool tc, cudaStream_t stream);
 cudaError_t launch_batch_stage3d32(const BatchInst* insts, int ninst, int ntiles, unsigned* queue, int kind, int flip,
                                    int rs, int grid, bool tc, cudaStream_t stream);
-int batch_stage3d_occupancy64(bool tc);
-int batch_stage3d_occupancy32(bool tc);
+// rs: Riemann solver (bit 0), corrected physics (bit 1).
+int batch_stage3d_occupancy64(int rs, bool tc);
+int batch_stage3d_occupancy32(int rs, bool tc);
 
 // Several RK2 steps of a group of FP32-mixed 2-D problems in one cooperative
 // launch (fv_batch32.cu, batch_multi32): for small grids, whose steps are

@@ -690,8 +690,8 @@ static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
 // Persistent FP64 kernel over a group of 3-D problems (see
 // launch_batch_stage3d64): CTAs take work items from the queue counter, find
 // their problem by binary search over the first item numbers, and run the
-// same body as the one-problem kernel.
-template <int KIND, int RS>
+// same body as the one-problem kernel (CORR: the corrected physics).
+template <int KIND, int RS, bool CORR>
 __global__ void __launch_bounds__(kThreads, FV_3D64_MIN_CTAS)
 batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int flip) {
   const int kind = KIND;
@@ -737,28 +737,35 @@ batch_stage3d64(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsi
     }
     // the group shares the solver (RS); the cell-size form is a uniform branch
     if (I.G.pow2_all)
-      stage3d_body<true, false>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
+      stage3d_body<true, CORR>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
     else
-      stage3d_body<false, false>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
+      stage3d_body<false, CORR>(I.G, uin, u0, uout, I.ctrl, RS, kind, bx, by, bz, I.tz, none, smem_raw, s_red);
   }
 }
 
 typedef void (*Batch3dKernel)(const BatchInst*, int, int, unsigned*, int);
 
-template <int RS>
+template <int RS, bool CORR>
 Batch3dKernel batch3d_kernel_rs(int kind) {
-  return kind == STAGE_EULER ? batch_stage3d64<STAGE_EULER, RS>
-                             : (kind == STAGE_RK_1 ? batch_stage3d64<STAGE_RK_1, RS> : batch_stage3d64<STAGE_RK_2, RS>);
+  return kind == STAGE_EULER ? batch_stage3d64<STAGE_EULER, RS, CORR>
+                             : (kind == STAGE_RK_1 ? batch_stage3d64<STAGE_RK_1, RS, CORR>
+                                                   : batch_stage3d64<STAGE_RK_2, RS, CORR>);
 }
 
+// rs: the Riemann solver (bit 0) and the corrected physics (bit 1).
 Batch3dKernel batch3d_kernel(int kind, int rs) {
-  return rs == 0 ? batch3d_kernel_rs<0>(kind) : batch3d_kernel_rs<1>(kind);
+  switch (rs & 3) {
+    case 0: return batch3d_kernel_rs<0, false>(kind);
+    case 1: return batch3d_kernel_rs<1, false>(kind);
+    case 2: return batch3d_kernel_rs<0, true>(kind);
+    default: return batch3d_kernel_rs<1, true>(kind);
+  }
 }
 
 bool batch3d_prepare() {
   static bool done = false;
   if (done) return true;
-  for (int rs = 0; rs < 2; ++rs)
+  for (int rs = 0; rs < 4; ++rs)
     for (int k = 0; k < 3; ++k)
       if (cudaFuncSetAttribute(batch3d_kernel(k, rs), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)Smem3::bytes(true)) != cudaSuccess)
@@ -771,10 +778,10 @@ bool batch3d_prepare() {
 
 int batch3d_columns() { return kTX; }
 
-int batch_stage3d_occupancy64(bool tc) {
+int batch_stage3d_occupancy64(int rs, bool tc) {
   if (!batch3d_prepare()) return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch3d_kernel(STAGE_RK_2, 1), kThreads, Smem3::bytes(tc)) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch3d_kernel(STAGE_RK_2, rs), kThreads, Smem3::bytes(tc)) !=
       cudaSuccess)
     return 0;
   return nb;

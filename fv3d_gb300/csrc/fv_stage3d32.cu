@@ -180,7 +180,7 @@ __device__ __forceinline__ void unslot3f(const float f[5], float out[5]) {
   }
 }
 
-template <int DIR>
+template <int DIR, bool CORR>
 __device__ __forceinline__ void face3f(const float c[4][5], int rs, int recon, const Grid& G, float out[5],
                                        float* pout) {
   float qL[5], qR[5];
@@ -204,7 +204,7 @@ __device__ __forceinline__ void face3f(const float c[4][5], int rs, int recon, c
   if (rs == 0)
     hll32(L, R, G.gamma_f, G.inv_gm1_f, f, pout);
   else
-    hllc32(L, R, G.gamma_f, G.inv_gm1_f, f, pout);
+    hllc32<CORR>(L, R, G.gamma_f, G.inv_gm1_f, f, pout);
   unslot3f<DIR>(f, out);
 }
 
@@ -216,11 +216,12 @@ struct RingVelF {
   }
 };
 
-// One mixed stage of the columns (bx, by), z chunk bz of tz layers.  Inputs
+// One mixed stage of the columns (bx, by), z chunk bz of tz layers (CORR:
+// the corrected physics, as the FP64 kernel's).  Inputs
 // per kind as the 2-D mixed tile: RK_1 reads U^n pairs and writes U*; RK_2
 // reads U* and U^n and writes U^n+1 over U^n; Euler reads pairs `src` and
 // writes pairs `dst`.
-template <int RS>
+template <int RS, bool CORR>
 __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields& M, float2* const src[5],
                                                float2* const dst[5], StepCtrl* ctrl, int kind, int bx, int by, int bz,
                                                int tz, float* smem, unsigned long long* s_red) {
@@ -265,7 +266,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
     for (int m = 0; m < 4; ++m)
 #pragma unroll
       for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k0 - 2 + m), v, cy + 2, cx + 2);
-    face3f<2>(c, RS, recon, G, fzL, need_pout ? &poutL : nullptr);
+    face3f<2, CORR>(c, RS, recon, G, fzL, need_pout ? &poutL : nullptr);
   }
   __syncthreads();
 
@@ -284,7 +285,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + 2, fx + m);
-        face3f<0>(c, RS, recon, G, f, nullptr);
+        face3f<0, CORR>(c, RS, recon, G, f, nullptr);
 #pragma unroll
         for (int v = 0; v < 5; ++v) S.fa(v, fy, fx) = f[v];
       } else {
@@ -294,7 +295,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(sk, v, fy + m, fx + 2);
-        face3f<1>(c, RS, recon, G, f, nullptr);
+        face3f<1, CORR>(c, RS, recon, G, f, nullptr);
 #pragma unroll
         for (int v = 0; v < 5; ++v) S.fb(v, fy, fx) = f[v];
       }
@@ -309,7 +310,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
         for (int m = 0; m < 4; ++m)
 #pragma unroll
           for (int v = 0; v < 5; ++v) c[m][v] = S.q(slot_of(k - 1 + m), v, cy + 2, cx + 2);
-        face3f<2>(c, RS, recon, G, fzR, need_pout ? &poutR : nullptr);
+        face3f<2, CORR>(c, RS, recon, G, fzR, need_pout ? &poutR : nullptr);
       }
       const unsigned o = (unsigned)k * zstride + col;
       float fL[5], fR[5];
@@ -383,9 +384,15 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
       if (G.visc) {  // Viscosity.h:145-151
         const RingVelF P{S, k, cy + 2, cx + 2};
         float vf[3][5];
-        viscous3d<false, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
+        viscous3d<CORR, float>(P, G.inv_dx_f, G.inv_dy_f, G.inv_dz_f, G.mu_f, vf);
+        if (CORR) {  // the flux differences divided by the cell sizes
 #pragma unroll
-        for (int v = 1; v < 5; ++v) du[v] += (vf[0][v] + vf[1][v] + vf[2][v]) * dt;
+          for (int v = 1; v < 5; ++v)
+            du[v] += (vf[0][v] * G.inv_dx_f + vf[1][v] * G.inv_dy_f + vf[2][v] * G.inv_dz_f) * dt;
+        } else {
+#pragma unroll
+          for (int v = 1; v < 5; ++v) du[v] += (vf[0][v] + vf[1][v] + vf[2][v]) * dt;
+        }
       }
       if (kind == STAGE_RK_1) {
         float us[5];
@@ -426,7 +433,7 @@ __device__ __forceinline__ void stage3d_body32(const Grid& G, const MixedFields&
 
 static_assert(sizeof(BatchInst) % 8 == 0, "descriptor copied as 8-byte words");
 
-template <int RS>
+template <int RS, bool CORR>
 __global__ void __launch_bounds__(kThreads, 4)
 batch_stage3d32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsigned* queue, int kind, int flip) {
   extern __shared__ float smem_f[];
@@ -472,18 +479,26 @@ batch_stage3d32(const BatchInst* __restrict__ insts, int ninst, int ntiles, unsi
       src[v] = (kind == STAGE_EULER && flip) ? b : a;
       dst[v] = (kind == STAGE_EULER && !flip) ? b : a;
     }
-    stage3d_body32<RS>(I.G, M, src, dst, I.ctrl, kind, bx, by, bz, I.tz, smem_f, s_red);
+    stage3d_body32<RS, CORR>(I.G, M, src, dst, I.ctrl, kind, bx, by, bz, I.tz, smem_f, s_red);
   }
 }
 
 typedef void (*Batch3dKernel32)(const BatchInst*, int, int, unsigned*, int, int);
 
-Batch3dKernel32 kernel32(int rs) { return rs == 0 ? batch_stage3d32<0> : batch_stage3d32<1>; }
+// rs: the Riemann solver (bit 0) and the corrected physics (bit 1).
+Batch3dKernel32 kernel32(int rs) {
+  switch (rs & 3) {
+    case 0: return batch_stage3d32<0, false>;
+    case 1: return batch_stage3d32<1, false>;
+    case 2: return batch_stage3d32<0, true>;
+    default: return batch_stage3d32<1, true>;
+  }
+}
 
 bool prepare32() {
   static bool done = false;
   if (done) return true;
-  for (int rs = 0; rs < 2; ++rs)
+  for (int rs = 0; rs < 4; ++rs)
     if (cudaFuncSetAttribute(kernel32(rs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem3f::bytes(true)) !=
         cudaSuccess)
       return false;
@@ -493,10 +508,10 @@ bool prepare32() {
 
 }  // namespace
 
-int batch_stage3d_occupancy32(bool tc) {
+int batch_stage3d_occupancy32(int rs, bool tc) {
   if (!prepare32()) return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel32(1), kThreads, Smem3f::bytes(tc)) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel32(rs), kThreads, Smem3f::bytes(tc)) != cudaSuccess)
     return 0;
   return nb;
 }

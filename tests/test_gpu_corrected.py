@@ -104,3 +104,37 @@ def test_shear_wave_decays_at_the_viscous_rate():
     assert abs(ratio - expect) < 0.02, (ratio, expect)
     ratio_ref, _, _ = _shear_wave("reference")
     assert ratio_ref > 0.97, ratio_ref  # the reference's viscous term is 1/dy = 64x too weak
+
+
+def test_corrected_in_batches():
+    """Batches run the corrected mode on the 3-D batch kernels (FP64 and
+    FP32-mixed), side by side with reference-mode problems: an FP64 batch
+    member equals the same problem on its own handle bit for bit; the mixed
+    batch stays within the mixed tolerances of the FP64 batch."""
+    from _helpers import assert_mixed
+    prs = [CASES[n]() for n in sorted(CASES)]
+    plain = CASES["3d_hllc_visc"]()
+    plain.params.physics = fv._abi.FV_PHYS_REFERENCE
+    prs.append(plain)
+    b = fv.Batch([pr.params for pr in prs])
+    for i, pr in enumerate(prs):
+        b.set_prim(i, *pr.prim)
+    b.run(3)
+    singles = []
+    for i, pr in enumerate(prs):
+        sim = fv.Simulation(pr.params)
+        sim.set_prim(*pr.prim)
+        assert sim.advance(1.0e30, max_steps=3)[1] == 3
+        singles.append(sim.get_prim())
+        np.testing.assert_array_equal(np.stack(b.get_prim(i)), np.stack(singles[-1]))
+    mixed = []
+    for pr in prs:
+        q = pr.params.copy()
+        q.precision = fv._abi.FV_PREC_FP32_MIXED
+        mixed.append(q)
+    m = fv.Batch(mixed)
+    for i, pr in enumerate(prs):
+        m.set_prim(i, *pr.prim)
+    m.run(3)
+    for i, pr in enumerate(prs):
+        assert_mixed(m.get_prim(i), singles[i], pr.params.gamma0, "corrected batch %d" % i)
