@@ -108,10 +108,8 @@ def test_batch3d_mixed_close_to_fp64(nsteps):
 
 
 def test_batch3d_rejects_what_it_does_not_run():
-    pr = _rand3d("x", M(8, 8, 8), ("periodic",) * 3, "hllc", 604, extra={"gpu": {"physics": "corrected"}})
-    with pytest.raises(fv.FvError) as e:
-        fv.Batch([pr.params])
-    assert e.value.status == 2
+    # corrected physics runs in batches (tests/test_gpu_corrected.py); a
+    # reflecting one-cell axis and B02 conductivity do not
     pr = _rand3d("y", M(1, 8, 8), ("reflecting", "periodic", "periodic"), "hllc", 605)
     with pytest.raises(fv.FvError) as e:
         fv.Batch([pr.params])
