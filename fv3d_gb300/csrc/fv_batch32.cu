@@ -180,6 +180,10 @@ __global__ void FV_MIXED_BOUNDS batch_multi32(const BatchInst* __restrict__ inst
     __syncthreads();
     decided = true;
     if (!s_any) break;  // every CTA decides alike: no problem steps any more
+    // kind stays a run-time value, as in the per-stage kernel: a copy of the
+    // stage body specialised per kind may contract its multiply-adds
+    // differently and break the bit-for-bit equality with the per-stage form
+#pragma unroll 1
     for (int kind = STAGE_RK_1; kind <= STAGE_RK_2; ++kind) {
       for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         __syncthreads();  // the previous item is finished with s_inst and smem
