@@ -394,12 +394,15 @@ __device__ __forceinline__ void faces32(const Grid& G, const PV& V, int rs, int 
 // VF: the viscous fluxes of the face-only branches come from the shared face
 // arrays visc_faces filled (the split form), else every cell evaluates its
 // stencil (the fused form).
-template <int PLANE, bool WACT, class TL, bool VF, class PV>
-__device__ __forceinline__ void update32(const Grid& G, const PV& V, const MixedFields& M, float2* const src[5],
-                                         float2* const dst[5], int kind, float dt, int x0, int y0, int nr, int tid,
-                                         float& red, bool& bad) {
+// RK2: compiled for RK2 stage 2 (kind == STAGE_RK_2) or for the other two
+// kinds; update32 picks the copy, so the stage-2 copy can hold U^n from the
+// start of a cell's update without the other kinds paying its registers.
+template <int PLANE, bool WACT, class TL, bool VF, bool RK2, class PV>
+__device__ __forceinline__ void update32_kind(const Grid& G, const PV& V, const MixedFields& M, float2* const src[5],
+                                              float2* const dst[5], int kind, float dt, int x0, int y0, int nr,
+                                              int tid, float& red, bool& bad) {
   constexpr int TX = TL::TX;
-  const bool in_pairs = kind != STAGE_RK_2;
+  const bool in_pairs = !RK2;
   const float inv_db = PLANE == PLANE_XY ? G.inv_dy_f : G.inv_dz_f;
   const float dtdx = dt * G.inv_dx_f;
   const float dtdb = dt * inv_db;
@@ -415,8 +418,7 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
     // Sedov 256^2 against loading it where it is added)
     float2 un[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v)
-      un[v] = (kind == STAGE_RK_2 && (WACT || v != 3)) ? M.un[v][o] : make_float2(0.0f, 0.0f);
+    for (int v = 0; v < 5; ++v) un[v] = (RK2 && (WACT || v != 3)) ? M.un[v][o] : make_float2(0.0f, 0.0f);
     float du[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v)
@@ -475,7 +477,7 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
         du[sv] += (vf[0][var] + vf[1][var] + vf[2][var]) * dt;
       }
     }
-    if (kind == STAGE_RK_1) {
+    if (!RK2 && kind == STAGE_RK_1) {
       float us[5];
 #pragma unroll
       for (int v = 0; v < 4; ++v) us[v] = (v == 3 && !WACT) ? 0.0f : base[v].x + (base[v].y + du[v]);
@@ -496,7 +498,7 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
         continue;
       }
       float2 r;
-      if (kind == STAGE_RK_2) {
+      if (RK2) {
         r = pair_add(pair_add(un[v], base[v]), du[v]);
         r = make_float2(0.5f * r.x, 0.5f * r.y);
       } else {
@@ -509,6 +511,16 @@ __device__ __forceinline__ void update32(const Grid& G, const PV& V, const Mixed
     bad |= !(inv <= 3.0e38f);  // NaN / inf: reported through the error flag
     red = fmaxf(red, inv);
   }
+}
+
+template <int PLANE, bool WACT, class TL, bool VF, class PV>
+__device__ __forceinline__ void update32(const Grid& G, const PV& V, const MixedFields& M, float2* const src[5],
+                                         float2* const dst[5], int kind, float dt, int x0, int y0, int nr, int tid,
+                                         float& red, bool& bad) {
+  if (kind == STAGE_RK_2)
+    update32_kind<PLANE, WACT, TL, VF, true>(G, V, M, src, dst, kind, dt, x0, y0, nr, tid, red, bad);
+  else
+    update32_kind<PLANE, WACT, TL, VF, false>(G, V, M, src, dst, kind, dt, x0, y0, nr, tid, red, bad);
 }
 
 // Moves halo rows TY..TY+3 of the previous block to rows 0..3 (the rows the
