@@ -30,9 +30,11 @@
 
 #include "fv_tile64.cuh"
 
-// Cells whose loads one thread issues before converting any of them (phase 1).
+// Cells whose loads one thread issues before converting any of them (phase 1),
+// for (hi, lo) pair input.  Measured on shear 4096^2 / RT 512x1536 / Sedov
+// 256^2: 3 cells +1.8 / +1.1 / +0.7 % over 2; 4 spill.
 #ifndef FV_MIXED_LOAD_BATCH
-#define FV_MIXED_LOAD_BATCH 2
+#define FV_MIXED_LOAD_BATCH 3
 #endif
 // Minimum resident CTAs per SM requested from the register allocator
 // (0: no bound beyond the 256 threads of a tile).
@@ -298,10 +300,18 @@ __device__ __forceinline__ void face_flux32(const float c[4][5], int rs, bool pl
 // input (pairs or U*) -> FP32 primitives (and temperature).  Batches of KB
 // cells per thread: every load of a batch is issued before any of them is
 // used, to keep many requests in flight.
-template <int PLANE, bool WACT, class TL, class PV>
-__device__ __forceinline__ void load_prims32(const Grid& G, const MixedFields& M, float2* const src[5],
-                                             bool in_pairs, const PV& V, int x0, int y0, int h0, int h1, int tid) {
-  constexpr int HX = TL::HX, KB = FV_MIXED_LOAD_BATCH;
+// PAIRS: compiled for (hi, lo) pair input (FV_MIXED_LOAD_BATCH cells per
+// batch) or for U* input (4-byte values, half the registers:
+// FV_MIXED_LOAD_BATCH_STAR cells per batch; 4 against 2: +2.2 % on shear
+// 4096^2, 3 the same as 4).
+#ifndef FV_MIXED_LOAD_BATCH_STAR
+#define FV_MIXED_LOAD_BATCH_STAR 4
+#endif
+template <int PLANE, bool WACT, class TL, bool PAIRS, class PV>
+__device__ __forceinline__ void load_prims32_kind(const Grid& G, const MixedFields& M, float2* const src[5],
+                                                  const PV& V, int x0, int y0, int h0, int h1, int tid) {
+  constexpr int HX = TL::HX, KB = PAIRS ? FV_MIXED_LOAD_BATCH : FV_MIXED_LOAD_BATCH_STAR;
+  constexpr bool in_pairs = PAIRS;
   const float gm1 = G.gm1_f;
   const int ncell = (h1 - h0) * HX;
   for (int base = 0; base < ncell; base += KB * kTileThreads) {
@@ -345,6 +355,15 @@ __device__ __forceinline__ void load_prims32(const Grid& G, const MixedFields& M
       if (G.tc) V.temp(hy, hx) = q[4] / q[0];
     }
   }
+}
+
+template <int PLANE, bool WACT, class TL, class PV>
+__device__ __forceinline__ void load_prims32(const Grid& G, const MixedFields& M, float2* const src[5],
+                                             bool in_pairs, const PV& V, int x0, int y0, int h0, int h1, int tid) {
+  if (in_pairs)
+    load_prims32_kind<PLANE, WACT, TL, true>(G, M, src, V, x0, y0, h0, h1, tid);
+  else
+    load_prims32_kind<PLANE, WACT, TL, false>(G, M, src, V, x0, y0, h0, h1, tid);
 }
 
 // Phase 2: a faces of cell rows 0..nr-1 and b faces of face rows fb0..nr.
