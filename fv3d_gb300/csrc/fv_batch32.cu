@@ -21,8 +21,19 @@ namespace {
 struct MixedKernel {
   int tx, block_rows, vface;
 };
-constexpr MixedKernel kKernels32[] = {{32, 16, 0}, {64, 16, 0}, {32, 8, 0}, {64, 8, 0}, {32, 16, 1}, {64, 16, 1}};
-constexpr TileShape kShapes32[] = {{32, 32}, {64, 16}, {32, 16}, {64, 32}, {32, 16}, {64, 8}, {32, 32}, {64, 16}};
+// Block rows of the two block heights (cells per thread in the update: 2 and
+// 1 for 32-wide blocks).
+#ifndef FV_MIXED_BR_A
+#define FV_MIXED_BR_A 16
+#endif
+#ifndef FV_MIXED_BR_B
+#define FV_MIXED_BR_B 8
+#endif
+constexpr int kBrA = FV_MIXED_BR_A, kBrB = FV_MIXED_BR_B;
+constexpr MixedKernel kKernels32[] = {{32, kBrA, 0}, {64, kBrA, 0}, {32, kBrB, 0},
+                                      {64, kBrB, 0}, {32, kBrA, 1}, {64, kBrA, 1}};
+constexpr TileShape kShapes32[] = {{32, 2 * kBrA}, {64, kBrA},     {32, kBrA}, {64, 2 * kBrA},
+                                   {32, 2 * kBrB}, {64, kBrB},     {32, 2 * kBrA}, {64, kBrA}};
 constexpr int kKernelOf32[] = {0, 1, 0, 1, 2, 3, 4, 5};
 constexpr int kNumShapes32 = sizeof(kShapes32) / sizeof(kShapes32[0]);
 

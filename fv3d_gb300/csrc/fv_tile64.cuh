@@ -54,7 +54,6 @@ struct Tile {
   static constexpr int NFA_PAD = (NFA + 31) / 32 * 32;   // keeps each warp on one face kind
   static constexpr int NFB = TX * (TY + 1);              // b-faces
   static constexpr int CELLS = TX * TY;
-  static_assert(CELLS % kTileThreads == 0, "tile cells must split evenly over the threads");
 };
 
 // Shared-memory layout for NV stored variables of element type T:
