@@ -560,6 +560,10 @@ template <bool WACT, class TL, class PV>
 __device__ __forceinline__ bool stage_rows_tma(const TmaState* tin, const PV& V, unsigned long long* mbar,
                                                unsigned& phase, int x0, int y0, int h0, int h1, StepCtrl* ctrl) {
   constexpr int HX = TL::HX;
+  // a tensor copy's shared-memory destination must be 128-byte aligned: every
+  // chunk starts a whole number of chunks into the 128-byte aligned ring
+  static_assert((kTmaRows * HX * sizeof(double)) % 128 == 0, "TMA chunk of the ring not a multiple of 128 bytes");
+  static_assert(4 % kTmaRows == 0 && TL::TY % kTmaRows == 0, "TMA chunks must tile the ring's new rows");
   if (threadIdx.x == 0) {
     fence_proxy_async();
     const unsigned nf = WACT ? 5u : 4u;

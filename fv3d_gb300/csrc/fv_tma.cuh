@@ -19,7 +19,13 @@ struct TmaState {
   CUtensorMap m[5];
 };
 
-constexpr int kTmaRows = 4;  // rows per tensor copy (the ring's chunk)
+#ifndef FV_TMA_ROWS
+#define FV_TMA_ROWS 4
+#endif
+// rows per tensor copy (the ring's chunk): divides 4 and the tile height, and
+// a chunk of (TX + 4) doubles per row is a multiple of 128 bytes (the
+// alignment of a tensor copy's shared-memory destination)
+constexpr int kTmaRows = FV_TMA_ROWS;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
