@@ -387,9 +387,28 @@ int Autotune(fv_batch* b, Group& g) {
   std::vector<std::pair<int, int>> cand;
   int max_nc = 1;
   for (int i : g.members) max_nc = std::max(max_nc, b->G[i].nc);
-  if (d3)  // z layers per work item; a 4-layer prologue is converted per item
+  if (d3) {  // z layers per work item; a 4-layer prologue is converted per item
     for (int z : {8, 16, 32, 64})
       if (z == 8 || z <= max_nc) cand.push_back({0, z});
+    // and the chunk lengths that make the work items fill 1-4 rounds of the
+    // resident CTAs (the fewest layers with at most r rounds of items)
+    const long long slots = (long long)Occupancy(b, g, 0) * SmCount();
+    const int side = fv::batch3d_columns();
+    auto items = [&](int z) {
+      long long n = 0;
+      for (int i : g.members)
+        n += (long long)((b->G[i].na + side - 1) / side) * ((b->G[i].nb + side - 1) / side) *
+             ((b->G[i].nc + z - 1) / z);
+      return n;
+    };
+    for (int r = 1; r <= 4 && slots > 0; ++r) {
+      int z = 4;
+      while (z < max_nc && items(z) > r * slots) ++z;
+      bool dup = false;
+      for (auto& c : cand) dup = dup || c.second == z;
+      if (!dup && items(z) <= r * slots) cand.push_back({0, z});
+    }
+  }
   for (int s = 0; s < ns && !d3; ++s)
     if (visc || !ShapeSchedule(b, s).vface || b->precision == FV_PREC_FP64) cand.push_back({s, shapes[s].ty});
   for (int s = 0; s < ns && !d3; ++s) {
