@@ -14,12 +14,15 @@
 // groups as symbol tables -- a version-1 B-tree of symbol-table nodes plus a
 // local heap of names -- and contiguous datasets), the format libhdf5 writes
 // by default, which every HDF5 reader (h5py, HighFive, ParaView, VisIt)
-// opens.  Every object is written once where the file ends; a later save
-// appends its group and a new copy of the root group's symbol table (B-tree,
-// nodes and name heap), then rewrites the root group's symbol-table message
-// and the superblock in place to point at it (the old copy stays as unused
-// space).  Little-endian byte order throughout; offsets and lengths are
-// 8 bytes.
+// opens.  Every dataset and group is written once where the file ends.  The
+// root group's symbol table (name heap, nodes and B-tree), which grows by
+// one entry per save, lives in a region reserved for a capacity of entries
+// (twice what it holds when the region is made): a later save rewrites the
+// table in that region while it fits, else reserves a region twice as large
+// at the end of the file, then points the root group's symbol-table message
+// and the superblock at the new table.  The capacity is read back from the
+// name heap's size, whose unused tail is one free block.  Little-endian
+// byte order throughout; offsets and lengths are 8 bytes.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -183,6 +186,29 @@ struct Entry {
   uint64_t btree, heap;        // groups: their symbol table
 };
 
+// Where the pieces of a symbol table go: appended at the end of the file, or
+// into [at, end) of a reserved region.
+struct Sink {
+  bool append;
+  uint64_t at, end;
+};
+
+// The root table's reserved region for `cap` entries: name heap (header +
+// data segment of kHeapPerEntry bytes per entry, the "" at offset 0 and room
+// for a free block), then room for the most nodes and B-tree nodes `cap`
+// entries take.
+constexpr uint64_t kHeapPerEntry = 16;  // a name of up to 15 characters, NUL, 8-byte aligned
+uint64_t HeapData(uint64_t cap) { return 8 + kHeapPerEntry * cap + 16; }
+uint64_t RegionBytes(uint64_t cap) {
+  uint64_t nodes = std::max<uint64_t>(1, (cap + 2 * kLeafK - 1) / (2 * kLeafK));
+  uint64_t bytes = 32 + HeapData(cap) + nodes * kSnodBytes;
+  for (;;) {  // B-tree levels
+    nodes = (nodes + 2 * kNodeK - 1) / (2 * kNodeK);
+    bytes += nodes * kTreeBytes;
+    if (nodes == 1) return bytes;
+  }
+}
+
 class H5File {
  public:
   ~H5File() {
@@ -215,7 +241,18 @@ class H5File {
     }
     uint8_t st[16];
     if (!root_stab_ || !ReadAt(root_stab_, st, sizeof(st))) return false;
-    return ReadGroup(Rd64(st), Rd64(st + 8), &root_);
+    // the root table's region: its heap starts it; the heap's data size gives
+    // the capacity (a heap without a free block belongs to no region)
+    uint8_t hh[32];
+    const uint64_t heap = Rd64(st + 8);
+    if (!ReadAt(heap, hh, sizeof(hh))) return false;
+    const uint64_t data = Rd64(hh + 8), cap = data >= 24 ? (data - 24) / kHeapPerEntry : 0;
+    if (Rd64(hh + 16) != kHeapFreeNull && Rd64(hh + 24) == heap + 32 && HeapData(cap) == data &&
+        heap + RegionBytes(cap) <= eof_) {
+      region_at_ = heap;
+      region_cap_ = cap;
+    }
+    return ReadGroup(Rd64(st), heap, &root_);
   }
 
   uint64_t Append(const void* p, size_t n) {
@@ -251,9 +288,28 @@ class H5File {
     return Append(ObjectHeader(msgs));
   }
 
+  // Writes b at the sink's next position; *where receives its address.
+  bool Put(Sink& sink, const Bytes& b, uint64_t* where) {
+    if (sink.append) {
+      *where = Append(b);
+      return *where != kUndef;
+    }
+    const uint64_t n = (b.size() + 7) & ~uint64_t(7);
+    if (sink.at + n > sink.end || !WriteAt(sink.at, b.b.data(), b.size())) return false;
+    *where = sink.at;
+    sink.at += n;
+    return true;
+  }
+
   // The symbol table of a group with these members: name heap, nodes and
-  // B-tree; *btree and *heap receive their addresses.
+  // B-tree; *btree and *heap receive their addresses.  heap_data: the size
+  // of the heap's data segment (0: just the names; larger: the rest is one
+  // free block of at least 16 bytes).  False when the table does not fit.
   bool SymbolTableOf(std::vector<Entry> members, uint64_t* btree, uint64_t* heap) {
+    Sink sink{true, 0, 0};
+    return SymbolTableOf(std::move(members), btree, heap, sink, 0);
+  }
+  bool SymbolTableOf(std::vector<Entry> members, uint64_t* btree, uint64_t* heap, Sink& sink, uint64_t heap_data) {
     std::sort(members.begin(), members.end(), [](const Entry& a, const Entry& b) {
       return std::strcmp(a.name.c_str(), b.name.c_str()) < 0;
     });
@@ -266,16 +322,24 @@ class H5File {
       names.raw(e.name.c_str(), e.name.size() + 1);
       names.pad8();
     }
+    const uint64_t used = names.size();
+    if (heap_data != 0) {  // the unused tail as one free block: next (none), size
+      if (used + 16 > heap_data) return false;
+      names.u64(kHeapFreeNull);
+      names.u64(heap_data - used);
+      names.zeros(heap_data - used - 16);
+    }
     Bytes h;
     h.raw("HEAP", 4);
     h.u8(0);
     h.zeros(3);
     h.u64(names.size());
-    h.u64(kHeapFreeNull);
-    const uint64_t heap_at = eof_;
+    h.u64(heap_data != 0 ? used : kHeapFreeNull);
+    const uint64_t heap_at = sink.append ? eof_ : sink.at;
     h.u64(heap_at + 32);  // data segment right after the header
     h.raw(names.b.data(), names.size());
-    if (Append(h) != heap_at) return false;
+    uint64_t at_h;
+    if (!Put(sink, h, &at_h) || at_h != heap_at) return false;
     // symbol-table nodes of up to 2K entries, filled evenly
     const size_t n = members.size();
     const size_t nodes = std::max<size_t>(1, (n + 2 * kLeafK - 1) / (2 * kLeafK));
@@ -302,8 +366,8 @@ class H5File {
         }
       }
       node.zeros(kSnodBytes - node.size());
-      const uint64_t at = Append(node);
-      if (at == kUndef) return false;
+      uint64_t at;
+      if (!Put(sink, node, &at)) return false;
       child.push_back(at);
       key.push_back(last > first ? off[last - 1] : 0);
       first = last;
@@ -314,7 +378,8 @@ class H5File {
       const size_t m = child.size();
       const size_t groups = (m + 2 * kNodeK - 1) / (2 * kNodeK);
       std::vector<uint64_t> addr(groups);
-      for (size_t g = 0; g < groups; ++g) addr[g] = eof_ + g * (uint64_t)kTreeBytes;
+      const uint64_t base = sink.append ? eof_ : sink.at;
+      for (size_t g = 0; g < groups; ++g) addr[g] = base + g * (uint64_t)kTreeBytes;
       std::vector<uint64_t> up_child, up_key;
       size_t c0 = 0;
       for (size_t g = 0; g < groups; ++g) {
@@ -332,7 +397,8 @@ class H5File {
           t.u64(key[c]);
         }
         t.zeros(kTreeBytes - t.size());
-        if (Append(t) != addr[g]) return false;
+        uint64_t at_t;
+        if (!Put(sink, t, &at_t) || at_t != addr[g]) return false;
         up_child.push_back(addr[g]);
         up_key.push_back(key[c1 - 1]);
         c0 = c1;
@@ -376,9 +442,27 @@ class H5File {
     return WriteAt(0, s.b.data(), s.size());
   }
 
+  // The root table into its region (a new one, twice the entries, when it
+  // does not fit the current one).
+  bool RootTable(uint64_t* bt, uint64_t* hp) {
+    if (region_cap_ < root_.size() || !TryRegion(bt, hp)) {
+      region_cap_ = std::max<uint64_t>(64, 2 * root_.size());
+      const uint64_t bytes = RegionBytes(region_cap_);
+      const std::vector<uint8_t> zero(bytes, 0);
+      region_at_ = Append(zero.data(), zero.size());
+      if (region_at_ == kUndef) return false;
+      return TryRegion(bt, hp);
+    }
+    return true;
+  }
+  bool TryRegion(uint64_t* bt, uint64_t* hp) {
+    Sink sink{false, region_at_, region_at_ + RegionBytes(region_cap_)};
+    return SymbolTableOf(root_, bt, hp, sink, HeapData(region_cap_));
+  }
+
   bool WriteRoot(const std::vector<Msg>& attrs) {
     uint64_t bt, hp;
-    if (!SymbolTableOf(root_, &bt, &hp)) return false;
+    if (!RootTable(&bt, &hp)) return false;
     std::vector<Msg> msgs{SymbolTable(bt, hp)};
     msgs.insert(msgs.end(), attrs.begin(), attrs.end());
     std::vector<size_t> at;
@@ -391,7 +475,7 @@ class H5File {
   // Points the root group at a new symbol table holding root_.
   bool UpdateRoot() {
     uint64_t bt, hp;
-    if (!SymbolTableOf(root_, &bt, &hp)) return false;
+    if (!RootTable(&bt, &hp)) return false;
     Bytes st;
     st.u64(bt);
     st.u64(hp);
@@ -448,6 +532,7 @@ class H5File {
   FILE* f_ = nullptr;
   uint64_t eof_ = 0;
   uint64_t root_header_ = 0, root_stab_ = 0;
+  uint64_t region_at_ = 0, region_cap_ = 0;  // the root table's reserved region
 };
 
 }  // namespace

@@ -135,3 +135,30 @@ def test_python_save_solution(tmp_path):
         assert f["ite_1"].attrs["time"] == 0.5
     with pytest.raises(fv.FvError):
         fv.save_solution(p, tmp_path / "b.h5", 2, 0.0, q)
+
+
+def test_root_table_region_is_reused(tmp_path):
+    """The root group's symbol table is rewritten in its reserved region
+    (moved to a twice-larger one when full), so the file grows linearly with
+    the saves and a reopened file keeps using the region."""
+    p = fv.parse_ini("[mesh]\nNx=4\nNy=1\nNz=3\n[physics]\nproblem=sod_x\n")
+    path = tmp_path / "run.h5"
+    sizes = {}
+    for it in range(800):
+        fv.save_solution(p, path, it, float(it), [np.full((3, 1, 4), it + 0.5 * k) for k in range(5)])
+        if it + 1 in (200, 400, 800):
+            sizes[it + 1] = os.path.getsize(path)
+    # per-save growth stays flat (a fresh table per save would grow with the entries)
+    g1 = (sizes[400] - sizes[200]) / 200.0
+    g2 = (sizes[800] - sizes[400]) / 400.0
+    assert g2 < 1.25 * g1, sizes
+    f = snapshots.File(str(path))
+    assert len(f.keys()) == 803
+    for it in (0, 1, 399, 400, 799):
+        np.testing.assert_array_equal(f["ite_%d/v" % it], np.full((3, 1, 4), it + 1.0))
+        assert f["ite_%d" % it].attrs["time"] == float(it)
+    h = snapshots.H5File(str(path))
+    stab = [b for t, b in h.messages(h.root) if t == 0x11][0]
+    heap = struct.unpack("<QQ", stab)[1]
+    dsize, free_head, daddr = struct.unpack_from("<QQQ", h._m, heap + 8)
+    assert daddr == heap + 32 and free_head != 1 and free_head < dsize  # a free tail: room for more entries
