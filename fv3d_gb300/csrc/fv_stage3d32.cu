@@ -2,7 +2,7 @@
 //
 // The same z-marching organisation as the FP64 3-D kernel (fv_stage3d.cu): a
 // CTA owns a 16 x 16 block of columns and a chunk of z layers; a ring of four
-// layers of primitives sits in shared memory (FP32 here: 49 KB with
+// layers of primitives sits in shared memory (FP32 here: 51.6 KB with
 // conduction, 4 CTAs per SM); the x and y faces of layer k are solved while
 // layer k+2 is loaded; each thread solves the z face above its column and
 // updates its cell.  The arithmetic is that of the 2-D mixed form
