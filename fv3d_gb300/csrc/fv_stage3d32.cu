@@ -12,8 +12,9 @@
 // turned into dt in FP64 by the control kernel.  Every reference feature of
 // the 3-D FP64 kernel is kept: C91 ghosts, the well-balanced / C91 z-flux
 // overrides, gravity, fixed-temperature / fixed-gradient conduction
-// boundaries, viscosity with the reference's z-branch quirks (B02
-// conductivity runs on the FP64 handle only).  Built with fast-math.
+// boundaries, viscosity with the reference's z-branch quirks, and the
+// corrected physics as a template option (B02 conductivity runs on the FP64
+// handle only).  Built with fast-math.
 #include "fv_tile32.cuh"
 
 namespace fv {
